@@ -1,0 +1,271 @@
+"""Seeded synthetic workloads for the VisSat geometry path.
+
+The reference runs on WorldView-3 scenes of the MVS3DM benchmark.  None of that data
+is available offline, so every input here is drawn from fixed-seed distributions with
+the shapes, layouts and value ranges the reference sees:
+
+* RPC cameras shaped like the dictionaries ``lib/parse_meta.py`` produces and
+  ``RPCModel.__init__`` consumes (``lib/rpc_model.py:132-158``): ten offsets/scales,
+  four 20-term coefficient lists, image width and height.
+* lat/lon/alt sample grids laid out exactly like ``gen_grid`` (``lib/gen_grid.py:38-56``,
+  z-major, ``ij`` meshgrid inside a slab), with ENU coordinates about the grid centre
+  at the lowest altitude as ``coordinate_system.py:45-47`` chooses its origin.
+* height maps of a "box city" scene sampled through a per-view pixel->UTM affine map,
+  flattened into (easting, northing, height) point lists -- the layout
+  ``aggregate_2p5d_util.py:96-98`` hands to ``proj_to_grid``.
+
+Small cases are generated with numpy (bit-reproducible on any host); the large
+per-view point clouds use torch so that they can be generated directly in device memory.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from .geodesy import geodetic_to_enu
+
+BASE_SEED = 20261203
+
+# Explorer AOI of the MVS3DM benchmark (UTM zone 21 S), used as the UTM anchor so the
+# FP64 origin subtraction of the rasteriser sees realistic magnitudes.
+EXPLORER_UL_EASTING = 354052.3651180889
+EXPLORER_UL_NORTHING = 6182702.10540914
+
+
+# --------------------------------------------------------------------------------------
+# RPC cameras
+# --------------------------------------------------------------------------------------
+def make_rpc_meta(seed: int, width: int = 2048, height: int = 2048) -> dict:
+    """One synthetic RPC camera in the ``meta_dict`` format ``RPCModel`` takes.
+
+    Offsets: LAT_OFF~U(20,50) deg, LONG_OFF~U(-120,120) deg, HEIGHT_OFF~U(0,500) m;
+    LAT/LONG_SCALE = 0.05 deg, HEIGHT_SCALE = 500 m; LINE/SAMP_OFF = LINE/SAMP_SCALE =
+    half the image size.  The numerator linear terms are +-1 (+N(0,0.05)) on the RPC
+    slot of the matching axis (colNum[1] <- lon, rowNum[2] <- lat, north up), every other
+    numerator term N(0,1e-3); the denominators are 1 + N(0,1e-4) terms.
+    """
+    rng = np.random.default_rng(seed)
+    col_num = rng.normal(0.0, 1e-3, 20)
+    row_num = rng.normal(0.0, 1e-3, 20)
+    col_num[1] = 1.0 + rng.normal(0.0, 0.05)
+    row_num[2] = -1.0 + rng.normal(0.0, 0.05)
+    col_den = np.concatenate(([1.0], rng.normal(0.0, 1e-4, 19)))
+    row_den = np.concatenate(([1.0], rng.normal(0.0, 1e-4, 19)))
+    rpc = {
+        'rowOff': height / 2.0, 'rowScale': height / 2.0,
+        'colOff': width / 2.0, 'colScale': width / 2.0,
+        'latOff': float(rng.uniform(20.0, 50.0)), 'latScale': 0.05,
+        'lonOff': float(rng.uniform(-120.0, 120.0)), 'lonScale': 0.05,
+        'altOff': float(rng.uniform(0.0, 500.0)), 'altScale': 500.0,
+        'rowNum': [float(v) for v in row_num], 'rowDen': [float(v) for v in row_den],
+        'colNum': [float(v) for v in col_num], 'colDen': [float(v) for v in col_den],
+    }
+    return {'rpc': rpc, 'width': width, 'height': height}
+
+
+def grid_points(x_points: np.ndarray, y_points: np.ndarray, z_points: np.ndarray):
+    """3-D sample grid in the layout of ``lib/gen_grid.py:38-56``.
+
+    Points are z-major; inside one z slab the (x, y) pairs follow an ``ij`` meshgrid
+    flattened row-major.  Returns three (N, 1) float64 columns.
+    """
+    nx, ny, nz = x_points.size, y_points.size, z_points.size
+    slab_x = np.repeat(np.asarray(x_points, dtype=np.float64), ny)
+    slab_y = np.tile(np.asarray(y_points, dtype=np.float64), nx)
+    xx = np.tile(slab_x, nz).reshape(-1, 1)
+    yy = np.tile(slab_y, nz).reshape(-1, 1)
+    zz = np.repeat(np.asarray(z_points, dtype=np.float64), nx * ny).reshape(-1, 1)
+    return xx, yy, zz
+
+
+@dataclass
+class SampleGrid:
+    """A lat/lon/alt sample grid and its ENU coordinates, each (N, 1) float64."""
+    lat: np.ndarray
+    lon: np.ndarray
+    alt: np.ndarray
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    origin: tuple
+
+    @property
+    def n(self) -> int:
+        return self.lat.shape[0]
+
+
+def rpc_sample_grid(meta: dict, n_xy: int, n_z: int) -> SampleGrid:
+    """Grid over the camera's normalised cube [-1, 1]^3 converted to degrees and metres.
+
+    Latitude runs north to south and longitude west to east, as the northing/easting
+    linspaces of ``camera_approx.py:66-70`` do.  ENU is taken about the grid's centre
+    latitude/longitude at its lowest altitude (``coordinate_system.py:45-47``).
+    """
+    r = meta['rpc']
+    lat_pts = r['latOff'] + r['latScale'] * np.linspace(1.0, -1.0, n_xy)
+    lon_pts = r['lonOff'] + r['lonScale'] * np.linspace(-1.0, 1.0, n_xy)
+    alt_pts = r['altOff'] + r['altScale'] * np.linspace(-1.0, 1.0, n_z)
+    lat, lon, alt = grid_points(lat_pts, lon_pts, alt_pts)
+    lat0 = (lat_pts.min() + lat_pts.max()) / 2.0
+    lon0 = (lon_pts.min() + lon_pts.max()) / 2.0
+    alt0 = float(alt_pts.min())
+    x, y, z = geodetic_to_enu(lat, lon, alt, lat0, lon0, alt0)
+    return SampleGrid(lat, lon, alt, x, y, z, (lat0, lon0, alt0))
+
+
+def normalized_cube(seed: int, n: int):
+    """N points uniform over the normalised cube [-1, 1]^3 as float32 (x=lat, y=lon, z=alt)."""
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-1.0, 1.0, size=(3, n)).astype(np.float32)
+
+
+# --------------------------------------------------------------------------------------
+# Height-map scenes and per-view point clouds
+# --------------------------------------------------------------------------------------
+@dataclass
+class DsmGrid:
+    """DSM grid spec, the arguments of ``proj_to_grid`` (``lib/proj_to_grid.py:41``)."""
+    xoff: float      # upper-left easting
+    yoff: float      # upper-left northing
+    xres: float
+    yres: float
+    xsize: int
+    ysize: int
+
+
+@dataclass
+class Scene:
+    """A box-city scene: axis-aligned boxes in UTM over a flat ground at 0 m."""
+    grid: DsmGrid
+    boxes: np.ndarray   # (B, 5) float64: e0, e1, n0, n1, height (box covers e0<=E<e1, n0<=N<n1)
+    noise: float
+
+
+def make_scene(seed: int, grid: DsmGrid, n_boxes: int, h_lo: float, h_hi: float,
+               noise: float = 0.3) -> Scene:
+    rng = np.random.default_rng(seed)
+    w = grid.xsize * grid.xres
+    h = grid.ysize * grid.yres
+    side_e = rng.uniform(4.0, 40.0, n_boxes)
+    side_n = rng.uniform(4.0, 40.0, n_boxes)
+    ce = grid.xoff + rng.uniform(0.0, w, n_boxes)
+    cn = grid.yoff - rng.uniform(0.0, h, n_boxes)
+    hh = rng.uniform(h_lo, h_hi, n_boxes)
+    boxes = np.stack([ce - side_e / 2, ce + side_e / 2, cn - side_n / 2, cn + side_n / 2, hh], axis=1)
+    return Scene(grid, boxes, noise)
+
+
+@dataclass
+class ViewSpec:
+    """Pixel -> UTM affine map and corruption of one synthetic height map."""
+    height: int
+    width: int
+    gsd: float          # metres per pixel
+    theta: float        # rotation (radians)
+    shift_e: float      # per-view jitter of the UL corner (metres)
+    shift_n: float
+    nan_frac: float
+    seed: int
+
+
+def make_views(seed: int, scene: Scene, n_views: int, height: int, width: int,
+               nan_lo: float, nan_hi: float, jitter: float) -> list:
+    """Per-view specs whose footprint covers the scene's DSM grid."""
+    rng = np.random.default_rng(seed)
+    g = scene.grid
+    gsd = max(g.xsize * g.xres / width, g.ysize * g.yres / height)
+    views = []
+    for v in range(n_views):
+        views.append(ViewSpec(height, width, gsd,
+                              theta=float(rng.uniform(-0.03, 0.03)),
+                              shift_e=float(rng.uniform(-jitter, jitter)),
+                              shift_n=float(rng.uniform(-jitter, jitter)),
+                              nan_frac=float(rng.uniform(nan_lo, nan_hi)),
+                              seed=int(seed * 1000 + v)))
+    return views
+
+
+def view_points_torch(scene: Scene, view: ViewSpec, device='cpu'):
+    """(H*W, 3) float64 torch tensor of (easting, northing, height) for one view.
+
+    Each pixel is mapped to UTM by the view's affine map; its height is the tallest box
+    covering that location (0 m ground elsewhere) plus N(0, noise) and is NaN with
+    probability ``nan_frac``.  Rows follow the pixel raster, like the depth-map point
+    lists of ``aggregate_2p5d_util.py:75-98``.
+    """
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(view.seed)
+    H, W = view.height, view.width
+    g = scene.grid
+    f64 = torch.float64
+    jj = torch.arange(W, device=device, dtype=f64) + 0.5
+    ii = torch.arange(H, device=device, dtype=f64) + 0.5
+    c, s = math.cos(view.theta), math.sin(view.theta)
+    # rotate about the image centre so every view covers the grid
+    dj = (jj - W / 2.0)[None, :]
+    di = (ii - H / 2.0)[:, None]
+    ce = g.xoff + g.xsize * g.xres / 2.0 + view.shift_e
+    cn = g.yoff - g.ysize * g.yres / 2.0 + view.shift_n
+    east = ce + view.gsd * (c * dj - s * di)
+    north = cn - view.gsd * (s * dj + c * di)
+    height = torch.zeros((H, W), device=device, dtype=torch.float32)
+    boxes = torch.as_tensor(scene.boxes, device=device, dtype=f64)
+    # paint boxes through their pixel bounding windows (cheap: boxes are small)
+    inv = 1.0 / view.gsd
+    for b in range(boxes.shape[0]):
+        e0, e1, n0, n1, hb = scene.boxes[b].tolist()
+        corners = [(e0, n0), (e0, n1), (e1, n0), (e1, n1)]
+        pj, pi = [], []
+        for (e, n) in corners:
+            de, dn = (e - ce) * inv, (n - cn) * inv
+            # inverse of the rotation above
+            pj.append(c * de - s * dn + W / 2.0)
+            pi.append(-s * de - c * dn + H / 2.0)
+        j0 = max(int(math.floor(min(pj))) - 1, 0)
+        j1 = min(int(math.ceil(max(pj))) + 1, W)
+        i0 = max(int(math.floor(min(pi))) - 1, 0)
+        i1 = min(int(math.ceil(max(pi))) + 1, H)
+        if j0 >= j1 or i0 >= i1:
+            continue
+        ew = east[i0:i1, j0:j1]
+        nw = north[i0:i1, j0:j1]
+        inside = (ew >= e0) & (ew < e1) & (nw >= n0) & (nw < n1)
+        win = height[i0:i1, j0:j1]
+        win[inside] = torch.clamp(win[inside], min=float(hb))
+    noise = torch.randn((H, W), generator=gen, device=device, dtype=torch.float32) * scene.noise
+    height = height + noise
+    nan_mask = torch.rand((H, W), generator=gen, device=device) < view.nan_frac
+    height = torch.where(nan_mask, torch.full_like(height, float('nan')), height)
+    pts = torch.stack([east.reshape(-1), north.reshape(-1), height.reshape(-1).to(f64)], dim=1)
+    return pts.contiguous()
+
+
+def view_points(scene: Scene, view: ViewSpec) -> np.ndarray:
+    """numpy (H*W, 3) float64 point list of one view (CPU generation)."""
+    return view_points_torch(scene, view, 'cpu').numpy()
+
+
+# --------------------------------------------------------------------------------------
+# Named workloads
+# --------------------------------------------------------------------------------------
+def small_raster_case(seed: int = BASE_SEED):
+    """One 1024x1024 FP32 height map (40 boxes 5-60 m, N(0,0.3) noise, 15% NaN) rasterised
+    into a 0.5 m DSM anchored at the Explorer AOI's UL corner."""
+    grid = DsmGrid(EXPLORER_UL_EASTING, EXPLORER_UL_NORTHING, 0.5, 0.5, 1025, 1025)
+    scene = make_scene(seed + 1, grid, 40, 5.0, 60.0)
+    view = ViewSpec(1024, 1024, 0.5, theta=0.02, shift_e=0.0, shift_n=0.0, nan_frac=0.15,
+                    seed=seed + 2)
+    return scene, view
+
+
+def aoi50_raster_case(seed: int = BASE_SEED, n_views: int = 50, image: int = 4096,
+                      cells: int = 2000, res: float = 0.3):
+    """50 views of 4096x4096 FP32 height maps of one scene (300 boxes 3-80 m, 0.5 m view
+    jitter, 10-20% NaN) rasterised to a 2000x2000 grid at 0.3 m."""
+    grid = DsmGrid(EXPLORER_UL_EASTING, EXPLORER_UL_NORTHING, res, res, cells, cells)
+    scene = make_scene(seed + 11, grid, 300, 3.0, 80.0)
+    views = make_views(seed + 12, scene, n_views, image, image, 0.10, 0.20, 0.5)
+    return scene, views
