@@ -1,0 +1,434 @@
+"""Benchmark of the VisSat geometry path on GB300.
+
+Workload (one "step"): the 50-view AOI -- per view, an RPC camera of a 4096x4096 image
+projects a 200x200x20 lat/lon/alt grid and is fitted with a perspective camera (with its
+error statistics), and a 4096x4096 FP32 height map (16.8 M points) is rasterised to a
+2000x2000 DSM at 0.3 m (max-height binning, hole fill, 3x3 median blur); then the 50
+DSMs are fused (MAD-filtered mean, blur).  Inputs are synthetic (seeded), with the
+shapes and value ranges of the MVS3DM WorldView-3 data the reference runs on.
+
+Metric: DSM cells/s = fused cell-views (2000 x 2000 x 50) per second of the whole step;
+the RPC points/s of the same step is reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'RPC pts/s & DSM cells/s vs plain GPU at ≤1e-3 px; p50/p99 AOI latency'
+UNIT = 'DSM cells/s'
+
+
+# ------------------------------------------------------------------------------------
+# workload
+# ------------------------------------------------------------------------------------
+class Workload:
+    def __init__(self, views=50, image=4096, grid_xy=200, grid_z=20, cells=2000, res=0.3, seed=None):
+        from vissatsatellitestereo_gb300 import synth
+        self.seed = synth.BASE_SEED if seed is None else seed
+        self.views, self.image, self.cells, self.res = views, image, cells, res
+        self.grid_xy, self.grid_z = grid_xy, grid_z
+        self.metas = [synth.make_rpc_meta(self.seed + 1000 + v, image, image) for v in range(views)]
+        self.n_rpc = grid_xy * grid_xy * grid_z
+        self.scene, self.view_specs = synth.aoi50_raster_case(self.seed, views, image, cells, res)
+        self.n_raster = image * image
+
+    def describe(self):
+        return {'workload': f'aoi{self.views}: {self.views} views x (RPC {self.image}^2 image, '
+                            f'{self.grid_xy}x{self.grid_xy}x{self.grid_z} grid projection + perspective fit; '
+                            f'{self.image}^2 FP32 height map -> {self.cells}x{self.cells} DSM @{self.res} m) '
+                            f'+ {self.views}-view fusion',
+                'views': self.views, 'image_px': self.image, 'rpc_grid': [self.grid_xy, self.grid_xy, self.grid_z],
+                'raster_points_per_view': self.n_raster, 'dsm_cells': [self.cells, self.cells],
+                'dsm_resolution_m': self.res}
+
+    def rpc_grids(self, views=None):
+        from vissatsatellitestereo_gb300 import synth
+        views = range(self.views) if views is None else views
+        gs = [synth.rpc_sample_grid(self.metas[v], self.grid_xy, self.grid_z) for v in views]
+        return {f: np.stack([getattr(g, f).ravel() for g in gs]) for f in ('lat', 'lon', 'alt', 'x', 'y', 'z')}
+
+    @property
+    def cells_per_step(self):
+        return self.cells * self.cells * self.views
+
+    @property
+    def rpc_points_per_step(self):
+        return self.n_rpc * self.views
+
+
+# ------------------------------------------------------------------------------------
+# clocks
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.path = None
+        self.dev = device_index
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix='.csv')
+            os.close(fd)
+            self.proc = subprocess.Popen(['nvidia-smi', f'--id={self.dev}', f'--query-gpu={self.QUERY}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == 'active':
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': max(smax) if smax else None,
+                'samples': len(sm), 'reasons': sorted(reasons)}
+
+
+# ------------------------------------------------------------------------------------
+# our arm
+# ------------------------------------------------------------------------------------
+def launches_per_step(views):
+    camera = 1 + 1 + 1 + 1 + 1 + 1 + 1 + 1 + 4 * 2 + 1      # bbox init/bbox/norm/project+moments/solve/wh/err/sel-init/4x(hist,step)/final
+    raster = 2 + views * 4                                   # thresholds x2, per view: bin, zero init, zero first, epilogue
+    fusion = 2                                               # fuse + blur
+    return camera + raster + fusion
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group('nccl', device_id=torch.device(f'cuda:{local}'))
+    from vissatsatellitestereo_gb300.build import build
+    build()
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.camera_approx import approx_perspective_enu
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+
+    wl = Workload(views=args.views, image=args.image, cells=args.cells)
+    dev = torch.device('cuda')
+    # ---- inputs resident in HBM
+    g = wl.rpc_grids()
+    grid_t = {k: torch.from_numpy(v).to(dev) for k, v in g.items()}
+    n_pts = wl.n_raster
+    points = torch.empty((wl.views * n_pts, 3), dtype=torch.float64, device=dev)
+    for v, spec in enumerate(wl.view_specs):
+        points[v * n_pts:(v + 1) * n_pts] = synth.view_points_torch(wl.scene, spec, dev)
+    offsets = torch.arange(0, wl.views + 1, dtype=torch.int64, device=dev) * n_pts
+    G = wl.scene.grid
+    gargs = (G.xoff, G.yoff, G.xres, G.yres, G.xsize, G.ysize)
+    dsms = torch.empty((wl.views, G.ysize, G.xsize), dtype=torch.float32, device=dev)
+    fused = torch.empty((G.ysize, G.xsize), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def step(stage_events=None):
+        ev = stage_events
+        if ev: ev[0].record()
+        params, err, status = approx_perspective_enu(wl.metas, grid_t['lat'], grid_t['lon'], grid_t['alt'],
+                                                     grid_t['x'], grid_t['y'], grid_t['z'], mode='fast',
+                                                     shared_points=False)
+        if ev: ev[1].record()
+        dsm_from_points(points, offsets, *gargs, out=dsms)
+        if ev: ev[2].record()
+        fuse_dsms(dsms, median_blur=True, layout='vhw', out=fused)
+        if ev: ev[3].record()
+        return params, err, status
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stage_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record()
+    for k in range(args.steps):
+        params, err, status = step(stage_ev[k])
+    t1.record()
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    if world > 1:
+        tt = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    ms_per_step = elapsed / args.steps * 1e3
+    stages = {'camera_fit_ms': [], 'raster_ms': [], 'fusion_ms': []}
+    for ev in stage_ev:
+        stages['camera_fit_ms'].append(ev[0].elapsed_time(ev[1]))
+        stages['raster_ms'].append(ev[1].elapsed_time(ev[2]))
+        stages['fusion_ms'].append(ev[2].elapsed_time(ev[3]))
+    stages = {k: statistics.median(v) for k, v in stages.items()}
+    status_np = status.cpu().numpy()
+    value = wl.cells_per_step * args.steps * world / elapsed
+
+    # ---- roofline of the dominant stage (rasterisation: bin_max_kernel dominates it)
+    import json as _json
+    peaks = {}
+    pk_path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(pk_path):
+        peaks = _json.load(open(pk_path))
+    hbm_peak = float(peaks.get('hbm_gbs', 6800.0))
+    raster_bytes = wl.views * n_pts * 24 + wl.views * G.xsize * G.ysize * 4
+    raster_gbs = raster_bytes / (stages['raster_ms'] / 1e3) / 1e9
+    roofline = {'bound': 'hbm', 'kernel': 'raster stage (bin_max_kernel + dsm_epilogue_kernel per view)',
+                'achieved': round(raster_gbs, 1), 'peak': hbm_peak, 'unit': 'GB/s',
+                'frac': round(raster_gbs / hbm_peak, 4),
+                'peak_source': 'MEASURED_PEAKS.json hbm_gbs' if 'hbm_gbs' in peaks else 'fallback 6800 GB/s',
+                'algorithmic_bytes_per_step': raster_bytes, 'traffic': None}
+
+    result = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f64+f32', 'data': 'synthetic (seeded RPCs, box-city height maps)',
+        'config': dict(wl.describe(), l2='inputs (21 GB) exceed L2; no flush needed', parallelism='replicas'),
+        'rpc_pts_per_s': wl.rpc_points_per_step * args.steps * world / elapsed,
+        'raster_pts_per_s': wl.views * n_pts * args.steps * world / elapsed,
+        'stages_ms': stages, 'fit_status_ok': bool(np.all(status_np == 0)),
+        'roofline': roofline, 'clocks': clock_info, 'gpu_launches': launches_per_step(wl.views) * args.steps,
+    }
+
+    if rank == 0 and not args.skip_extra:
+        # ---- e2e: host (pinned) inputs through the public API, copies inside the timed region
+        host = {k: v.cpu().pin_memory() for k, v in grid_t.items()}
+        host_pts = torch.empty(points.shape, dtype=torch.float64, pin_memory=True)
+        host_pts.copy_(points)
+        host_off = offsets.cpu()
+        out_fused = torch.empty(fused.shape, dtype=torch.float32, pin_memory=True)
+        out_params = torch.empty((wl.views, 14), dtype=torch.float64, pin_memory=True)
+        out_err = torch.empty((wl.views, 6), dtype=torch.float64, pin_memory=True)
+        del points
+        torch.cuda.empty_cache()
+
+        def e2e_step():
+            p, e, s = approx_perspective_enu(wl.metas, host['lat'], host['lon'], host['alt'], host['x'], host['y'],
+                                             host['z'], mode='fast', shared_points=False)
+            d = dsm_from_points(host_pts, host_off, *gargs, out=dsms)
+            f = fuse_dsms(d, median_blur=True, layout='vhw', out=fused)
+            out_fused.copy_(f, non_blocking=True)
+            out_params.copy_(p, non_blocking=True)
+            out_err.copy_(e, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e_steps = max(1, min(args.steps, 3))
+        e0.record()
+        for _ in range(e_steps):
+            e2e_step()
+        e1.record()
+        torch.cuda.synchronize()
+        e_elapsed = e0.elapsed_time(e1) / 1e3
+        h2d = sum(v.numel() * v.element_size() for v in host.values()) + host_pts.numel() * 8 + host_off.numel() * 8
+        d2h = out_fused.numel() * 4 + out_params.numel() * 8 + out_err.numel() * 8
+        result['e2e'] = {'value': wl.cells_per_step * e_steps / e_elapsed, 'unit': UNIT,
+                         'ms_per_step': e_elapsed / e_steps * 1e3, 'steps': e_steps,
+                         'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
+                         'api': 'approx_perspective_enu + dsm_from_points + fuse_dsms on pinned host tensors'}
+        del host_pts
+        # ---- plain per-view GPU form (drop-in calls, one view at a time)
+        result['plain_per_view'] = plain_per_view(wl, grid_t, gargs, args)
+        # ---- CPU baseline (oracle, bounded sample)
+        result['cpu_baseline'] = cpu_baseline(wl, gargs, sample_views=1, pool=False)
+    if world > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result))
+
+
+def plain_per_view(wl, grid_t, gargs, args, n_views=None):
+    """The reference's structure on the GPU: per-view drop-in calls (exact projection,
+    single-view fit and error, proj_to_grid, blur), then fusion.  Timed over a subset of
+    views and scaled to the full step."""
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.check_error import perspective_error_batch
+    from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3, proj_to_grid
+    from vissatsatellitestereo_gb300.rpc_model import RPCModel
+    from vissatsatellitestereo_gb300.solve_perspective import solve_perspective_batch
+    n_views = n_views or min(8, wl.views)
+    dev = torch.device('cuda')
+    G = wl.scene.grid
+    pts = [synth.view_points_torch(wl.scene, wl.view_specs[v], dev) for v in range(n_views)]
+    dsms = torch.empty((wl.views, G.ysize, G.xsize), dtype=torch.float32, device=dev)
+
+    def one_view(v):
+        m = RPCModel(wl.metas[v])
+        col, row = m.projection(grid_t['lat'][v], grid_t['lon'][v], grid_t['alt'][v])
+        keep = (col >= 0) & (row >= 0) & (col < m.width) & (row < m.height)
+        K, R, t, st = solve_perspective_batch(grid_t['x'][v], grid_t['y'][v], grid_t['z'][v], col.view(1, -1),
+                                              row.view(1, -1), keep.view(1, -1))
+        perspective_error_batch(grid_t['x'][v], grid_t['y'][v], grid_t['z'][v], col.view(1, -1), row.view(1, -1),
+                                K, R, t, keep.view(1, -1))
+        dsm = proj_to_grid(pts[v], *gargs)
+        dsms[v] = median_blur3x3(dsm)
+
+    one_view(0)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e2 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for v in range(n_views):
+        one_view(v)
+    e1.record()
+    fuse_dsms(dsms, median_blur=True, layout='vhw')
+    e2.record()
+    torch.cuda.synchronize()
+    per_view = e0.elapsed_time(e1) / n_views / 1e3
+    step_s = per_view * wl.views + e1.elapsed_time(e2) / 1e3
+    return {'value': wl.cells_per_step / step_s, 'unit': UNIT, 'ms_per_step': step_s * 1e3,
+            'sample': f'{n_views} views timed, scaled to {wl.views}',
+            'form': 'per-view RPCModel(exact).projection, solve_perspective, check_perspective_error, '
+                    'proj_to_grid, medianBlur; then fuse_dsms'}
+
+
+# ------------------------------------------------------------------------------------
+# CPU baseline / reference arm (the oracle restatement of the reference, on host cores)
+# ------------------------------------------------------------------------------------
+def _cpu_raster_view(args):
+    scene, spec, gargs = args
+    from oracle import blur, raster
+    from vissatsatellitestereo_gb300 import synth
+    pts = synth.view_points(scene, spec)
+    t0 = time.perf_counter()
+    dsm = raster.proj_to_grid(pts, *gargs, loop=True)
+    blur.median_blur3x3(dsm.astype(np.float32))
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(wl, gargs, sample_views=1, pool=False, fusion_rows=100):
+    """Time the oracle on a bounded sample of the step and scale it to the full step."""
+    from oracle import blur, dlt, fuse, rpc
+    # camera fit: the reference loops over views in one process
+    g = wl.rpc_grids(range(sample_views))
+    t_cam = 0.0
+    for v in range(sample_views):
+        m = wl.metas[v]
+        t0 = time.perf_counter()
+        c, r = rpc.projection(m, g['lat'][v], g['lon'][v], g['alt'][v])
+        keep = rpc.in_image(m, c, r)
+        K, R, t = dlt.solve_perspective(g['x'][v], g['y'][v], g['z'][v], c, r, keep)
+        dlt.perspective_error(g['x'][v], g['y'][v], g['z'][v], c, r, K, R, t, keep)
+        t_cam += time.perf_counter() - t0
+    t_cam /= sample_views
+    # rasterisation: one process per view (the reference's multiprocessing pool)
+    cores = 1
+    jobs = [(wl.scene, wl.view_specs[v], gargs) for v in range(sample_views)]
+    if pool:
+        import multiprocessing as mp
+        cores = min(os.cpu_count() or 1, len(jobs))
+        ctx = mp.get_context('spawn')
+        with ctx.Pool(cores) as p:
+            times = p.map(_cpu_raster_view, jobs)      # each worker times its own view
+        wall = max(times)                              # one wave of `cores` concurrent views
+        t_ras_step = wall * math.ceil(wl.views / cores)
+    else:
+        t_ras = sum(_cpu_raster_view(j) for j in jobs) / len(jobs)
+        t_ras_step = t_ras * wl.views
+    # fusion on a band of rows, scaled to the grid
+    rng = np.random.default_rng(1)
+    band = rng.normal(20, 5, (fusion_rows, wl.cells, wl.views)).astype(np.float32)
+    band[rng.random(band.shape) < 0.15] = np.nan
+    t0 = time.perf_counter()
+    blur.median_blur3x3(fuse.fuse_numpy(band))
+    t_fuse = (time.perf_counter() - t0) * (wl.cells / fusion_rows)
+    step = t_cam * wl.views + t_ras_step + t_fuse
+    return {'value': wl.cells_per_step / step, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+            'est_step_s': step,
+            'sample': f'{sample_views} view(s) of projection+fit+error and of rasterisation (loop hole fill, '
+                      f'blur), fusion on {fusion_rows} of {wl.cells} rows; scaled to {wl.views} views'}
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    wl = Workload(views=args.views, image=args.image, cells=args.cells)
+    G = wl.scene.grid
+    gargs = (G.xoff, G.yoff, G.xres, G.yres, G.xsize, G.ysize)
+    ncpu = os.cpu_count() or 1
+    vals = []
+    t_start = time.perf_counter()
+    for _ in range(args.warmup + args.steps):
+        vals.append(cpu_baseline(wl, gargs, sample_views=min(ncpu, wl.views) if args.full_pool else 1,
+                                 pool=True, fusion_rows=50))
+        if time.perf_counter() - t_start > 240:
+            break
+    timed = vals[args.warmup:] or vals[-1:]
+    step_s = statistics.median(v['est_step_s'] for v in timed)
+    value = wl.cells_per_step / step_s
+    cb = dict(timed[-1], value=value)
+    print(json.dumps({'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': 1,
+                      'steps': len(timed), 'warmup': args.warmup, 'ms_per_step': step_s * 1e3,
+                      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64+f32',
+                      'data': 'synthetic', 'config': wl.describe(), 'cpu_baseline': cb,
+                      'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', choices=['ours', 'reference'], default='ours')
+    ap.add_argument('--views', type=int, default=50)
+    ap.add_argument('--image', type=int, default=4096)
+    ap.add_argument('--cells', type=int, default=2000)
+    ap.add_argument('--skip-extra', action='store_true', help='only the device-timed value')
+    ap.add_argument('--full-pool', action='store_true', help='reference arm: one view per host core')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,161 @@
+/*
+ * vissat_gb300.h -- C ABI of the GB300 (sm_103a) geometry path of VisSat satellite stereo.
+ *
+ * Every entry point:
+ *   - is plain C (extern "C"), takes device pointers, sizes and a cudaStream_t passed as
+ *     void* (NULL = legacy default stream), and never throws;
+ *   - returns an int status (VS_OK = 0) and records a message for vs_last_error();
+ *   - is asynchronous on the given stream (results are valid after the stream is
+ *     synchronised); device-side per-problem failures are written to a caller buffer;
+ *   - allocates no device memory: scratch comes from a caller-provided workspace whose
+ *     size the matching *_workspace_size() function reports.
+ * Calls on different streams may run concurrently; calls sharing a workspace must be
+ * ordered by the caller.
+ *
+ * Each function names the reference routine it replaces (paths relative to the
+ * VisSatSatelliteStereo repository).
+ */
+#ifndef VISSAT_GB300_H
+#define VISSAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define VS_OK 0
+#define VS_ERR_ARG 1        /* invalid argument: null pointer, negative size, bad enum */
+#define VS_ERR_CUDA 2       /* a CUDA runtime call or kernel launch failed */
+#define VS_ERR_WORKSPACE 3  /* caller workspace smaller than *_workspace_size() */
+#define VS_ERR_FACTORIZE 4  /* per-view: factorisation check failed (the reference asserts) */
+#define VS_ERR_DEGENERATE 5 /* per-view: fewer than 6 kept points / singular system */
+
+/* ---- data types ------------------------------------------------------------------ */
+
+/* One RPC camera (RPC00B): the fields RPCModel.__init__ reads from meta_dict
+ * (lib/rpc_model.py:132-158).  Coefficients follow the RPC monomial order with
+ * x = normalised latitude, y = longitude, z = altitude (lib/rpc_model.py:40-63). */
+typedef struct VsRpcCamera {
+    double row_off, row_scale, col_off, col_scale;
+    double lat_off, lat_scale, lon_off, lon_scale, alt_off, alt_scale;
+    double row_num[20], row_den[20], col_num[20], col_den[20];
+    double width, height;
+} VsRpcCamera;
+
+/* Projection arithmetic. */
+#define VS_PROJ_EXACT 0   /* FP64 in the reference's operation order: bit-identical results */
+#define VS_PROJ_FAST 1    /* compensated FP32 (double-float) evaluation, |err| < 1e-4 px   */
+
+/* Layouts of a stack of per-view DSMs. */
+#define VS_LAYOUT_HWV 0   /* [H][W][V]: the reference's np.concatenate(all_dsm, axis=2)   */
+#define VS_LAYOUT_VHW 1   /* [V][H][W]: one plane per view                                 */
+
+/* Length of the per-view camera parameter vector:
+ * [w, h, fx, fy, cx, cy, s, qw, qx, qy, qz, tx, ty, tz] (camera_approx.py:178-182). */
+#define VS_CAMERA_PARAMS 14
+/* Length of the per-view error vector: mean/median/max reprojection error (px) and
+ * mean/median/max inverse-projection error (m) (lib/check_error.py:121). */
+#define VS_ERROR_STATS 6
+
+/* ---- library ----------------------------------------------------------------------- */
+const char *vs_version(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *vs_last_error(void);
+
+/* ---- (a) RPC projection ------------------------------------------------------------ */
+
+/* Replaces RPCModel.projection (lib/rpc_model.py:160-168), for n_cams cameras at once.
+ * cams: device array of n_cams cameras.  lat/lon/alt: device FP64 arrays; camera c reads
+ * its n points at lat + c*point_stride (point_stride 0: one point set shared by all).
+ * col/row: device FP64 outputs [n_cams][n].  keep (nullable): device uint8 [n_cams][n],
+ * the in-image mask of camera_approx.py:170-174.  mode: VS_PROJ_EXACT or VS_PROJ_FAST. */
+int vs_rpc_project(const VsRpcCamera *cams, int n_cams, const double *lat, const double *lon,
+                   const double *alt, int64_t n, int64_t point_stride, double *col, double *row,
+                   uint8_t *keep, int mode, void *stream);
+
+/* ---- (b) perspective fit ------------------------------------------------------------ */
+
+/* Replaces solve_perspective (lib/solve_perspective.py:82-126) and its factorize
+ * (:38-79) for n_views independent problems.  x/y/z: device FP64 ENU points, view v at
+ * x + v*xyz_stride (0: shared).  col/row: device FP64 [n_views][n].  keep (nullable):
+ * device uint8 [n_views][n].  Outputs (device, row-major FP64): K [n_views][9],
+ * R [n_views][9], t [n_views][3]; status (device int32 [n_views]): VS_OK,
+ * VS_ERR_FACTORIZE or VS_ERR_DEGENERATE. */
+size_t vs_dlt_fit_workspace_size(int n_views, int64_t n);
+int vs_dlt_fit(const double *x, const double *y, const double *z, int64_t xyz_stride,
+               const double *col, const double *row, const uint8_t *keep, int n_views, int64_t n,
+               double *K, double *R, double *t, int32_t *status, void *workspace,
+               size_t workspace_bytes, void *stream);
+
+/* Replaces check_perspective_error (lib/check_error.py:37-121): per view the
+ * mean/median/max pixel reprojection error and mean/median/max inverse-projection error
+ * of camera K[R|t] over the kept points.  err: device FP64 [n_views][6]. */
+size_t vs_perspective_error_workspace_size(int n_views, int64_t n);
+int vs_perspective_error(const double *x, const double *y, const double *z, int64_t xyz_stride,
+                         const double *col, const double *row, const uint8_t *keep, int n_views,
+                         int64_t n, const double *K, const double *R, const double *t, double *err,
+                         void *workspace, size_t workspace_bytes, void *stream);
+
+/* Replaces the per-view loop of CameraApprox.approx_perspective_enu
+ * (camera_approx.py:166-189): projection of the lat/lon/alt grid through each RPC
+ * camera, in-image mask, DLT fit, factorisation, quaternion and error statistics, for
+ * all views in one call.  Points of view v at lat + v*point_stride (0: shared grid, as in
+ * the reference).  params: device FP64 [n_views][14]; err: device FP64 [n_views][6]
+ * (nullable: skip the statistics); status: device int32 [n_views]. */
+size_t vs_camera_approx_workspace_size(int n_views, int64_t n);
+int vs_camera_approx_perspective(const VsRpcCamera *cams, int n_views, const double *lat,
+                                 const double *lon, const double *alt, const double *x,
+                                 const double *y, const double *z, int64_t n,
+                                 int64_t point_stride, int proj_mode, double *params, double *err,
+                                 int32_t *status, void *workspace, size_t workspace_bytes,
+                                 void *stream);
+
+/* ---- (c) rasterisation ----------------------------------------------------------------- */
+
+/* Replaces proj_to_grid (lib/proj_to_grid.py:41-81): FP64 binning of (easting, northing,
+ * height) points, per-cell nanmax of the heights and the non-propagating 3x3 median hole
+ * fill.  points: device FP64 [n][3] row-major.  dsm: device FP64 [ysize][xsize].
+ * Bit-identical to the reference (NaN payloads aside). */
+size_t vs_proj_to_grid_workspace_size(int64_t xsize, int64_t ysize);
+int vs_proj_to_grid(const double *points, int64_t n, double xoff, double yoff, double xresolution,
+                    double yresolution, int64_t xsize, int64_t ysize, double *dsm, void *workspace,
+                    size_t workspace_bytes, void *stream);
+
+/* 3x3 median blur with replicated borders, the cv2.medianBlur(img, 3) calls of
+ * produce_dsm.py:58 and aggregate_2p5d.py:81 (NaN ordered after every number).
+ * n_img images of [h][w]; the _f64 variant first rounds FP64 input to float32
+ * (dsm.astype(np.float32)). */
+int vs_median_blur3x3_f32(const float *in, float *out, int64_t h, int64_t w, int64_t n_img,
+                          void *stream);
+int vs_median_blur3x3_f64(const double *in, float *out, int64_t h, int64_t w, int64_t n_img,
+                          void *stream);
+
+/* Batched form of produce_dsm_from_points (produce_dsm.py:46-58) over n_views point
+ * clouds on one DSM grid: proj_to_grid then the float32 3x3 median blur per view.
+ * points: device FP64 [total][3]; offsets: device int64 [n_views+1] (view v owns rows
+ * offsets[v] .. offsets[v+1]-1).  dsm: device float32 [n_views][ysize][xsize]. */
+size_t vs_dsm_from_points_workspace_size(int n_views, int64_t xsize, int64_t ysize);
+int vs_dsm_from_points(const double *points, const int64_t *offsets, int n_views, double xoff,
+                       double yoff, double xresolution, double yresolution, int64_t xsize,
+                       int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
+                       void *stream);
+
+/* ---- (d) fusion ----------------------------------------------------------------------- */
+
+/* Replaces the fusion block of run_fuse (aggregate_2p5d.py:65-81): per cell, reject
+ * cells with <= 2 valid views, nanmedian, MAD rejection, nanmean (numpy's float32
+ * pairwise order), then the 3x3 median blur when median_blur != 0.  dsm: device
+ * float32 stack in `layout`; out: device float32 [h][w].  Bit-identical to the
+ * reference's numpy arithmetic (NaN payloads aside). */
+size_t vs_fuse_dsms_workspace_size(int64_t h, int64_t w);
+int vs_fuse_dsms(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
+                 int median_blur, void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VISSAT_GB300_H */

@@ -1,0 +1,54 @@
+"""The C ABI: the library builds/loads and exports every symbol the header declares (CPU)."""
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, 'include', 'vissat_gb300.h')).read()
+    txt = re.sub(r'/\*.*?\*/', '', txt, flags=re.S)
+    return sorted(set(re.findall(r'\b(vs_\w+)\s*\(', txt)))
+
+
+def test_header_declares_the_boundary():
+    syms = header_symbols()
+    for name in ('vs_rpc_project', 'vs_dlt_fit', 'vs_perspective_error', 'vs_camera_approx_perspective',
+                 'vs_proj_to_grid', 'vs_dsm_from_points', 'vs_median_blur3x3_f32', 'vs_fuse_dsms'):
+        assert name in syms
+
+
+def test_library_exports_every_declared_symbol():
+    from vissatsatellitestereo_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from vissatsatellitestereo_gb300.build import build
+        build()
+    lib = _lib.lib()
+    for name in header_symbols():
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f'{name} has no ctypes signature'
+    assert lib.vs_version().decode().startswith('vissat-gb300')
+
+
+def test_workspace_queries_need_no_gpu():
+    from vissatsatellitestereo_gb300 import _lib
+    lib = _lib.lib()
+    assert lib.vs_proj_to_grid_workspace_size(2000, 2000) >= 2000 * 2000 * 8
+    assert lib.vs_fuse_dsms_workspace_size(10, 10) >= 400
+    assert lib.vs_dlt_fit_workspace_size(0, 10) == 0
+    assert lib.vs_camera_approx_workspace_size(50, 800000) > 50 * 800000 * 16
+
+
+def test_camera_array_layout():
+    from vissatsatellitestereo_gb300 import _lib, synth
+    meta = synth.make_rpc_meta(1, 4096, 2048)
+    a = _lib.camera_array([meta, meta])
+    assert a.shape == (2, _lib.CAMERA_DOUBLES)
+    r = meta['rpc']
+    assert a[0, 0] == r['rowOff'] and a[0, 3] == r['colScale'] and a[0, 10] == r['rowNum'][0]
+    assert a[0, 50] == r['colNum'][0] and a[0, 70] == r['colDen'][0] and a[0, 90] == 4096 and a[0, 91] == 2048
+    with pytest.raises(ValueError):
+        bad = dict(meta, rpc=dict(r, rowNum=r['rowNum'][:19]))
+        _lib.camera_array([bad])

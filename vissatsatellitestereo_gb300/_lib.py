@@ -1,0 +1,110 @@
+"""ctypes binding of libvissat_gb300.so (the C ABI declared in include/vissat_gb300.h).
+
+The shared library is the product: there is no CPU fallback.  Loading fails loudly if
+the library has not been built (``python -m vissatsatellitestereo_gb300.build``), and
+every call raises ``VsError`` with the library's message on a non-zero status.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'libvissat_gb300.so')
+
+VS_OK = 0
+VS_ERR_ARG = 1
+VS_ERR_CUDA = 2
+VS_ERR_WORKSPACE = 3
+VS_ERR_FACTORIZE = 4
+VS_ERR_DEGENERATE = 5
+
+VS_PROJ_EXACT = 0
+VS_PROJ_FAST = 1
+VS_LAYOUT_HWV = 0
+VS_LAYOUT_VHW = 1
+VS_CAMERA_PARAMS = 14
+VS_ERROR_STATS = 6
+
+# VsRpcCamera: 92 doubles in declaration order
+CAMERA_DOUBLES = 92
+
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+_dbl = ctypes.c_double
+_sz = ctypes.c_size_t
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    'vs_version': (ctypes.c_char_p, []),
+    'vs_last_error': (ctypes.c_char_p, []),
+    'vs_rpc_project': (_int, [_vp, _int, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
+    'vs_dlt_fit_workspace_size': (_sz, [_int, _i64]),
+    'vs_dlt_fit': (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _int, _i64, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    'vs_perspective_error_workspace_size': (_sz, [_int, _i64]),
+    'vs_perspective_error': (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _int, _i64, _vp, _vp, _vp, _vp, _vp,
+                                    _sz, _vp]),
+    'vs_camera_approx_workspace_size': (_sz, [_int, _i64]),
+    'vs_camera_approx_perspective': (_int, [_vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _int, _vp,
+                                            _vp, _vp, _vp, _sz, _vp]),
+    'vs_proj_to_grid_workspace_size': (_sz, [_i64, _i64]),
+    'vs_proj_to_grid': (_int, [_vp, _i64, _dbl, _dbl, _dbl, _dbl, _i64, _i64, _vp, _vp, _sz, _vp]),
+    'vs_median_blur3x3_f32': (_int, [_vp, _vp, _i64, _i64, _i64, _vp]),
+    'vs_median_blur3x3_f64': (_int, [_vp, _vp, _i64, _i64, _i64, _vp]),
+    'vs_dsm_from_points_workspace_size': (_sz, [_int, _i64, _i64]),
+    'vs_dsm_from_points': (_int, [_vp, _vp, _int, _dbl, _dbl, _dbl, _dbl, _i64, _i64, _vp, _vp, _sz, _vp]),
+    'vs_fuse_dsms_workspace_size': (_sz, [_i64, _i64]),
+    'vs_fuse_dsms': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp, _sz, _vp]),
+}
+
+
+class VsError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f'vissat-gb300 status {status}: {message}')
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """The loaded library (loaded on first use)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f'{LIB_PATH} is missing: build it with '
+                              '`python -m vissatsatellitestereo_gb300.build` (needs nvcc)')
+        handle = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+def check(status):
+    if status != VS_OK:
+        raise VsError(status, lib().vs_last_error().decode())
+
+
+def call(name, *args):
+    check(getattr(lib(), name)(*args))
+
+
+def camera_array(meta_dicts):
+    """(C, 92) float64 rows in VsRpcCamera field order from reference meta_dicts."""
+    rows = []
+    for m in meta_dicts:
+        r = m['rpc']
+        row = [r['rowOff'], r['rowScale'], r['colOff'], r['colScale'], r['latOff'], r['latScale'],
+               r['lonOff'], r['lonScale'], r['altOff'], r['altScale']]
+        for key in ('rowNum', 'rowDen', 'colNum', 'colDen'):
+            coeffs = [float(c) for c in r[key]]
+            if len(coeffs) != 20:
+                raise ValueError(f'{key} must hold 20 coefficients, got {len(coeffs)}')
+            row += coeffs
+        row += [float(m['width']), float(m['height'])]
+        rows.append(row)
+    arr = np.asarray(rows, dtype=np.float64).reshape(-1, CAMERA_DOUBLES)
+    return np.ascontiguousarray(arr)

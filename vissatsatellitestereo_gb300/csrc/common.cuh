@@ -1,0 +1,131 @@
+// Shared helpers of the sm_103a geometry kernels: status handling, launch geometry,
+// double-float (compensated FP32) arithmetic and order-preserving integer keys.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/vissat_gb300.h"
+
+namespace vs {
+
+// ---- host-side error reporting ------------------------------------------------------
+void set_error(const char *fmt, ...);
+int check_launch(const char *what);          // VS_OK or VS_ERR_CUDA after a launch
+
+#define VS_REQUIRE(cond, ...)            \
+    do {                                 \
+        if (!(cond)) {                   \
+            ::vs::set_error(__VA_ARGS__); \
+            return VS_ERR_ARG;           \
+        }                                \
+    } while (0)
+
+#define VS_LAUNCH_CHECK(what)                         \
+    do {                                              \
+        int _st = ::vs::check_launch(what);           \
+        if (_st != VS_OK) return _st;                 \
+    } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Number of SMs of the current device (152 on GB300), cached per process.
+int sm_count();
+
+// Carves aligned sub-buffers out of a caller workspace.
+struct Carver {
+    char *base;
+    size_t used = 0;
+    explicit Carver(void *p) : base(static_cast<char *>(p)) {}
+    template <typename T>
+    T *take(size_t count) {
+        used = (used + 255) & ~size_t(255);
+        T *p = reinterpret_cast<T *>(base ? base + used : nullptr);
+        used += count * sizeof(T);
+        return p;
+    }
+};
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---- double-float arithmetic ---------------------------------------------------------
+// A value hi + lo with |lo| <= ulp(hi)/2 carried in two floats (about 48 significant
+// bits).  Error-free transformations after Knuth (TwoSum) and Dekker (TwoProduct with
+// an FMA); the file is compiled without fast-math so the compiler keeps their order.
+struct df {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
+    float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ df two_prod(float a, float b) {
+    float p = a * b;
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+    df s = two_sum(a.hi, b.hi);
+    df t = two_sum(a.lo, b.lo);
+    s.lo += t.hi;
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo += t.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df df_add_f(df a, float b) {
+    df s = two_sum(a.hi, b);
+    s.lo += a.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df df_mul(df a, df b) {
+    df p = two_prod(a.hi, b.hi);
+    p.lo = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
+    return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+    df p = two_prod(a.hi, b);
+    p.lo = __fmaf_rn(a.lo, b, p.lo);
+    return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ df df_div(df a, df b) {
+    float q1 = __fdiv_rn(a.hi, b.hi);
+    df p = df_mul_f(b, q1);
+    df r = df_add(a, {-p.hi, -p.lo});
+    float q2 = __fdiv_rn(r.hi, b.hi);
+    return fast_two_sum(q1, q2);
+}
+__host__ __device__ inline df df_from_double(double v) {
+    float hi = static_cast<float>(v);
+    return {hi, static_cast<float>(v - static_cast<double>(hi))};
+}
+__device__ __forceinline__ double df_to_double(df a) {
+    return static_cast<double>(a.hi) + static_cast<double>(a.lo);
+}
+
+// ---- order-preserving keys --------------------------------------------------------------
+// Unsigned keys whose integer order is the numeric order of the float value; key 0 is
+// reserved for "no value" (it would decode to a NaN).
+__device__ __forceinline__ unsigned long long key_from_double(double v) {
+    unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double double_from_key(unsigned long long k) {
+    unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double(static_cast<long long>(b));
+}
+__device__ __forceinline__ unsigned key_from_float(float v) {
+    unsigned b = __float_as_uint(v);
+    return (b >> 31) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float float_from_key(unsigned k) {
+    unsigned b = (k >> 31) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(b);
+}
+
+}  // namespace vs

@@ -1,0 +1,272 @@
+// (d) Fusion of per-view DSMs: the inline block of run_fuse (aggregate_2p5d.py:65-81).
+//
+// Per cell over the V views (float32, NaN = no measurement):
+//   n = #valid; n <= 2 -> NaN                                    (aggregate_2p5d.py:69-71)
+//   med = nanmedian: sorted s, ((0 + s[(n-1)/2]) + s[n/2]) / 2    (:74, numpy masked median)
+//   mad = nanmedian(|x - med|)                                    (:75)
+//   drop x with |x - med| > mad                                   (:76-77)
+//   mean = nanmean: NaN -> 0, numpy's float32 pairwise sum over the V slots in view order
+//          (8 accumulators for 8 <= V <= 128, halving above), started from 0, then the
+//          float32 division by the kept count                     (:78)
+// then optionally the 3x3 median blur (:81), launched from raster.cu's blur kernel.
+//
+// One thread owns one cell; the V values live in registers (V padded to a power of two,
+// template parameter) and are sorted with a bitonic network on order-preserving integer
+// keys (NaN -> all ones, so missing values sort last).  Views beyond 64 use a
+// local-memory path with the same arithmetic.
+#include <algorithm>
+#include <math.h>
+
+#include "common.cuh"
+
+namespace vs {
+int launch_blur_f32(const float *in, float *out, long long h, long long w, cudaStream_t st);
+
+namespace {
+
+constexpr unsigned kMissing = 0xffffffffu;
+
+__device__ __forceinline__ unsigned fkey(float v) { return isnan(v) ? kMissing : key_from_float(v); }
+
+template <int N>
+__device__ __forceinline__ void bitonic_sort(unsigned (&a)[N]) {
+#pragma unroll
+    for (int k = 2; k <= N; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned lo = min(a[i], a[l]), hi = max(a[i], a[l]);
+                    if ((i & k) == 0) { a[i] = lo; a[l] = hi; }
+                    else { a[i] = hi; a[l] = lo; }
+                }
+            }
+}
+
+// select sorted[idx] with compile-time indexing (keeps the array in registers)
+template <int N>
+__device__ __forceinline__ unsigned pick(const unsigned (&a)[N], int idx) {
+    unsigned r = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) r = (i == idx) ? a[i] : r;
+    return r;
+}
+
+__device__ __forceinline__ float median_of_sorted(unsigned lo_key, unsigned hi_key) {
+    const float lo = float_from_key(lo_key), hi = float_from_key(hi_key);
+    return __fdiv_rn(__fadd_rn(__fadd_rn(0.0f, lo), hi), 2.0f);
+}
+
+// numpy float32 pairwise sum of the first V entries of x (V <= 128), plus the outer 0.
+template <int N>
+__device__ __forceinline__ float numpy_sum(const float (&x)[N], int V) {
+    float res;
+    if (V < 8) {
+        res = 0.0f;
+#pragma unroll
+        for (int i = 0; i < (N < 8 ? N : 8); ++i)
+            if (i < V) res = __fadd_rn(res, x[i]);
+    } else {
+        float r[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) r[j] = (j < N) ? x[j] : 0.0f;
+        const int full = V - (V % 8);
+#pragma unroll
+        for (int b = 8; b < N; b += 8)
+            if (b < full)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], x[(b + j) < N ? b + j : 0]);
+        res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
+                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
+#pragma unroll
+        for (int i = 8; i < N; ++i)
+            if (i >= full && i < V) res = __fadd_rn(res, x[i]);
+    }
+    return __fadd_rn(0.0f, res);
+}
+
+template <int N>
+__device__ float fuse_cell(const float (&x)[N], int V) {
+    unsigned k[N];
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        k[i] = (i < V) ? fkey(x[i]) : kMissing;
+        n += (k[i] != kMissing);
+    }
+    if (n <= 2) return __int_as_float(0x7fffffff);
+    bitonic_sort(k);
+    const float med = median_of_sorted(pick(k, (n - 1) >> 1), pick(k, n >> 1));
+    // deviations |x - med| of the valid values; NaN deviations (inf - inf) are missing
+    unsigned dk[N];
+    int nd = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        float d = (i < V && !isnan(x[i])) ? fabsf(__fsub_rn(x[i], med)) : __int_as_float(0x7fffffff);
+        dk[i] = fkey(d);
+        nd += (dk[i] != kMissing);
+    }
+    float mad = __int_as_float(0x7fffffff);
+    if (nd > 0) {
+        bitonic_sort(dk);
+        mad = median_of_sorted(pick(dk, (nd - 1) >> 1), pick(dk, nd >> 1));
+    }
+    float kept[N];
+    int cnt = 0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        bool keep = false;
+        if (i < V && !isnan(x[i])) {
+            const float d = fabsf(__fsub_rn(x[i], med));
+            keep = !(d > mad);
+        }
+        kept[i] = keep ? x[i] : 0.0f;
+        cnt += keep;
+    }
+    const float tot = numpy_sum(kept, V);
+    return __fdiv_rn(tot, static_cast<float>(cnt));   // cnt == 0 -> 0/0 = NaN
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) fuse_kernel(const float *__restrict__ dsm, int layout, int V,
+                                                   long long cells, float *__restrict__ out) {
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < cells;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        float x[N];
+        if (layout == VS_LAYOUT_VHW) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) x[i] = (i < V) ? __ldcs(dsm + i * cells + c) : 0.0f;
+        } else {
+            const float *p = dsm + c * V;
+#pragma unroll
+            for (int i = 0; i < N; ++i) x[i] = (i < V) ? __ldcs(p + i) : 0.0f;
+        }
+        out[c] = fuse_cell(x, V);
+    }
+}
+
+// ---- V > 64: same arithmetic with local arrays -----------------------------------------
+__device__ float pairwise_any(const float *x, int n) {
+    // numpy's recursion, unrolled with an explicit stack of (offset, length) blocks
+    float res;
+    if (n < 8) {
+        res = 0.0f;
+        for (int i = 0; i < n; ++i) res = __fadd_rn(res, x[i]);
+        return res;
+    }
+    if (n <= 128) {
+        float r[8];
+        for (int j = 0; j < 8; ++j) r[j] = x[j];
+        int i = 8;
+        for (; i < n - (n % 8); i += 8)
+            for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], x[i + j]);
+        res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
+                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
+        for (; i < n; ++i) res = __fadd_rn(res, x[i]);
+        return res;
+    }
+    int n2 = n / 2;
+    n2 -= n2 % 8;
+    return __fadd_rn(pairwise_any(x, n2), pairwise_any(x + n2, n - n2));
+}
+
+constexpr int kMaxViewsLocal = 512;
+
+__device__ void insertion_sort(unsigned *a, int n) {
+    for (int i = 1; i < n; ++i) {
+        unsigned v = a[i];
+        int j = i - 1;
+        while (j >= 0 && a[j] > v) { a[j + 1] = a[j]; --j; }
+        a[j + 1] = v;
+    }
+}
+
+__global__ void fuse_kernel_large(const float *__restrict__ dsm, int layout, int V, long long cells,
+                                  float *__restrict__ out) {
+    float x[kMaxViewsLocal];
+    unsigned k[kMaxViewsLocal];
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < cells;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        int n = 0;
+        for (int i = 0; i < V; ++i) {
+            x[i] = layout == VS_LAYOUT_VHW ? dsm[i * cells + c] : dsm[c * V + i];
+            if (!isnan(x[i])) k[n++] = key_from_float(x[i]);
+        }
+        if (n <= 2) { out[c] = __int_as_float(0x7fffffff); continue; }
+        insertion_sort(k, n);
+        const float med = median_of_sorted(k[(n - 1) >> 1], k[n >> 1]);
+        int nd = 0;
+        for (int i = 0; i < V; ++i)
+            if (!isnan(x[i])) {
+                float d = fabsf(__fsub_rn(x[i], med));
+                if (!isnan(d)) k[nd++] = key_from_float(d);
+            }
+        float mad = __int_as_float(0x7fffffff);
+        if (nd > 0) {
+            insertion_sort(k, nd);
+            mad = median_of_sorted(k[(nd - 1) >> 1], k[nd >> 1]);
+        }
+        int cnt = 0;
+        for (int i = 0; i < V; ++i) {
+            bool keep = !isnan(x[i]) && !(fabsf(__fsub_rn(x[i], med)) > mad);
+            cnt += keep;
+            x[i] = keep ? x[i] : 0.0f;
+        }
+        const float tot = __fadd_rn(0.0f, pairwise_any(x, V));
+        out[c] = __fdiv_rn(tot, static_cast<float>(cnt));
+    }
+}
+
+template <int N>
+void launch_fuse(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
+    const int threads = 128;
+    long long want = ceil_div(cells, threads);
+    unsigned g = static_cast<unsigned>(std::min<long long>(want, sm_count() * 16LL));
+    fuse_kernel<N><<<g, threads, 0, st>>>(dsm, layout, V, cells, out);
+}
+
+}  // namespace
+}  // namespace vs
+
+using namespace vs;
+
+extern "C" size_t vs_fuse_dsms_workspace_size(int64_t h, int64_t w) {
+    if (h <= 0 || w <= 0) return 0;
+    return sizeof(float) * static_cast<size_t>(h) * w + 256;
+}
+
+extern "C" int vs_fuse_dsms(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
+                            int median_blur, void *workspace, size_t workspace_bytes, void *stream) {
+    VS_REQUIRE(h > 0 && w > 0 && n_views > 0 && n_views <= kMaxViewsLocal,
+               "vs_fuse_dsms: bad sizes views=%lld grid=%lldx%lld", (long long)n_views, (long long)h,
+               (long long)w);
+    VS_REQUIRE(layout == VS_LAYOUT_HWV || layout == VS_LAYOUT_VHW, "vs_fuse_dsms: bad layout %d", layout);
+    VS_REQUIRE(dsm && out, "vs_fuse_dsms: null pointer");
+    cudaStream_t st = as_stream(stream);
+    const long long cells = h * w;
+    float *dst = out;
+    if (median_blur) {
+        const size_t need = vs_fuse_dsms_workspace_size(h, w);
+        VS_REQUIRE(workspace, "vs_fuse_dsms: median_blur needs a workspace");
+        if (workspace_bytes < need) {
+            set_error("vs_fuse_dsms: workspace %zu < %zu bytes", workspace_bytes, need);
+            return VS_ERR_WORKSPACE;
+        }
+        dst = static_cast<float *>(workspace);
+    }
+    const int V = static_cast<int>(n_views);
+    if (V <= 8) launch_fuse<8>(dsm, layout, V, cells, dst, st);
+    else if (V <= 16) launch_fuse<16>(dsm, layout, V, cells, dst, st);
+    else if (V <= 32) launch_fuse<32>(dsm, layout, V, cells, dst, st);
+    else if (V <= 64) launch_fuse<64>(dsm, layout, V, cells, dst, st);
+    else {
+        const int threads = 64;
+        unsigned g = static_cast<unsigned>(std::min<long long>(ceil_div(cells, threads), sm_count() * 8LL));
+        fuse_kernel_large<<<g, threads, 0, st>>>(dsm, layout, V, cells, dst);
+    }
+    VS_LAUNCH_CHECK("fuse_kernel");
+    if (median_blur) return launch_blur_f32(dst, out, h, w, st);
+    return VS_OK;
+}

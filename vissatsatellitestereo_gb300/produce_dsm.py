@@ -1,0 +1,30 @@
+"""Batched ``produce_dsm_from_points`` (produce_dsm.py:46-58): every view's point cloud
+rasterised onto one DSM grid (proj_to_grid) and median-blurred in float32, in one call."""
+import torch
+
+from . import _lib
+from ._dev import as_device, ptr, require_cuda, stream_handle, workspace
+
+E_RESOLUTION = 0.5   # produce_dsm.py:41-42
+N_RESOLUTION = 0.5
+
+
+def grid_size(aoi_width, aoi_height, e_resolution=E_RESOLUTION, n_resolution=N_RESOLUTION):
+    """(e_size, n_size) as produce_dsm.py:54-55 derives them."""
+    return int(aoi_width / e_resolution) + 1, int(aoi_height / n_resolution) + 1
+
+
+def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize, ysize, out=None):
+    """points: (total, 3) float64 (device tensor or array); offsets: (V+1,) int64 view
+    boundaries.  Returns (V, ysize, xsize) float32 device tensor."""
+    require_cuda()
+    pts = as_device(points, torch.float64)
+    offs = as_device(offsets, torch.int64)
+    V = offs.numel() - 1
+    xsize, ysize = int(xsize), int(ysize)
+    if out is None:
+        out = torch.empty((V, ysize, xsize), dtype=torch.float32, device='cuda')
+    wp, wb = workspace(_lib.lib().vs_dsm_from_points_workspace_size(V, xsize, ysize))
+    _lib.call('vs_dsm_from_points', ptr(pts), ptr(offs), V, float(xoff), float(yoff), float(xresolution),
+              float(yresolution), xsize, ysize, ptr(out), wp, wb, stream_handle())
+    return out

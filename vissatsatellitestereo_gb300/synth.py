@@ -172,10 +172,11 @@ class ViewSpec:
 
 def make_views(seed: int, scene: Scene, n_views: int, height: int, width: int,
                nan_lo: float, nan_hi: float, jitter: float) -> list:
-    """Per-view specs whose footprint covers the scene's DSM grid."""
+    """Per-view specs whose footprint covers the scene's DSM grid (6% margin, so the
+    small rotations and shifts leave no uncovered corners)."""
     rng = np.random.default_rng(seed)
     g = scene.grid
-    gsd = max(g.xsize * g.xres / width, g.ysize * g.yres / height)
+    gsd = 1.06 * max(g.xsize * g.xres / width, g.ysize * g.yres / height)
     views = []
     for v in range(n_views):
         views.append(ViewSpec(height, width, gsd,
