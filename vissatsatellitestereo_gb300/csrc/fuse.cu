@@ -148,28 +148,38 @@ __global__ void __launch_bounds__(128) fuse_kernel(const float *__restrict__ dsm
 }
 
 // ---- V > 64: same arithmetic with local arrays -----------------------------------------
-__device__ float pairwise_any(const float *x, int n) {
-    // numpy's recursion, unrolled with an explicit stack of (offset, length) blocks
+// numpy's pairwise block of n <= 128 values: 8 accumulators, combined in a tree, then the
+// tail (n < 8: a plain sequential sum from 0).
+__device__ __forceinline__ float pairwise_block(const float *x, int n) {
     float res;
     if (n < 8) {
         res = 0.0f;
         for (int i = 0; i < n; ++i) res = __fadd_rn(res, x[i]);
         return res;
     }
-    if (n <= 128) {
-        float r[8];
-        for (int j = 0; j < 8; ++j) r[j] = x[j];
-        int i = 8;
-        for (; i < n - (n % 8); i += 8)
-            for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], x[i + j]);
-        res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
-                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
-        for (; i < n; ++i) res = __fadd_rn(res, x[i]);
-        return res;
+    float r[8];
+    for (int j = 0; j < 8; ++j) r[j] = x[j];
+    int i = 8;
+    for (; i < n - (n % 8); i += 8)
+        for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], x[i + j]);
+    res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
+                    __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
+    for (; i < n; ++i) res = __fadd_rn(res, x[i]);
+    return res;
+}
+
+// numpy's halving recursion above 128 values, unrolled at compile time (no call stack):
+// D levels of halving cover n <= 128 * 2^D.
+template <int D>
+__device__ __forceinline__ float pairwise_any(const float *x, int n) {
+    if constexpr (D == 0) {
+        return pairwise_block(x, n);
+    } else {
+        if (n <= 128) return pairwise_block(x, n);
+        int n2 = n / 2;
+        n2 -= n2 % 8;
+        return __fadd_rn(pairwise_any<D - 1>(x, n2), pairwise_any<D - 1>(x + n2, n - n2));
     }
-    int n2 = n / 2;
-    n2 -= n2 % 8;
-    return __fadd_rn(pairwise_any(x, n2), pairwise_any(x + n2, n - n2));
 }
 
 constexpr int kMaxViewsLocal = 512;
@@ -214,7 +224,7 @@ __global__ void fuse_kernel_large(const float *__restrict__ dsm, int layout, int
             cnt += keep;
             x[i] = keep ? x[i] : 0.0f;
         }
-        const float tot = __fadd_rn(0.0f, pairwise_any(x, V));
+        const float tot = __fadd_rn(0.0f, pairwise_any<4>(x, V));   // 4 levels: V <= 2048
         out[c] = __fdiv_rn(tot, static_cast<float>(cnt));
     }
 }
