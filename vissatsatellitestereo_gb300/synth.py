@@ -188,13 +188,47 @@ def make_views(seed: int, scene: Scene, n_views: int, height: int, width: int,
     return views
 
 
+_SCENE_CACHE = {}
+
+
+def scene_raster_torch(scene: Scene, device='cpu'):
+    """The scene's height field on a raster 4x finer than the DSM grid (plus a 10% margin),
+    boxes painted once; returns (raster, e0, n0, step) with raster[i, j] the height at
+    easting e0 + (j + 0.5) * step, northing n0 - (i + 0.5) * step."""
+    import torch
+    key = (id(scene), str(device))
+    hit = _SCENE_CACHE.get(key)
+    if hit is not None and hit[0] is scene:
+        return hit[1]
+    g = scene.grid
+    step = min(g.xres, g.yres) / 4.0
+    w = g.xsize * g.xres
+    h = g.ysize * g.yres
+    e0 = g.xoff - 0.1 * w
+    n0 = g.yoff + 0.1 * h
+    nx = int(math.ceil(1.2 * w / step))
+    ny = int(math.ceil(1.2 * h / step))
+    ras = torch.zeros((ny, nx), dtype=torch.float32, device=device)
+    for b in range(scene.boxes.shape[0]):
+        be0, be1, bn0, bn1, hb = scene.boxes[b].tolist()
+        j0 = max(int(math.ceil((be0 - e0) / step - 0.5)), 0)
+        j1 = min(int(math.ceil((be1 - e0) / step - 0.5)), nx)
+        i0 = max(int(math.ceil((n0 - bn1) / step - 0.5)), 0)
+        i1 = min(int(math.ceil((n0 - bn0) / step - 0.5)), ny)
+        if j0 < j1 and i0 < i1:
+            ras[i0:i1, j0:j1].clamp_(min=float(hb))
+    out = (ras, e0, n0, step)
+    _SCENE_CACHE[key] = (scene, out)
+    return out
+
+
 def view_points_torch(scene: Scene, view: ViewSpec, device='cpu'):
     """(H*W, 3) float64 torch tensor of (easting, northing, height) for one view.
 
-    Each pixel is mapped to UTM by the view's affine map; its height is the tallest box
-    covering that location (0 m ground elsewhere) plus N(0, noise) and is NaN with
-    probability ``nan_frac``.  Rows follow the pixel raster, like the depth-map point
-    lists of ``aggregate_2p5d_util.py:75-98``.
+    Each pixel is mapped to UTM by the view's affine map; its height is the scene height
+    there (tallest box, 0 m ground elsewhere) plus N(0, noise), and NaN with probability
+    ``nan_frac``.  Rows follow the pixel raster, like the depth-map point lists of
+    ``aggregate_2p5d_util.py:75-98``.
     """
     import torch
     gen = torch.Generator(device=device)
@@ -202,6 +236,7 @@ def view_points_torch(scene: Scene, view: ViewSpec, device='cpu'):
     H, W = view.height, view.width
     g = scene.grid
     f64 = torch.float64
+    ras, e0, n0, step = scene_raster_torch(scene, device)
     jj = torch.arange(W, device=device, dtype=f64) + 0.5
     ii = torch.arange(H, device=device, dtype=f64) + 0.5
     c, s = math.cos(view.theta), math.sin(view.theta)
@@ -212,30 +247,11 @@ def view_points_torch(scene: Scene, view: ViewSpec, device='cpu'):
     cn = g.yoff - g.ysize * g.yres / 2.0 + view.shift_n
     east = ce + view.gsd * (c * dj - s * di)
     north = cn - view.gsd * (s * dj + c * di)
-    height = torch.zeros((H, W), device=device, dtype=torch.float32)
-    boxes = torch.as_tensor(scene.boxes, device=device, dtype=f64)
-    # paint boxes through their pixel bounding windows (cheap: boxes are small)
-    inv = 1.0 / view.gsd
-    for b in range(boxes.shape[0]):
-        e0, e1, n0, n1, hb = scene.boxes[b].tolist()
-        corners = [(e0, n0), (e0, n1), (e1, n0), (e1, n1)]
-        pj, pi = [], []
-        for (e, n) in corners:
-            de, dn = (e - ce) * inv, (n - cn) * inv
-            # inverse of the rotation above
-            pj.append(c * de - s * dn + W / 2.0)
-            pi.append(-s * de - c * dn + H / 2.0)
-        j0 = max(int(math.floor(min(pj))) - 1, 0)
-        j1 = min(int(math.ceil(max(pj))) + 1, W)
-        i0 = max(int(math.floor(min(pi))) - 1, 0)
-        i1 = min(int(math.ceil(max(pi))) + 1, H)
-        if j0 >= j1 or i0 >= i1:
-            continue
-        ew = east[i0:i1, j0:j1]
-        nw = north[i0:i1, j0:j1]
-        inside = (ew >= e0) & (ew < e1) & (nw >= n0) & (nw < n1)
-        win = height[i0:i1, j0:j1]
-        win[inside] = torch.clamp(win[inside], min=float(hb))
+    ci = ((east - e0) / step).floor().long()
+    ri = ((n0 - north) / step).floor().long()
+    inside = (ci >= 0) & (ci < ras.shape[1]) & (ri >= 0) & (ri < ras.shape[0])
+    height = ras[ri.clamp(0, ras.shape[0] - 1), ci.clamp(0, ras.shape[1] - 1)]
+    height = torch.where(inside, height, torch.zeros_like(height))
     noise = torch.randn((H, W), generator=gen, device=device, dtype=torch.float32) * scene.noise
     height = height + noise
     nan_mask = torch.rand((H, W), generator=gen, device=device) < view.nan_frac
