@@ -104,9 +104,21 @@ __host__ __device__ inline df df_from_double(double v) {
     float hi = static_cast<float>(v);
     return {hi, static_cast<float>(v - static_cast<double>(hi))};
 }
-__device__ __forceinline__ double df_to_double(df a) {
-    return static_cast<double>(a.hi) + static_cast<double>(a.lo);
+// float -> double by bit manipulation (exact; the conversion instruction shares GB300's
+// narrow FP64 pipe).  Subnormal, infinite and NaN floats take the instruction.
+__device__ __forceinline__ double f32_to_f64(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0 || e == 0xffu) {
+        if ((u << 1) == 0) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(u) << 32));
+        return static_cast<double>(f);
+    }
+    const unsigned long long b = (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
+                                 (static_cast<unsigned long long>(e + 1023u - 127u) << 52) |
+                                 (static_cast<unsigned long long>(u & 0x7fffffu) << 29);
+    return __longlong_as_double(static_cast<long long>(b));
 }
+__device__ __forceinline__ double df_to_double(df a) { return __dadd_rn(f32_to_f64(a.hi), f32_to_f64(a.lo)); }
 
 // ---- order-preserving keys --------------------------------------------------------------
 // Unsigned keys whose integer order is the numeric order of the float value; key 0 is

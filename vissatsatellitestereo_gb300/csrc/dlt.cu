@@ -7,12 +7,16 @@
 // The fit solves the reference's problem -- the unit vector p minimising |A p| for the
 // 2N x 12 DLT matrix A -- without forming A.  A^T A only depends on 40 point moments
 // (sum X X^T weighted by 1, c, r, c^2 + r^2 with X = [x y z 1]), so one streaming pass
-// accumulates them in coordinates centred and scaled per view (FP32 partial sums over 32
-// points, FP64 beyond).  The 12x12 problem is then solved in FP64 by inverse iteration on
-// the normalised Gram matrix, with the centring/scaling map M applied exactly, so the
-// minimiser is the reference's un-normalised one.  Factorisation is a positive-diagonal
-// RQ (Gram-Schmidt from the last row), which is unique and equals the reference's
-// sign-fixed scipy RQ.
+// accumulates them in coordinates centred and scaled per view (FP32 sums over at most 32
+// points per thread and across a warp, FP64 beyond).  The 12x12 problem is then solved in
+// FP64 by inverse iteration on the normalised Gram matrix, with the centring/scaling map M
+// applied exactly, so the minimiser is the reference's un-normalised one.  Factorisation is
+// a positive-diagonal RQ (Gram-Schmidt from the last row), which is unique and equals the
+// reference's sign-fixed scipy RQ.
+//
+// GB300 executes FP64 arithmetic, FP64 compares and every conversion instruction on a
+// narrow pipe (~1/64 of FP32), so the per-point passes use integer bit manipulation for
+// conversions and double-float (two-FP32) arithmetic where FP32 is not accurate enough.
 #include <algorithm>
 #include <math.h>
 
@@ -21,10 +25,6 @@
 
 namespace vs {
 namespace {
-
-constexpr int kMom = 40;            // 4 weights x 10 unique entries of X X^T
-constexpr int kMomThreads = 128;
-constexpr int kChunk = 32;          // points per FP32 partial sum
 
 // ---------------------------------------------------------------------------------------
 // (a) projection
@@ -76,101 +76,118 @@ __global__ void __launch_bounds__(256) rpc_project_kernel(const VsRpcCamera *__r
 // ---------------------------------------------------------------------------------------
 // Per-view normalisation: X' = (X - centre) / s, c' = (col - c0) / sp, r' = (row - r0) / sp
 struct Norm {
-    double cx, cy, cz, s, c0, r0, sp, count;
+    double cx, cy, cz, s, c0, r0, sp;
 };
 
-// Min/max of x, y, z, col, row over the kept points of each view, as order-preserving
-// keys (min via the complemented key so everything is an atomicMax).
+constexpr int kBoxSamples = 65536;   // points sampled per view for the normalisation box
+
+// Min/max of x, y, z (and col, row when given) over a strided sample of the kept points,
+// as order-preserving keys (the min through the complemented key).  Any centre and scale
+// serve the normalisation; it only has to keep the moments well scaled.
 __global__ void bbox_init_kernel(unsigned long long *bb, int n_views) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n_views * 11) bb[i] = 0ull;
+    if (i < n_views * 10) bb[i] = 0ull;
 }
 
 __global__ void __launch_bounds__(256) bbox_kernel(const double *__restrict__ x, const double *__restrict__ y,
                                                    const double *__restrict__ z, long long xyz_stride,
                                                    const double *__restrict__ col, const double *__restrict__ row,
-                                                   const uint8_t *__restrict__ keep, long long n,
+                                                   const uint8_t *__restrict__ keep, long long n, long long step,
                                                    unsigned long long *__restrict__ bb) {
     const int v = blockIdx.y;
     const double *src[5] = {x + v * xyz_stride, y + v * xyz_stride, z + v * xyz_stride, col ? col + v * n : nullptr,
                             row ? row + v * n : nullptr};
     unsigned long long hi[5], lo[5];
-    unsigned long long cnt = 0;
 #pragma unroll
     for (int j = 0; j < 5; ++j) hi[j] = lo[j] = 0ull;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    for (long long i = (blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x) * step; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x * step) {
         if (keep && !keep[v * n + i]) continue;
-        ++cnt;
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
             if (!src[j]) continue;
-            unsigned long long k = key_from_double(src[j][i]);
+            const unsigned long long k = key_from_double(src[j][i]);
             hi[j] = max(hi[j], k);
             lo[j] = max(lo[j], ~k);
         }
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+    for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
             hi[j] = max(hi[j], __shfl_xor_sync(0xffffffffu, hi[j], off));
             lo[j] = max(lo[j], __shfl_xor_sync(0xffffffffu, lo[j], off));
         }
-    }
     if ((threadIdx.x & 31) == 0) {
-        unsigned long long *b = bb + v * 11;
+        unsigned long long *b = bb + v * 10;
         for (int j = 0; j < 5; ++j) {
-            atomicMax(b + j, hi[j]);
-            atomicMax(b + 5 + j, lo[j]);
+            if (hi[j]) atomicMax(b + j, hi[j]);
+            if (lo[j]) atomicMax(b + 5 + j, lo[j]);
         }
-        atomicAdd(b + 10, cnt);
     }
 }
 
-// Normalisation from the bounding boxes.  For the fused camera path the pixel frame is the
-// RPC's own (colOff/rowOff, max scale) and the count is filled in by the moments pass.
+__device__ __forceinline__ double finite_or(double v, double fallback) {
+    return (isfinite(v)) ? v : fallback;
+}
+
+// Normalisation from the sampled boxes.  For the fused camera path the pixel frame is the
+// RPC's own (colOff/rowOff, larger scale).
 __global__ void norm_kernel(const unsigned long long *__restrict__ bb, const VsRpcCamera *__restrict__ cams,
                             int n_views, Norm *__restrict__ norm) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n_views) return;
-    const unsigned long long *b = bb + v * 11;
+    const unsigned long long *b = bb + v * 10;
     double mx[5], mn[5];
     for (int j = 0; j < 5; ++j) {
         mx[j] = b[j] ? double_from_key(b[j]) : 0.0;
         mn[j] = b[5 + j] ? double_from_key(~b[5 + j]) : 0.0;
     }
     Norm nm;
-    nm.cx = 0.5 * (mn[0] + mx[0]);
-    nm.cy = 0.5 * (mn[1] + mx[1]);
-    nm.cz = 0.5 * (mn[2] + mx[2]);
+    nm.cx = finite_or(0.5 * (mn[0] + mx[0]), 0.0);
+    nm.cy = finite_or(0.5 * (mn[1] + mx[1]), 0.0);
+    nm.cz = finite_or(0.5 * (mn[2] + mx[2]), 0.0);
     double s = fmax(fmax(mx[0] - mn[0], mx[1] - mn[1]), mx[2] - mn[2]) * 0.5;
     nm.s = (s > 0.0 && isfinite(s)) ? s : 1.0;
     if (cams) {
         nm.c0 = cams[v].col_off;
         nm.r0 = cams[v].row_off;
         nm.sp = fmax(fabs(cams[v].col_scale), fabs(cams[v].row_scale));
-        if (!(nm.sp > 0.0)) nm.sp = 1.0;
+        if (!(nm.sp > 0.0) || !isfinite(nm.sp)) nm.sp = 1.0;
     } else {
-        nm.c0 = 0.5 * (mn[3] + mx[3]);
-        nm.r0 = 0.5 * (mn[4] + mx[4]);
+        nm.c0 = finite_or(0.5 * (mn[3] + mx[3]), 0.0);
+        nm.r0 = finite_or(0.5 * (mn[4] + mx[4]), 0.0);
         double sp = fmax(mx[3] - mn[3], mx[4] - mn[4]) * 0.5;
         nm.sp = (sp > 0.0 && isfinite(sp)) ? sp : 1.0;
     }
-    nm.count = static_cast<double>(b[10]);
     norm[v] = nm;
 }
 
+// Per-view normalisation in the forms the per-point kernels use.
 struct NormF {
-    float cx, cy, cz, inv_s, c0, r0, inv_sp;
+    df cx, cy, cz, inv_s, c0, r0, inv_sp;
+    float sp;
 };
 
-__device__ __forceinline__ NormF to_f32(const Norm &nm) {
-    return {static_cast<float>(nm.cx), static_cast<float>(nm.cy), static_cast<float>(nm.cz),
-            static_cast<float>(1.0 / nm.s), static_cast<float>(nm.c0), static_cast<float>(nm.r0),
-            static_cast<float>(1.0 / nm.sp)};
+__device__ __forceinline__ NormF make_normf(const Norm &nm) {
+    NormF f;
+    f.cx = df_from_double(nm.cx);
+    f.cy = df_from_double(nm.cy);
+    f.cz = df_from_double(nm.cz);
+    f.inv_s = df_from_double(1.0 / nm.s);
+    f.c0 = df_from_double(nm.c0);
+    f.r0 = df_from_double(nm.r0);
+    f.inv_sp = df_from_double(1.0 / nm.sp);
+    f.sp = static_cast<float>(nm.sp);
+    return f;
 }
+
+__device__ __forceinline__ df centre(df v, df off, df inv) { return df_mul(df_add(v, {-off.hi, -off.lo}), inv); }
+
+constexpr int kMom = 40;            // 4 weights x 10 unique entries of X X^T
+constexpr int kSlots = 41;          // + kept-point count
+constexpr int kMomThreads = 128;
+constexpr int kChunk = 32;          // points per thread (FP32 partial sums)
 
 // Accumulates one point's 40 moment terms into FP32 partial sums.
 __device__ __forceinline__ void add_moments(float (&m)[kMom], float x, float y, float z, float c, float r) {
@@ -186,60 +203,71 @@ __device__ __forceinline__ void add_moments(float (&m)[kMom], float x, float y, 
     }
 }
 
-// Block reduction of the per-thread FP64 accumulators into partial[v][blockIdx.x][40].
-__device__ __forceinline__ void store_block_moments(double (&acc)[kMom], double *partial, double *red) {
-    // warp shuffle, then across warps through shared memory (fixed order: deterministic)
+// Warp sums in FP32, warps combined in FP64 in a fixed order (deterministic):
+// partial[kSlots] of this block.
+__device__ __forceinline__ void store_block_moments(float (&m)[kMom], float count, double *partial, double *red) {
 #pragma unroll
-    for (int k = 0; k < kMom; ++k) {
+    for (int k = 0; k < kMom; ++k)
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
-    }
+        for (int off = 16; off > 0; off >>= 1) m[k] += __shfl_xor_sync(0xffffffffu, m[k], off);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) count += __shfl_xor_sync(0xffffffffu, count, off);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0)
+    if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < kMom; ++k) red[warp * kMom + k] = acc[k];
+        for (int k = 0; k < kMom; ++k) red[warp * kSlots + k] = f32_to_f64(m[k]);
+        red[warp * kSlots + kMom] = f32_to_f64(count);
+    }
     __syncthreads();
-    if (threadIdx.x < kMom) {
+    if (threadIdx.x < kSlots) {
         double s = 0.0;
-        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) s += red[w * kMom + threadIdx.x];
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) s += red[w * kSlots + threadIdx.x];
         partial[threadIdx.x] = s;
     }
 }
 
-// Moments of the drop-in fit: points and (col, row) are given (FP64).
+// Normalised coordinates of one kept point from FP64 ENU and double-float pixels.
+__device__ __forceinline__ void normalised_point(const NormF &nf, double X, double Y, double Z, df c, df r,
+                                                 float &px, float &py, float &pz, float &pc, float &pr) {
+    const df x = centre(split_double(X), nf.cx, nf.inv_s);
+    const df y = centre(split_double(Y), nf.cy, nf.inv_s);
+    const df z = centre(split_double(Z), nf.cz, nf.inv_s);
+    const df cc = centre(c, nf.c0, nf.inv_sp);
+    const df rr = centre(r, nf.r0, nf.inv_sp);
+    px = x.hi + x.lo;
+    py = y.hi + y.lo;
+    pz = z.hi + z.lo;
+    pc = cc.hi + cc.lo;
+    pr = rr.hi + rr.lo;
+}
+
+// Moments of the drop-in fit: points and (col, row) are given (FP64).  Block b of view v
+// owns points [b * 128 * kChunk, (b + 1) * 128 * kChunk).
 __global__ void __launch_bounds__(kMomThreads) moments_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
     const double *__restrict__ col, const double *__restrict__ row, const uint8_t *__restrict__ keep, long long n,
     const Norm *__restrict__ norm, double *__restrict__ partial) {
-    __shared__ double red[(kMomThreads / 32) * kMom];
+    __shared__ double red[(kMomThreads / 32) * kSlots];
     const int v = blockIdx.y;
-    const NormF nf = to_f32(norm[v]);
+    const NormF nf = make_normf(norm[v]);
     const double *xv = x + v * xyz_stride, *yv = y + v * xyz_stride, *zv = z + v * xyz_stride;
     const double *cv = col + v * n, *rv = row + v * n;
-    double acc[kMom];
     float m[kMom];
 #pragma unroll
-    for (int k = 0; k < kMom; ++k) acc[k] = 0.0, m[k] = 0.0f;
-    int in_chunk = 0;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    for (int k = 0; k < kMom; ++k) m[k] = 0.0f;
+    float count = 0.0f;
+    const long long base = static_cast<long long>(blockIdx.x) * kMomThreads * kChunk + threadIdx.x;
+#pragma unroll 1
+    for (int j = 0; j < kChunk; ++j) {
+        const long long i = base + static_cast<long long>(j) * kMomThreads;
+        if (i >= n) break;
         if (keep && !keep[v * n + i]) continue;
-        const float px = (__double2float_rn(xv[i]) - nf.cx) * nf.inv_s;
-        const float py = (__double2float_rn(yv[i]) - nf.cy) * nf.inv_s;
-        const float pz = (__double2float_rn(zv[i]) - nf.cz) * nf.inv_s;
-        const df dc = split_double(cv[i]), dr = split_double(rv[i]);
-        const float pc = ((dc.hi - nf.c0) + dc.lo) * nf.inv_sp;
-        const float pr = ((dr.hi - nf.r0) + dr.lo) * nf.inv_sp;
+        float px, py, pz, pc, pr;
+        normalised_point(nf, xv[i], yv[i], zv[i], split_double(cv[i]), split_double(rv[i]), px, py, pz, pc, pr);
         add_moments(m, px, py, pz, pc, pr);
-        if (++in_chunk == kChunk) {
-#pragma unroll
-            for (int k = 0; k < kMom; ++k) acc[k] += m[k], m[k] = 0.0f;
-            in_chunk = 0;
-        }
+        count += 1.0f;
     }
-#pragma unroll
-    for (int k = 0; k < kMom; ++k) acc[k] += m[k];
-    store_block_moments(acc, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kMom, red);
+    store_block_moments(m, count, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kSlots, red);
 }
 
 // Fused camera path: project the grid through view v's RPC, apply the in-image mask,
@@ -249,8 +277,8 @@ __global__ void __launch_bounds__(kMomThreads) project_moments_kernel(
     const VsRpcCamera *__restrict__ cams, const double *__restrict__ lat, const double *__restrict__ lon,
     const double *__restrict__ alt, const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, long long n, long long stride, const Norm *__restrict__ norm,
-    double *__restrict__ partial, float4 *__restrict__ colrow, unsigned long long *__restrict__ counts) {
-    __shared__ double red[(kMomThreads / 32) * kMom];
+    double *__restrict__ partial, float4 *__restrict__ colrow) {
+    __shared__ double red[(kMomThreads / 32) * kSlots];
     __shared__ VsRpcCamera cam;
     __shared__ RpcFast fast;
     const int v = blockIdx.y;
@@ -262,16 +290,17 @@ __global__ void __launch_bounds__(kMomThreads) project_moments_kernel(
     __syncthreads();
     if (threadIdx.x == 0) prepare_fast(cam, fast);
     __syncthreads();
-    const NormF nf = to_f32(norm[v]);
+    const NormF nf = make_normf(norm[v]);
     const long long off = v * stride;
-    double acc[kMom];
     float m[kMom];
 #pragma unroll
-    for (int k = 0; k < kMom; ++k) acc[k] = 0.0, m[k] = 0.0f;
-    int in_chunk = 0;
-    unsigned long long kept = 0;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    for (int k = 0; k < kMom; ++k) m[k] = 0.0f;
+    float count = 0.0f;
+    const long long base = static_cast<long long>(blockIdx.x) * kMomThreads * kChunk + threadIdx.x;
+#pragma unroll 1
+    for (int j = 0; j < kChunk; ++j) {
+        const long long i = base + static_cast<long long>(j) * kMomThreads;
+        if (i >= n) break;
         df dc, dr;
         if (MODE == VS_PROJ_EXACT) {
             double cc, rr;
@@ -282,28 +311,15 @@ __global__ void __launch_bounds__(kMomThreads) project_moments_kernel(
             project_fast(fast, split_double(lat[off + i]), split_double(lon[off + i]), split_double(alt[off + i]),
                          dc, dr);
         }
-        const bool k = df_ge0(dc) && df_ge0(dr) && df_lt(dc, fast.width) && df_lt(dr, fast.height);
         colrow[static_cast<long long>(v) * n + i] = make_float4(dc.hi, dc.lo, dr.hi, dr.lo);
+        const bool k = df_ge0(dc) && df_ge0(dr) && df_lt(dc, fast.width) && df_lt(dr, fast.height);
         if (!k) continue;
-        ++kept;
-        const float px = (__double2float_rn(x[off + i]) - nf.cx) * nf.inv_s;
-        const float py = (__double2float_rn(y[off + i]) - nf.cy) * nf.inv_s;
-        const float pz = (__double2float_rn(z[off + i]) - nf.cz) * nf.inv_s;
-        const float pc = ((dc.hi - nf.c0) + dc.lo) * nf.inv_sp;
-        const float pr = ((dr.hi - nf.r0) + dr.lo) * nf.inv_sp;
+        float px, py, pz, pc, pr;
+        normalised_point(nf, x[off + i], y[off + i], z[off + i], dc, dr, px, py, pz, pc, pr);
         add_moments(m, px, py, pz, pc, pr);
-        if (++in_chunk == kChunk) {
-#pragma unroll
-            for (int k2 = 0; k2 < kMom; ++k2) acc[k2] += m[k2], m[k2] = 0.0f;
-            in_chunk = 0;
-        }
+        count += 1.0f;
     }
-#pragma unroll
-    for (int k = 0; k < kMom; ++k) acc[k] += m[k];
-#pragma unroll
-    for (int off2 = 16; off2 > 0; off2 >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, off2);
-    if ((threadIdx.x & 31) == 0) atomicAdd(counts + v, kept);
-    store_block_moments(acc, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kMom, red);
+    store_block_moments(m, count, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kSlots, red);
 }
 
 // ---- 12x12 solve (one thread per view; FP64) -------------------------------------------
@@ -439,26 +455,75 @@ __device__ int factorize(double *P, double *K, double *R, double *t) {
     return VS_OK;
 }
 
+// What the error pass needs of one view's camera: the camera in the normalised frame
+// (q = M p, rescaled) as double-floats, the normalisation, and K^-1.
+struct ErrCam {
+    df q[12];
+    NormF nf;
+    float qscale;      // q = qscale * M p
+    float kinv[9];
+    float w, h;
+    int ok;
+};
+
+__device__ void make_errcam(const double *K, const double *R, const double *t, const Norm &nm, float w, float h,
+                            int ok, ErrCam &ec) {
+    double P[12];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 4; ++j) {
+            double s = 0.0;
+            for (int l = 0; l < 3; ++l) s += K[3 * i + l] * (j < 3 ? R[3 * l + j] : t[l]);
+            P[4 * i + j] = s;
+        }
+    double u[3][4];
+    for (int i = 0; i < 3; ++i) {   // T^T p_i
+        const double *p = P + 4 * i;
+        u[i][0] = nm.s * p[0];
+        u[i][1] = nm.s * p[1];
+        u[i][2] = nm.s * p[2];
+        u[i][3] = nm.cx * p[0] + nm.cy * p[1] + nm.cz * p[2] + p[3];
+    }
+    double q[12], mx = 0.0;
+    for (int j = 0; j < 4; ++j) {
+        q[j] = (u[0][j] - nm.c0 * u[2][j]) / nm.sp;
+        q[4 + j] = (u[1][j] - nm.r0 * u[2][j]) / nm.sp;
+        q[8 + j] = u[2][j];
+    }
+    for (int i = 0; i < 12; ++i) mx = fmax(mx, fabs(q[i]));
+    const double sc = (mx > 0.0 && isfinite(mx)) ? 1.0 / mx : 1.0;
+    for (int i = 0; i < 12; ++i) ec.q[i] = df_from_double(q[i] * sc);
+    ec.qscale = static_cast<float>(sc);
+    ec.nf = make_normf(nm);
+    const double a = K[0], b = K[1], c = K[2], d = K[3], e = K[4], f = K[5], g = K[6], hh = K[7], i9 = K[8];
+    const double det = a * (e * i9 - f * hh) - b * (d * i9 - f * g) + c * (d * hh - e * g);
+    const double ki[9] = {(e * i9 - f * hh) / det, (c * hh - b * i9) / det, (b * f - c * e) / det,
+                          (f * g - d * i9) / det,  (a * i9 - c * g) / det,  (c * d - a * f) / det,
+                          (d * hh - e * g) / det,  (b * g - a * hh) / det,  (a * e - b * d) / det};
+    for (int k = 0; k < 9; ++k) ec.kinv[k] = static_cast<float>(ki[k]);
+    ec.w = w;
+    ec.h = h;
+    ec.ok = ok;
+}
+
 // One CTA per view: sum the block partials in a fixed order, solve, factorise.
 __global__ void __launch_bounds__(64) solve_kernel(const double *__restrict__ partial, int n_blocks,
                                                    const Norm *__restrict__ norm,
-                                                   const unsigned long long *__restrict__ counts,
                                                    const VsRpcCamera *__restrict__ cams, double *__restrict__ K_out,
                                                    double *__restrict__ R_out, double *__restrict__ t_out,
-                                                   double *__restrict__ params, double *__restrict__ pinfo,
+                                                   double *__restrict__ params, ErrCam *__restrict__ errcam,
                                                    int32_t *__restrict__ status) {
-    __shared__ double mom[kMom];
+    __shared__ double mom[kSlots];
     const int v = blockIdx.x;
-    if (threadIdx.x < kMom) {
+    if (threadIdx.x < kSlots) {
         double s = 0.0;
-        const double *p = partial + static_cast<long long>(v) * n_blocks * kMom + threadIdx.x;
-        for (int b = 0; b < n_blocks; ++b) s += p[b * kMom];
+        const double *p = partial + static_cast<long long>(v) * n_blocks * kSlots + threadIdx.x;
+        for (int b = 0; b < n_blocks; ++b) s += p[b * kSlots];
         mom[threadIdx.x] = s;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;
     const Norm nm = norm[v];
-    const double count = counts ? static_cast<double>(counts[v]) : nm.count;
+    const double count = mom[kMom];
     double K[9], R[9], t[3];
     for (int i = 0; i < 9; ++i) K[i] = R[i] = 0.0;
     t[0] = t[1] = t[2] = 0.0;
@@ -526,21 +591,9 @@ __global__ void __launch_bounds__(64) solve_kernel(const double *__restrict__ pa
     for (int i = 0; i < 9; ++i) K_out[v * 9 + i] = K[i], R_out[v * 9 + i] = R[i];
     for (int i = 0; i < 3; ++i) t_out[v * 3 + i] = t[i];
     status[v] = st;
-    if (pinfo) {       // K[R|t] and K^-1 for the error pass
-        double *pi = pinfo + v * 21;
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 4; ++j) {
-                double s = 0.0;
-                for (int l = 0; l < 3; ++l) s += K[3 * i + l] * (j < 3 ? R[3 * l + j] : t[l]);
-                pi[4 * i + j] = s;
-            }
-        // K^-1 of an upper-triangular K
-        const double a = K[0], b = K[1], c = K[2], d = K[4], e = K[5], f = K[8];
-        double *ki = pi + 12;
-        ki[0] = 1 / a; ki[1] = -b / (a * d); ki[2] = (b * e - c * d) / (a * d * f);
-        ki[3] = 0; ki[4] = 1 / d; ki[5] = -e / (d * f);
-        ki[6] = 0; ki[7] = 0; ki[8] = 1 / f;
-    }
+    if (errcam)
+        make_errcam(K, R, t, nm, cams ? static_cast<float>(cams[v].width) : 0.f,
+                    cams ? static_cast<float>(cams[v].height) : 0.f, st == VS_OK, errcam[v]);
     if (params) {
         double q[4] = {0, 0, 0, 0};
         if (st == VS_OK) quaternion(R, q);
@@ -556,91 +609,94 @@ __global__ void __launch_bounds__(64) solve_kernel(const double *__restrict__ pa
 // ---------------------------------------------------------------------------------------
 // error statistics (check_perspective_error)
 // ---------------------------------------------------------------------------------------
-// P^ = K[R|t] and K^-1 for given K, R, t
-__global__ void pinfo_kernel(const double *K, const double *R, const double *t, int n_views, double *pinfo) {
+// ErrCam for given K, R, t (the drop-in statistics entry)
+__global__ void errcam_kernel(const double *K, const double *R, const double *t, const Norm *norm, int n_views,
+                              ErrCam *ec) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n_views) return;
-    const double *k = K + v * 9, *r = R + v * 9, *tt = t + v * 3;
-    double *pi = pinfo + v * 21;
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 4; ++j) {
-            double s = 0.0;
-            for (int l = 0; l < 3; ++l) s += k[3 * i + l] * (j < 3 ? r[3 * l + j] : tt[l]);
-            pi[4 * i + j] = s;
-        }
-    // general 3x3 inverse (np.linalg.inv(K.T) is used transposed: ray = K^-1 [c r 1])
-    const double a = k[0], b = k[1], c = k[2], d = k[3], e = k[4], f = k[5], g = k[6], h = k[7], i9 = k[8];
-    const double det = a * (e * i9 - f * h) - b * (d * i9 - f * g) + c * (d * h - e * g);
-    double *ki = pi + 12;
-    ki[0] = (e * i9 - f * h) / det; ki[1] = (c * h - b * i9) / det; ki[2] = (b * f - c * e) / det;
-    ki[3] = (f * g - d * i9) / det; ki[4] = (a * i9 - c * g) / det; ki[5] = (c * d - a * f) / det;
-    ki[6] = (d * h - e * g) / det; ki[7] = (b * g - a * h) / det; ki[8] = (a * e - b * d) / det;
+    make_errcam(K + 9 * v, R + 9 * v, t + 3 * v, norm[v], 0.f, 0.f, 1, ec[v]);
 }
 
 struct ErrWs {
     unsigned *keys;          // [2][V][n] float bits of the per-point errors (kept points only)
-    double *sums;            // [V][blocks][2]
+    double *sums;            // [V][blocks][3]: pixel sum, metric sum, count
     unsigned *maxk;          // [V][2]
-    unsigned long long *cnt; // [V]
     unsigned *hist;          // [V][4][256]
     unsigned *sel;           // [V][4][3]: prefix, mask, k
+    double *cnt;             // [V]
 };
 
 constexpr int kErrThreads = 256;
 
+__device__ __forceinline__ df dot4(const df *q, df x, df y, df z) {
+    df s = df_add(df_mul(q[0], x), df_mul(q[1], y));
+    s = df_add(s, df_mul(q[2], z));
+    return df_add(s, q[3]);
+}
+
 // Per kept point: pixel reprojection error and metric inverse-projection error.
-// colrow_df (fused path) or col/row (FP64) supply the observations.
+//  * reprojection: in the fit's normalised frame, est' = (q1.X', q2.X') / q3.X' in
+//    double-float, minus the normalised observation, times the pixel scale;
+//  * inverse projection: the reference's |scale*ray - cam| is the distance from the camera-
+//    frame point to the ray d = K^-1 [c r 1].  The point lies on the ray through its own
+//    projection, cam = h * K^-1 [c^ r^ 1] with h = (P^ X)_3, so the distance equals
+//    |h| |delta x d| / |d| with delta = K^-1 [c^ - c, r^ - r, 0]: the pixel residual
+//    enters directly and nothing of the camera's ~1e5-1e6 m depth cancels.
 __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
     const double *__restrict__ col, const double *__restrict__ row, const float4 *__restrict__ colrow,
-    const uint8_t *__restrict__ keep, const float *__restrict__ wh, long long n, const double *__restrict__ pinfo,
-    const double *__restrict__ Rm, const double *__restrict__ tv, ErrWs w) {
-    __shared__ double red[2][kErrThreads / 32];
+    const uint8_t *__restrict__ keep, long long n, const ErrCam *__restrict__ cams, ErrWs w) {
+    __shared__ ErrCam ec;
+    __shared__ double red[3][kErrThreads / 32];
     const int v = blockIdx.y;
     const int V = gridDim.y;
-    const double *pi = pinfo + v * 21, *ki = pi + 12, *R = Rm + v * 9, *t = tv + v * 3;
-    double ps = 0.0, is = 0.0;
+    if (threadIdx.x == 0) ec = cams[v];
+    __syncthreads();
+    float ps = 0.0f, is = 0.0f, cnt = 0.0f;
     unsigned pmax = 0, imax = 0;
-    unsigned long long cnt = 0;
+    const double *xv = x + v * xyz_stride, *yv = y + v * xyz_stride, *zv = z + v * xyz_stride;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        double c, r;
+        df c, r;
         bool k;
         if (colrow) {
             const float4 cr = colrow[static_cast<long long>(v) * n + i];
-            const df dc{cr.x, cr.y}, dr{cr.z, cr.w};
-            k = df_ge0(dc) && df_ge0(dr) && df_lt(dc, wh[2 * v]) && df_lt(dr, wh[2 * v + 1]);
-            c = df_to_double(dc);
-            r = df_to_double(dr);
+            c = {cr.x, cr.y};
+            r = {cr.z, cr.w};
+            k = df_ge0(c) && df_ge0(r) && df_lt(c, ec.w) && df_lt(r, ec.h);
         } else {
-            c = col[v * n + i];
-            r = row[v * n + i];
+            c = split_double(col[v * n + i]);
+            r = split_double(row[v * n + i]);
             k = keep ? keep[v * n + i] != 0 : true;
         }
         unsigned pk = 0xffffffffu, ik = 0xffffffffu;
-        if (k) {
-            const double X = x[v * xyz_stride + i], Y = y[v * xyz_stride + i], Z = z[v * xyz_stride + i];
-            const double cx = R[0] * X + R[1] * Y + R[2] * Z + t[0];
-            const double cy = R[3] * X + R[4] * Y + R[5] * Z + t[1];
-            const double cz = R[6] * X + R[7] * Y + R[8] * Z + t[2];
-            const double h0 = pi[0] * X + pi[1] * Y + pi[2] * Z + pi[3];
-            const double h1 = pi[4] * X + pi[5] * Y + pi[6] * Z + pi[7];
-            const double h2 = pi[8] * X + pi[9] * Y + pi[10] * Z + pi[11];
-            const double ec = h0 / h2 - c, er = h1 / h2 - r;
-            const double pe = sqrt(er * er + ec * ec);
-            const double rx = ki[0] * c + ki[1] * r + ki[2];
-            const double ry = ki[3] * c + ki[4] * r + ki[5];
-            const double rz = ki[6] * c + ki[7] * r + ki[8];
-            const double sc = (cx * rx + cy * ry + cz * rz) / (rx * rx + ry * ry + rz * rz);
-            const double dx = rx * sc - cx, dy = ry * sc - cy, dz = rz * sc - cz;
-            const double ie = sqrt(dx * dx + dy * dy + dz * dz);
+        if (k && ec.ok) {
+            const df X = centre(split_double(xv[i]), ec.nf.cx, ec.nf.inv_s);
+            const df Y = centre(split_double(yv[i]), ec.nf.cy, ec.nf.inv_s);
+            const df Z = centre(split_double(zv[i]), ec.nf.cz, ec.nf.inv_s);
+            const df h0 = dot4(ec.q, X, Y, Z), h1 = dot4(ec.q + 4, X, Y, Z), h2 = dot4(ec.q + 8, X, Y, Z);
+            const df ec_ = df_add(df_div(h0, h2), df_mul({-1.0f, 0.0f}, centre(c, ec.nf.c0, ec.nf.inv_sp)));
+            const df er_ = df_add(df_div(h1, h2), df_mul({-1.0f, 0.0f}, centre(r, ec.nf.r0, ec.nf.inv_sp)));
+            const float dc = ec.nf.sp * (ec_.hi + ec_.lo), dr = ec.nf.sp * (er_.hi + er_.lo);
+            const float pe = sqrtf(__fmaf_rn(dr, dr, dc * dc));
+            const float *ki = ec.kinv;
+            const float cf = c.hi, rf = r.hi;
+            const float d0 = __fmaf_rn(ki[0], cf, __fmaf_rn(ki[1], rf, ki[2]));
+            const float d1 = __fmaf_rn(ki[3], cf, __fmaf_rn(ki[4], rf, ki[5]));
+            const float d2 = __fmaf_rn(ki[6], cf, __fmaf_rn(ki[7], rf, ki[8]));
+            const float e0 = __fmaf_rn(ki[0], dc, ki[1] * dr);
+            const float e1 = __fmaf_rn(ki[3], dc, ki[4] * dr);
+            const float e2 = __fmaf_rn(ki[6], dc, ki[7] * dr);
+            const float x0 = e1 * d2 - e2 * d1, x1 = e2 * d0 - e0 * d2, x2 = e0 * d1 - e1 * d0;
+            const float hz = fabsf((h2.hi + h2.lo) / ec.qscale);
+            const float ie = hz * sqrtf((x0 * x0 + x1 * x1 + x2 * x2) / (d0 * d0 + d1 * d1 + d2 * d2));
             ps += pe;
             is += ie;
-            pk = __float_as_uint(__double2float_rn(pe));
-            ik = __float_as_uint(__double2float_rn(ie));
+            cnt += 1.0f;
+            pk = __float_as_uint(pe);
+            ik = __float_as_uint(ie);
             pmax = max(pmax, pk);
             imax = max(imax, ik);
-            ++cnt;
         }
         w.keys[static_cast<long long>(v) * n + i] = pk;
         w.keys[(static_cast<long long>(V) + v) * n + i] = ik;
@@ -649,41 +705,44 @@ __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
     for (int off = 16; off > 0; off >>= 1) {
         ps += __shfl_xor_sync(0xffffffffu, ps, off);
         is += __shfl_xor_sync(0xffffffffu, is, off);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
         pmax = max(pmax, __shfl_xor_sync(0xffffffffu, pmax, off));
         imax = max(imax, __shfl_xor_sync(0xffffffffu, imax, off));
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
     }
     const int warp = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        red[0][warp] = ps;
-        red[1][warp] = is;
-        atomicMax(w.maxk + 2 * v, pmax);
-        atomicMax(w.maxk + 2 * v + 1, imax);
-        atomicAdd(w.cnt + v, cnt);
+        red[0][warp] = f32_to_f64(ps);
+        red[1][warp] = f32_to_f64(is);
+        red[2][warp] = f32_to_f64(cnt);
+        if (pmax) atomicMax(w.maxk + 2 * v, pmax);
+        if (imax) atomicMax(w.maxk + 2 * v + 1, imax);
     }
     __syncthreads();
-    if (threadIdx.x < 2) {
+    if (threadIdx.x < 3) {
         double s = 0.0;
         for (int i = 0; i < kErrThreads / 32; ++i) s += red[threadIdx.x][i];
-        w.sums[(static_cast<long long>(v) * gridDim.x + blockIdx.x) * 2 + threadIdx.x] = s;
+        w.sums[(static_cast<long long>(v) * gridDim.x + blockIdx.x) * 3 + threadIdx.x] = s;
+    }
+}
+
+// per-view totals of the block sums (fixed order) and the selection ranks
+__global__ void error_count_kernel(ErrWs w, int n_views, int n_blocks) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_views) return;
+    double c = 0.0;
+    for (int b = 0; b < n_blocks; ++b) c += w.sums[(static_cast<long long>(v) * n_blocks + b) * 3 + 2];
+    w.cnt[v] = c;
+    const unsigned long long n = static_cast<unsigned long long>(c);
+    for (int t = 0; t < 4; ++t) {
+        const int i = v * 4 + t;
+        w.sel[3 * i] = 0;       // prefix
+        w.sel[3 * i + 1] = 0;   // mask
+        w.sel[3 * i + 2] = n ? static_cast<unsigned>((t & 1) ? n / 2 : (n - 1) / 2) : 0u;
     }
 }
 
 // Radix selection of the two middle order statistics of both error arrays, 8 bits a pass.
 // Targets per view: 0/1 = low/high middle of the pixel errors, 2/3 = of the metric errors.
-__global__ void select_init_kernel(ErrWs w, int n_views) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_views * 4) return;
-    const int v = i / 4;
-    const unsigned long long n = w.cnt[v];
-    const int t = i % 4;
-    unsigned k = 0;
-    if (n > 0) k = static_cast<unsigned>((t & 1) ? n / 2 : (n - 1) / 2);
-    w.sel[3 * i] = 0;       // prefix
-    w.sel[3 * i + 1] = 0;   // mask
-    w.sel[3 * i + 2] = k;   // rank still to skip inside the prefix bucket
-}
-
 __global__ void __launch_bounds__(256) select_hist_kernel(ErrWs w, long long n, int shift) {
     __shared__ unsigned h[4][256];
     const int v = blockIdx.y, V = gridDim.y;
@@ -727,32 +786,21 @@ __global__ void select_step_kernel(ErrWs w, int n_views, int shift) {
 __global__ void error_final_kernel(ErrWs w, int n_views, int n_blocks, double *err) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n_views) return;
-    const double cnt = static_cast<double>(w.cnt[v]);
+    const double cnt = w.cnt[v];
     double s[2] = {0.0, 0.0};
     for (int b = 0; b < n_blocks; ++b) {
-        s[0] += w.sums[(static_cast<long long>(v) * n_blocks + b) * 2];
-        s[1] += w.sums[(static_cast<long long>(v) * n_blocks + b) * 2 + 1];
+        s[0] += w.sums[(static_cast<long long>(v) * n_blocks + b) * 3];
+        s[1] += w.sums[(static_cast<long long>(v) * n_blocks + b) * 3 + 1];
     }
     double *o = err + v * VS_ERROR_STATS;
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
     for (int q = 0; q < 2; ++q) {
         const double lo = __uint_as_float(w.sel[3 * (v * 4 + 2 * q)]);
         const double hi = __uint_as_float(w.sel[3 * (v * 4 + 2 * q + 1)]);
-        const double nan = __longlong_as_double(0x7ff8000000000000ll);
         o[3 * q] = cnt > 0 ? s[q] / cnt : nan;
         o[3 * q + 1] = cnt > 0 ? ((0.0 + lo) + hi) / 2.0 : nan;
         o[3 * q + 2] = cnt > 0 ? static_cast<double>(__uint_as_float(w.maxk[2 * v + q])) : nan;
     }
-}
-
-ErrWs carve_err(Carver &cv, int V, long long n, int blocks) {
-    ErrWs w;
-    w.keys = cv.take<unsigned>(2 * static_cast<size_t>(V) * n);
-    w.sums = cv.take<double>(static_cast<size_t>(V) * blocks * 2);
-    w.maxk = cv.take<unsigned>(2 * V);
-    w.cnt = cv.take<unsigned long long>(V);
-    w.hist = cv.take<unsigned>(static_cast<size_t>(V) * 1024);
-    w.sel = cv.take<unsigned>(static_cast<size_t>(V) * 12);
-    return w;
 }
 
 int err_blocks(long long n) {
@@ -760,64 +808,90 @@ int err_blocks(long long n) {
     return static_cast<int>(std::max<long long>(1, std::min<long long>(want, sm_count() * 4LL)));
 }
 
+ErrWs carve_err(Carver &cv, int V, long long n, int blocks) {
+    ErrWs w;
+    w.keys = cv.take<unsigned>(2 * static_cast<size_t>(V) * n);
+    w.sums = cv.take<double>(static_cast<size_t>(V) * blocks * 3);
+    w.maxk = cv.take<unsigned>(2 * V);
+    w.hist = cv.take<unsigned>(static_cast<size_t>(V) * 1024);
+    w.sel = cv.take<unsigned>(static_cast<size_t>(V) * 12);
+    w.cnt = cv.take<double>(V);
+    return w;
+}
+
 int run_error_stats(const double *x, const double *y, const double *z, long long xyz_stride, const double *col,
-                    const double *row, const float4 *colrow, const uint8_t *keep, const float *wh, int V,
-                    long long n, const double *pinfo, const double *R, const double *t, double *err, ErrWs &w,
-                    cudaStream_t st) {
+                    const double *row, const float4 *colrow, const uint8_t *keep, int V, long long n,
+                    const ErrCam *cams, double *err, ErrWs &w, cudaStream_t st) {
     const int blocks = err_blocks(n);
     if (cudaMemsetAsync(w.maxk, 0, sizeof(unsigned) * 2 * V, st) != cudaSuccess ||
-        cudaMemsetAsync(w.cnt, 0, sizeof(unsigned long long) * V, st) != cudaSuccess ||
         cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 1024 * V, st) != cudaSuccess) {
         set_error("cudaMemsetAsync failed");
         return VS_ERR_CUDA;
     }
-    error_points_kernel<<<dim3(blocks, V), kErrThreads, 0, st>>>(x, y, z, xyz_stride, col, row, colrow, keep, wh, n,
-                                                                  pinfo, R, t, w);
-    VS_LAUNCH_CHECK("error_points_kernel");
+    if (n > 0) {
+        error_points_kernel<<<dim3(blocks, V), kErrThreads, 0, st>>>(x, y, z, xyz_stride, col, row, colrow, keep, n,
+                                                                      cams, w);
+        VS_LAUNCH_CHECK("error_points_kernel");
+    } else if (cudaMemsetAsync(w.sums, 0, sizeof(double) * V * blocks * 3, st) != cudaSuccess) {
+        set_error("cudaMemsetAsync failed");
+        return VS_ERR_CUDA;
+    }
+    const unsigned vg = static_cast<unsigned>(ceil_div(V, 128));
+    error_count_kernel<<<vg, 128, 0, st>>>(w, V, blocks);
+    VS_LAUNCH_CHECK("error_count_kernel");
     const unsigned sg = static_cast<unsigned>(ceil_div(V * 4, 128));
-    select_init_kernel<<<sg, 128, 0, st>>>(w, V);
-    VS_LAUNCH_CHECK("select_init_kernel");
-    for (int shift = 24; shift >= 0; shift -= 8) {
+    for (int shift = 24; shift >= 0 && n > 0; shift -= 8) {
         select_hist_kernel<<<dim3(blocks, V), 256, 0, st>>>(w, n, shift);
         VS_LAUNCH_CHECK("select_hist_kernel");
         select_step_kernel<<<sg, 128, 0, st>>>(w, V, shift);
         VS_LAUNCH_CHECK("select_step_kernel");
     }
-    error_final_kernel<<<static_cast<unsigned>(ceil_div(V, 128)), 128, 0, st>>>(w, V, blocks, err);
+    error_final_kernel<<<vg, 128, 0, st>>>(w, V, blocks, err);
     VS_LAUNCH_CHECK("error_final_kernel");
     return VS_OK;
 }
 
 int mom_blocks(long long n) {
-    long long want = ceil_div(n, kMomThreads * 8);
-    return static_cast<int>(std::max<long long>(1, std::min<long long>(want, sm_count() * 2LL)));
+    return static_cast<int>(std::max<long long>(1, ceil_div(n, static_cast<long long>(kMomThreads) * kChunk)));
+}
+
+long long box_step(long long n) { return std::max<long long>(1, n / kBoxSamples); }
+
+int box_blocks(long long n) {
+    long long samples = ceil_div(n, box_step(n));
+    return static_cast<int>(std::max<long long>(1, std::min<long long>(ceil_div(samples, 256), 64)));
 }
 
 struct FitWs {
     unsigned long long *bb;
     Norm *norm;
     double *partial;
-    double *pinfo;
-    unsigned long long *counts;
-    float *wh;
+    ErrCam *errcam;
     float4 *colrow;
 };
 
 FitWs carve_fit(Carver &cv, int V, long long n, bool fused) {
     FitWs f;
-    f.bb = cv.take<unsigned long long>(static_cast<size_t>(V) * 11);
+    f.bb = cv.take<unsigned long long>(static_cast<size_t>(V) * 10);
     f.norm = cv.take<Norm>(V);
-    f.partial = cv.take<double>(static_cast<size_t>(V) * mom_blocks(n) * kMom);
-    f.pinfo = cv.take<double>(static_cast<size_t>(V) * 21);
-    f.counts = cv.take<unsigned long long>(V);
-    f.wh = cv.take<float>(2 * static_cast<size_t>(V));
+    f.partial = cv.take<double>(static_cast<size_t>(V) * mom_blocks(n) * kSlots);
+    f.errcam = cv.take<ErrCam>(V);
     f.colrow = fused ? cv.take<float4>(static_cast<size_t>(V) * n) : nullptr;
     return f;
 }
 
-__global__ void wh_kernel(const VsRpcCamera *cams, int V, float *wh) {
-    int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v < V) wh[2 * v] = static_cast<float>(cams[v].width), wh[2 * v + 1] = static_cast<float>(cams[v].height);
+int launch_norm(const double *x, const double *y, const double *z, long long xyz_stride, const double *col,
+                const double *row, const uint8_t *keep, const VsRpcCamera *cams, int V, long long n, FitWs &f,
+                cudaStream_t st) {
+    bbox_init_kernel<<<static_cast<unsigned>(ceil_div(V * 10, 128)), 128, 0, st>>>(f.bb, V);
+    VS_LAUNCH_CHECK("bbox_init_kernel");
+    if (n > 0) {
+        bbox_kernel<<<dim3(box_blocks(n), V), 256, 0, st>>>(x, y, z, xyz_stride, col, row, keep, n, box_step(n), f.bb);
+        VS_LAUNCH_CHECK("bbox_kernel");
+    }
+    norm_kernel<<<static_cast<unsigned>(ceil_div(V, 64)), 64, 0, st>>>(f.bb, cams, V, f.norm);
+    VS_LAUNCH_CHECK("norm_kernel");
+    return VS_OK;
 }
 
 }  // namespace
@@ -865,20 +939,13 @@ extern "C" int vs_dlt_fit(const double *x, const double *y, const double *z, int
     cudaStream_t st = as_stream(stream);
     Carver cv(workspace);
     FitWs f = carve_fit(cv, n_views, n, false);
-    bbox_init_kernel<<<static_cast<unsigned>(ceil_div(n_views * 11, 128)), 128, 0, st>>>(f.bb, n_views);
-    VS_LAUNCH_CHECK("bbox_init_kernel");
+    int s = launch_norm(x, y, z, xyz_stride, col, row, keep, nullptr, n_views, n, f, st);
+    if (s != VS_OK) return s;
     const int blocks = mom_blocks(n);
-    if (n > 0) {
-        bbox_kernel<<<dim3(blocks, n_views), 256, 0, st>>>(x, y, z, xyz_stride, col, row, keep, n, f.bb);
-        VS_LAUNCH_CHECK("bbox_kernel");
-    }
-    norm_kernel<<<static_cast<unsigned>(ceil_div(n_views, 64)), 64, 0, st>>>(f.bb, nullptr, n_views, f.norm);
-    VS_LAUNCH_CHECK("norm_kernel");
     moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, xyz_stride, col, row, keep, n, f.norm,
                                                                    f.partial);
     VS_LAUNCH_CHECK("moments_kernel");
-    solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, nullptr, nullptr, K, R, t, nullptr, nullptr,
-                                         status);
+    solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, nullptr, K, R, t, nullptr, nullptr, status);
     VS_LAUNCH_CHECK("solve_kernel");
     return VS_OK;
 }
@@ -886,7 +953,7 @@ extern "C" int vs_dlt_fit(const double *x, const double *y, const double *z, int
 extern "C" size_t vs_perspective_error_workspace_size(int n_views, int64_t n) {
     if (n_views <= 0 || n < 0) return 0;
     Carver cv(nullptr);
-    cv.take<double>(static_cast<size_t>(n_views) * 21);
+    carve_fit(cv, n_views, 0, false);
     carve_err(cv, n_views, n, err_blocks(n));
     return cv.used + 256;
 }
@@ -904,18 +971,20 @@ extern "C" int vs_perspective_error(const double *x, const double *y, const doub
     }
     cudaStream_t st = as_stream(stream);
     Carver cv(workspace);
-    double *pinfo = cv.take<double>(static_cast<size_t>(n_views) * 21);
+    FitWs f = carve_fit(cv, n_views, 0, false);
     ErrWs w = carve_err(cv, n_views, n, err_blocks(n));
-    pinfo_kernel<<<static_cast<unsigned>(ceil_div(n_views, 64)), 64, 0, st>>>(K, R, t, n_views, pinfo);
-    VS_LAUNCH_CHECK("pinfo_kernel");
-    return run_error_stats(x, y, z, xyz_stride, col, row, nullptr, keep, nullptr, n_views, n, pinfo, R, t, err, w, st);
+    int s = launch_norm(x, y, z, xyz_stride, col, row, keep, nullptr, n_views, n, f, st);
+    if (s != VS_OK) return s;
+    errcam_kernel<<<static_cast<unsigned>(ceil_div(n_views, 64)), 64, 0, st>>>(K, R, t, f.norm, n_views, f.errcam);
+    VS_LAUNCH_CHECK("errcam_kernel");
+    return run_error_stats(x, y, z, xyz_stride, col, row, nullptr, keep, n_views, n, f.errcam, err, w, st);
 }
 
 extern "C" size_t vs_camera_approx_workspace_size(int n_views, int64_t n) {
     if (n_views <= 0 || n < 0) return 0;
     Carver cv(nullptr);
     carve_fit(cv, n_views, n, true);
-    cv.take<double>(static_cast<size_t>(n_views) * 21);   // K
+    cv.take<double>(static_cast<size_t>(n_views) * 9);    // K
     cv.take<double>(static_cast<size_t>(n_views) * 9);    // R
     cv.take<double>(static_cast<size_t>(n_views) * 3);    // t
     carve_err(cv, n_views, n, err_blocks(n));
@@ -940,36 +1009,24 @@ extern "C" int vs_camera_approx_perspective(const VsRpcCamera *cams, int n_views
     cudaStream_t st = as_stream(stream);
     Carver cv(workspace);
     FitWs f = carve_fit(cv, n_views, n, true);
-    double *K = cv.take<double>(static_cast<size_t>(n_views) * 21);
+    double *K = cv.take<double>(static_cast<size_t>(n_views) * 9);
     double *R = cv.take<double>(static_cast<size_t>(n_views) * 9);
     double *t = cv.take<double>(static_cast<size_t>(n_views) * 3);
     ErrWs ew = carve_err(cv, n_views, n, err_blocks(n));
-    // ENU bounding box (all points) -> normalisation; pixel frame from each RPC
-    bbox_init_kernel<<<static_cast<unsigned>(ceil_div(n_views * 11, 128)), 128, 0, st>>>(f.bb, n_views);
-    VS_LAUNCH_CHECK("bbox_init_kernel");
+    // ENU box (sampled) -> normalisation; pixel frame from each RPC
+    int s = launch_norm(x, y, z, point_stride, nullptr, nullptr, nullptr, cams, n_views, n, f, st);
+    if (s != VS_OK) return s;
     const int blocks = mom_blocks(n);
-    if (n > 0) {
-        bbox_kernel<<<dim3(blocks, n_views), 256, 0, st>>>(x, y, z, point_stride, nullptr, nullptr, nullptr, n, f.bb);
-        VS_LAUNCH_CHECK("bbox_kernel");
-    }
-    norm_kernel<<<static_cast<unsigned>(ceil_div(n_views, 64)), 64, 0, st>>>(f.bb, cams, n_views, f.norm);
-    VS_LAUNCH_CHECK("norm_kernel");
-    if (cudaMemsetAsync(f.counts, 0, sizeof(unsigned long long) * n_views, st) != cudaSuccess) {
-        set_error("cudaMemsetAsync failed");
-        return VS_ERR_CUDA;
-    }
     if (proj_mode == VS_PROJ_EXACT)
         project_moments_kernel<VS_PROJ_EXACT><<<dim3(blocks, n_views), kMomThreads, 0, st>>>(
-            cams, lat, lon, alt, x, y, z, n, point_stride, f.norm, f.partial, f.colrow, f.counts);
+            cams, lat, lon, alt, x, y, z, n, point_stride, f.norm, f.partial, f.colrow);
     else
         project_moments_kernel<VS_PROJ_FAST><<<dim3(blocks, n_views), kMomThreads, 0, st>>>(
-            cams, lat, lon, alt, x, y, z, n, point_stride, f.norm, f.partial, f.colrow, f.counts);
+            cams, lat, lon, alt, x, y, z, n, point_stride, f.norm, f.partial, f.colrow);
     VS_LAUNCH_CHECK("project_moments_kernel");
-    solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, f.counts, cams, K, R, t, params, f.pinfo, status);
+    solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, cams, K, R, t, params, f.errcam, status);
     VS_LAUNCH_CHECK("solve_kernel");
     if (!err) return VS_OK;
-    wh_kernel<<<static_cast<unsigned>(ceil_div(n_views, 64)), 64, 0, st>>>(cams, n_views, f.wh);
-    VS_LAUNCH_CHECK("wh_kernel");
-    return run_error_stats(x, y, z, point_stride, nullptr, nullptr, f.colrow, nullptr, f.wh, n_views, n, f.pinfo, R,
-                           t, err, ew, st);
+    return run_error_stats(x, y, z, point_stride, nullptr, nullptr, f.colrow, nullptr, n_views, n, f.errcam, err, ew,
+                           st);
 }

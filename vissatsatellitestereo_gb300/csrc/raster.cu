@@ -39,7 +39,7 @@ struct Axis {
     long long n;                 // cells along the axis
     const long long *thr;        // n + 1 integer thresholds (ulps of off), fast path only
     unsigned long long top12;    // sign + exponent of off
-    float approx_scale;          // 65536 * ulp(off) / res
+    unsigned long long mul;      // floor(2^64 * ulp(off) / res): row estimate = mulhi(d, mul)
     int neg;                     // off < 0
     int dir;
     int fast;                    // fast path usable
@@ -64,9 +64,9 @@ __device__ __forceinline__ long long axis_index(const Axis &ax, double v) {
         long long bv = static_cast<long long>(b);
         long long d = ((ax.dir > 0) != (ax.neg != 0)) ? (bv - bo) : (bo - bv);
         if (d < 0 || d >= __ldg(ax.thr + ax.n)) return -1;
-        long long r = static_cast<long long>(
-            static_cast<float>(static_cast<unsigned>(d >> 16)) * ax.approx_scale);
-        r = r < 0 ? 0 : (r >= ax.n ? ax.n - 1 : r);
+        // integer estimate (no conversion instructions: on GB300 they share the FP64 pipe)
+        long long r = static_cast<long long>(__umul64hi(static_cast<unsigned long long>(d), ax.mul));
+        r = r >= ax.n ? ax.n - 1 : r;
 #pragma unroll 1
         for (int it = 0; it < 8 && __ldg(ax.thr + r) > d; ++it) --r;
 #pragma unroll 1
@@ -98,17 +98,22 @@ __device__ __forceinline__ bool is_nan_bits(unsigned long long b) {
     return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
 }
 
-// Pass 1: bin every point of every view and atomicMax its height key into the cell.
+// Zero heights are collected in a side list during binning: (cell, point index) pairs.
+struct ZeroList {
+    unsigned long long *entries;   // [2 * kZeroCap]: cell, index
+    int *count;                    // number of zero points seen (may exceed kZeroCap)
+};
+constexpr int kZeroCap = 1 << 16;
+
+// Pass 1: bin every point of one view and atomicMax its height key into the cell.
 // View v owns points [offsets[v], offsets[v+1]); vk is its key grid.
 __global__ void __launch_bounds__(256) bin_max_kernel(const double *__restrict__ pts,
                                                       const long long *__restrict__ offsets, int v,
                                                       long long single_n, Tables tb,
-                                                      unsigned long long *__restrict__ vk,
-                                                      int *__restrict__ zero_flag) {
+                                                      unsigned long long *__restrict__ vk, ZeroList zl) {
     const long long begin = offsets ? offsets[v] : 0;
     const long long end = offsets ? offsets[v + 1] : single_n;
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * 2;
-    bool saw_zero = false;
     for (long long i = begin + (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * 2;
          i < end; i += stride) {
         double p[6];
@@ -131,20 +136,46 @@ __global__ void __launch_bounds__(256) bin_max_kernel(const double *__restrict__
             if (r < 0) continue;
             long long c = axis_index(tb.col, x);
             if (c < 0) continue;
-            const bool zero = (zb << 1) == 0;
-            saw_zero |= zero;
-            unsigned long long key = zero ? kZeroKey : key_from_double(z);
-            atomicMax(vk + r * tb.col.n + c, key);
+            const long long cell = r * tb.col.n + c;
+            unsigned long long key;
+            if ((zb << 1) == 0) {            // +-0: one shared key, sign resolved afterwards
+                key = kZeroKey;
+                const int slot = atomicAdd(zl.count, 1);
+                if (slot < kZeroCap) {
+                    zl.entries[2 * slot] = static_cast<unsigned long long>(cell);
+                    zl.entries[2 * slot + 1] = static_cast<unsigned long long>(i + k);
+                }
+            } else {
+                key = key_from_double(z);
+            }
+            atomicMax(vk + cell, key);
         }
     }
-    if (__syncthreads_or(saw_zero) && threadIdx.x == 0) atomicOr(zero_flag, 1);
 }
 
-// Zero-sign resolution (only does work when some in-grid height was +-0).
+// Zero-sign resolution: first[cell] = smallest index of a zero point of a cell whose
+// maximum is zero.  Normally from the side list; a full pass if the list overflowed.
+__global__ void zero_list_init_kernel(const unsigned long long *__restrict__ keys,
+                                      unsigned long long *__restrict__ first, ZeroList zl) {
+    const int n = min(*zl.count, kZeroCap);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const unsigned long long cell = zl.entries[2 * e];
+        if (keys[cell] == kZeroKey) first[cell] = kNoIndex;
+    }
+}
+
+__global__ void zero_list_min_kernel(const unsigned long long *__restrict__ keys,
+                                     unsigned long long *__restrict__ first, ZeroList zl) {
+    const int n = min(*zl.count, kZeroCap);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const unsigned long long cell = zl.entries[2 * e];
+        if (keys[cell] == kZeroKey) atomicMin(first + cell, zl.entries[2 * e + 1]);
+    }
+}
+
 __global__ void zero_init_kernel(const unsigned long long *__restrict__ keys,
-                                 unsigned long long *__restrict__ first, long long total,
-                                 const int *__restrict__ zero_flag) {
-    if (!*zero_flag) return;
+                                 unsigned long long *__restrict__ first, long long total, ZeroList zl) {
+    if (*zl.count <= kZeroCap) return;
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < total;
          c += static_cast<long long>(gridDim.x) * blockDim.x)
         if (keys[c] == kZeroKey) first[c] = kNoIndex;
@@ -153,9 +184,8 @@ __global__ void zero_init_kernel(const unsigned long long *__restrict__ keys,
 __global__ void zero_first_kernel(const double *__restrict__ pts, const long long *__restrict__ offsets, int v,
                                   long long single_n, Tables tb,
                                   const unsigned long long *__restrict__ keys,
-                                  unsigned long long *__restrict__ first,
-                                  const int *__restrict__ zero_flag) {
-    if (!*zero_flag) return;
+                                  unsigned long long *__restrict__ first, ZeroList zl) {
+    if (*zl.count <= kZeroCap) return;
     const long long begin = offsets ? offsets[v] : 0;
     const long long end = offsets ? offsets[v + 1] : single_n;
     for (long long i = begin + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < end;
@@ -171,40 +201,52 @@ __global__ void zero_first_kernel(const double *__restrict__ pts, const long lon
     }
 }
 
-__device__ __forceinline__ double cell_value(unsigned long long k, long long cell,
-                                             const unsigned long long *first, const double *pts,
-                                             int zero_flag) {
-    if (k == kEmptyKey) return __longlong_as_double(0x7ff8000000000000ll);
-    if (k == kZeroKey && zero_flag) return pts[3 * first[cell] + 2];   // signed zero
-    return double_from_key(k);
+// Key of a cell's nanmax with the zero sign resolved (0 = empty cell).
+__device__ __forceinline__ unsigned long long cell_key(unsigned long long k, long long cell,
+                                                       const unsigned long long *first, const double *pts,
+                                                       int has_zero) {
+    if (k == kZeroKey && has_zero) return key_from_double(pts[3 * first[cell] + 2]);
+    return k;
+}
+
+__device__ __forceinline__ double key_value(unsigned long long k) {
+    return k == kEmptyKey ? __longlong_as_double(0x7ff8000000000000ll) : double_from_key(k);
 }
 
 // nanmax grid (FP64) from the keys.
 __global__ void decode_kernel(const unsigned long long *__restrict__ keys,
                               const unsigned long long *__restrict__ first,
-                              const double *__restrict__ pts, const int *__restrict__ zero_flag,
+                              const double *__restrict__ pts, ZeroList zl,
                               double *__restrict__ out, long long total) {
-    const int zf = *zero_flag;
+    const int hz = *zl.count > 0;
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < total;
          c += static_cast<long long>(gridDim.x) * blockDim.x)
-        out[c] = cell_value(keys[c], c, first, pts, zf);
+        out[c] = key_value(cell_key(keys[c], c, first, pts, hz));
 }
 
-// numpy's median of n <= 8 FP64 values (no NaN): sorted s, odd n -> (0 + s[n/2]) / 1,
-// even n -> ((0 + s[n/2-1]) + s[n/2]) / 2 (the sum reduction starts from its identity 0).
-__device__ __forceinline__ double median_small(double *s, int n) {
-    for (int i = 1; i < n; ++i) {          // insertion sort by order-preserving keys
-        double v = s[i];
-        unsigned long long kv = key_from_double(v);
+// numpy's median of the n <= 8 non-NaN neighbour values, given as order-preserving keys:
+// sorted s, odd n -> (0 + s[n/2]) / 1, even n -> ((0 + s[n/2-1]) + s[n/2]) / 2 (the sum
+// reduction starts from its identity 0, which also turns -0 into +0).
+__device__ __forceinline__ double median_keys(unsigned long long *s, int n) {
+    for (int i = 1; i < n; ++i) {          // insertion sort
+        const unsigned long long v = s[i];
         int j = i - 1;
-        while (j >= 0 && key_from_double(s[j]) > kv) {
+        while (j >= 0 && s[j] > v) {
             s[j + 1] = s[j];
             --j;
         }
         s[j + 1] = v;
     }
-    if (n & 1) return __dadd_rn(0.0, s[n >> 1]);
-    return __ddiv_rn(__dadd_rn(__dadd_rn(0.0, s[(n >> 1) - 1]), s[n >> 1]), 2.0);
+    if (n & 1) {
+        unsigned long long k = s[n >> 1];
+        if (k == 0x7fffffffffffffffull) k = kZeroKey;   // -0 + 0 = +0
+        return double_from_key(k);
+    }
+    return __dmul_rn(__dadd_rn(__dadd_rn(0.0, double_from_key(s[(n >> 1) - 1])), double_from_key(s[n >> 1])), 0.5);
+}
+
+__device__ __forceinline__ bool nan_double(double v) {
+    return is_nan_bits(static_cast<unsigned long long>(__double_as_longlong(v)));
 }
 
 // Non-propagating hole fill (lib/proj_to_grid.py:64-79) on an FP64 grid.
@@ -217,26 +259,46 @@ __global__ void hole_fill_kernel(const double *__restrict__ in, double *__restri
         const long long r = rc / W, col = rc - r * W;
         const double *img = in + plane * H * W;
         double v = img[rc];
-        if (!isnan(v)) {
+        if (!nan_double(v)) {
             out[c] = v;
             continue;
         }
-        double s[8];
+        unsigned long long s[8];
         int n = 0;
         for (int dj = -1; dj <= 1; ++dj)
             for (int dk = -1; dk <= 1; ++dk) {
                 long long j = r + dj, k = col + dk;
                 if (j < 0 || j >= H || k < 0 || k >= W) continue;
                 double u = img[j * W + k];
-                if (!isnan(u)) s[n++] = u;
+                if (!nan_double(u)) s[n++] = key_from_double(u);
             }
-        out[c] = n ? median_small(s, n) : v;
+        out[c] = n ? median_keys(s, n) : v;
     }
+}
+
+// Round-to-nearest FP64 -> FP32 (astype(np.float32)) with integer operations; the
+// conversion instruction runs on GB300's narrow FP64 pipe, so it is kept for the
+// float-subnormal range only.
+__device__ __forceinline__ float f64_to_f32(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
+    const int e = static_cast<int>((b >> 52) & 0x7ff);
+    const unsigned long long m = b & 0xfffffffffffffull;
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));   // inf / NaN
+    const int e32 = e - 1023 + 127;
+    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);                          // overflow
+    if (e == 0 && m == 0) return __uint_as_float(sign);                                   // signed zero
+    if (e32 <= 0) return __double2float_rn(v);                                           // float-subnormal range
+    const unsigned m23 = static_cast<unsigned>(m >> 29);
+    const unsigned rem = static_cast<unsigned>(m & 0x1fffffffu);
+    const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
+    return __uint_as_float(sign | ((static_cast<unsigned>(e32) << 23) + m23 + up));       // carry may round to inf
 }
 
 // ---- 3x3 median blur (float32, replicate border, NaN after every number) -----------------
 __device__ __forceinline__ unsigned blur_key(float v) {
-    return isnan(v) ? 0xffffffffu : key_from_float(v);
+    const unsigned b = __float_as_uint(v);
+    return (b & 0x7fffffffu) > 0x7f800000u ? 0xffffffffu : key_from_float(v);
 }
 __device__ __forceinline__ void sort3(unsigned &a, unsigned &b, unsigned &c) {
     unsigned lo = min(a, b), hi = max(a, b);
@@ -263,7 +325,7 @@ __device__ __forceinline__ float median9(unsigned a0, unsigned a1, unsigned a2, 
 template <typename T>
 __device__ __forceinline__ float as_f32(T v) { return static_cast<float>(v); }
 template <>
-__device__ __forceinline__ float as_f32<double>(double v) { return __double2float_rn(v); }
+__device__ __forceinline__ float as_f32<double>(double v) { return f64_to_f32(v); }
 
 template <typename T>
 __global__ void median_blur3x3_kernel(const T *__restrict__ in, float *__restrict__ out, long long H,
@@ -293,38 +355,40 @@ constexpr int TX = 32, TY = 8;
 
 __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
-    const double *__restrict__ pts, const int *__restrict__ zero_flag, float *__restrict__ out,
-    long long H, long long W) {
-    __shared__ double raw[TY + 4][TX + 4];
+    const double *__restrict__ pts, ZeroList zl, float *__restrict__ out, long long H, long long W) {
+    __shared__ unsigned long long raw[TY + 4][TX + 4];   // 0: empty cell or outside the image
     __shared__ float filled[TY + 2][TX + 2];
     const long long r0 = static_cast<long long>(blockIdx.y) * TY, c0 = static_cast<long long>(blockIdx.x) * TX;
-    const int zf = *zero_flag;
+    const int hz = *zl.count > 0;
     const int tid = threadIdx.y * TX + threadIdx.x;
     for (int i = tid; i < (TY + 4) * (TX + 4); i += TX * TY) {
         int ly = i / (TX + 4), lx = i - ly * (TX + 4);
         long long r = r0 + ly - 2, c = c0 + lx - 2;
-        double val = __longlong_as_double(0x7ff8000000000000ll);   // outside: not a neighbour
+        unsigned long long k = kEmptyKey;
         if (r >= 0 && r < H && c >= 0 && c < W) {
             long long cell = r * W + c;
-            val = cell_value(vk[cell], cell, first, pts, zf);
+            k = cell_key(vk[cell], cell, first, pts, hz);
         }
-        raw[ly][lx] = val;
+        raw[ly][lx] = k;
     }
     __syncthreads();
     for (int i = tid; i < (TY + 2) * (TX + 2); i += TX * TY) {
         int ly = i / (TX + 2), lx = i - ly * (TX + 2);
-        double val = raw[ly + 1][lx + 1];
-        if (isnan(val)) {
-            double s[8];
+        const unsigned long long k = raw[ly + 1][lx + 1];
+        float f;
+        if (k != kEmptyKey) {
+            f = f64_to_f32(double_from_key(k));
+        } else {
+            unsigned long long s[8];
             int n = 0;
             for (int dj = 0; dj < 3; ++dj)
                 for (int dk = 0; dk < 3; ++dk) {
-                    double u = raw[ly + dj][lx + dk];
-                    if (!isnan(u)) s[n++] = u;
+                    const unsigned long long u = raw[ly + dj][lx + dk];
+                    if (u != kEmptyKey) s[n++] = u;
                 }
-            if (n) val = median_small(s, n);
+            f = n ? f64_to_f32(median_keys(s, n)) : __uint_as_float(0x7fffffffu);
         }
-        filled[ly][lx] = __double2float_rn(val);
+        filled[ly][lx] = f;
     }
     __syncthreads();
     const long long r = r0 + threadIdx.y, c = c0 + threadIdx.x;
@@ -359,13 +423,13 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
     ax.top12 = b >> 52;
     const unsigned e = static_cast<unsigned>((b >> 52) & 0x7ff);
     ax.fast = 0;
-    ax.approx_scale = 0.f;
+    ax.mul = 0;
     if (!(e >= 1 && e <= 2046 && isfinite(res) && res >= 1e-9 && res <= 1e9)) return VS_OK;
     const double ulp = ldexp(1.0, static_cast<int>(e) - 1075);
-    // the thresholds must stay below 2^48 ulps for the 32-bit estimate
-    if (static_cast<double>(n + 1) * res / ulp >= 281474976710656.0) return VS_OK;
+    // thresholds below 2^52 ulps (same-exponent differences) and an estimate multiplier < 2^64
+    if (static_cast<double>(n + 1) * res / ulp >= 4503599627370496.0 || ulp >= res) return VS_OK;
     ax.fast = 1;
-    ax.approx_scale = static_cast<float>(65536.0 * ulp / res);
+    ax.mul = static_cast<unsigned long long>(ldexp(ulp / res, 64));
     const int threads = 256;
     axis_thresholds_kernel<<<static_cast<unsigned>(ceil_div(n + 1, threads)), threads, 0, st>>>(thr, n, ulp, res);
     return check_launch("axis_thresholds_kernel");
@@ -374,7 +438,7 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
 struct RasterWs {
     unsigned long long *keys, *first;   // one grid, reused view after view
     long long *row_thr, *col_thr;
-    int *zero_flag;
+    ZeroList zl;
     size_t bytes;
 };
 
@@ -386,7 +450,8 @@ RasterWs carve_raster(void *ws, long long xsize, long long ysize) {
     r.first = cv.take<unsigned long long>(cells);
     r.row_thr = cv.take<long long>(ysize + 1);
     r.col_thr = cv.take<long long>(xsize + 1);
-    r.zero_flag = cv.take<int>(1);
+    r.zl.entries = cv.take<unsigned long long>(2 * static_cast<size_t>(kZeroCap));
+    r.zl.count = cv.take<int>(1);
     r.bytes = cv.used;
     return r;
 }
@@ -404,7 +469,7 @@ int make_tables(double xoff, double yoff, double xres, double yres, long long xs
 int bin_view(const double *points, const long long *offsets, int v, long long single_n, long long max_points,
              const Tables &tb, RasterWs &w, long long cells, cudaStream_t st) {
     if (cudaMemsetAsync(w.keys, 0, sizeof(unsigned long long) * cells, st) != cudaSuccess ||
-        cudaMemsetAsync(w.zero_flag, 0, sizeof(int), st) != cudaSuccess) {
+        cudaMemsetAsync(w.zl.count, 0, sizeof(int), st) != cudaSuccess) {
         set_error("cudaMemsetAsync failed");
         return VS_ERR_CUDA;
     }
@@ -413,13 +478,18 @@ int bin_view(const double *points, const long long *offsets, int v, long long si
     long long want = ceil_div(ceil_div(max_points, 2), threads);
     long long cap = static_cast<long long>(sm_count()) * 8;
     unsigned gx = static_cast<unsigned>(std::max(1LL, std::min(want, cap)));
-    bin_max_kernel<<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, w.keys, w.zero_flag);
+    bin_max_kernel<<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, w.keys, w.zl);
     VS_LAUNCH_CHECK("bin_max_kernel");
+    const unsigned gl = static_cast<unsigned>(kZeroCap / threads);
+    zero_list_init_kernel<<<gl, threads, 0, st>>>(w.keys, w.first, w.zl);
+    VS_LAUNCH_CHECK("zero_list_init_kernel");
+    zero_list_min_kernel<<<gl, threads, 0, st>>>(w.keys, w.first, w.zl);
+    VS_LAUNCH_CHECK("zero_list_min_kernel");
     unsigned gz = static_cast<unsigned>(std::min<long long>(ceil_div(cells, threads), sm_count() * 8LL));
-    zero_init_kernel<<<gz, threads, 0, st>>>(w.keys, w.first, cells, w.zero_flag);
+    zero_init_kernel<<<gz, threads, 0, st>>>(w.keys, w.first, cells, w.zl);
     VS_LAUNCH_CHECK("zero_init_kernel");
     zero_first_kernel<<<std::max<unsigned>(gx / 4, 1u), threads, 0, st>>>(points, offsets, v, single_n, tb, w.keys,
-                                                                          w.first, w.zero_flag);
+                                                                          w.first, w.zl);
     VS_LAUNCH_CHECK("zero_first_kernel");
     return VS_OK;
 }
@@ -466,7 +536,7 @@ extern "C" int vs_proj_to_grid(const double *points, int64_t n, double xoff, dou
     if (s != VS_OK) return s;
     const int threads = 256;
     unsigned g = static_cast<unsigned>(std::min<long long>(ceil_div(cells, threads), sm_count() * 16LL));
-    decode_kernel<<<g, threads, 0, st>>>(w.keys, w.first, points, w.zero_flag, nanmax, cells);
+    decode_kernel<<<g, threads, 0, st>>>(w.keys, w.first, points, w.zl, nanmax, cells);
     VS_LAUNCH_CHECK("decode_kernel");
     hole_fill_kernel<<<g, threads, 0, st>>>(nanmax, dsm, ysize, xsize, cells);
     VS_LAUNCH_CHECK("hole_fill_kernel");
@@ -502,7 +572,7 @@ extern "C" int vs_dsm_from_points(const double *points, const int64_t *offsets, 
     for (int v = 0; v < n_views; ++v) {
         s = bin_view(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, w, cells, st);
         if (s != VS_OK) return s;
-        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(w.keys, w.first, points, w.zero_flag, dsm + v * cells,
+        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(w.keys, w.first, points, w.zl, dsm + v * cells,
                                                             ysize, xsize);
         VS_LAUNCH_CHECK("dsm_epilogue_kernel");
     }
