@@ -16,8 +16,15 @@
 //
 // Per-cell nanmax: heights become order-preserving 64-bit keys and meet in atomicMax.
 // numpy_groupies (numba flavour, the reference's pinned environment) keeps the first of
-// two equal values, which only shows for +0/-0: zeros share one key and, when a cell's
-// maximum is zero, a second pass finds the first zero of that cell in input order.
+// two equal values, which only shows for +0/-0: zeros share one key, and every zero point
+// also posts its index into a per-cell "first zero" word (atomicMax of a view epoch tag and
+// the complemented index), from which the epilogue takes the sign when a cell's maximum is
+// zero.  The epoch tag makes stale words of earlier views lose without any clearing.
+//
+// GB300 issues FP64 arithmetic, FP64 compares, 64-bit multiply-high and several
+// conversions to a narrow pipe (measured: DADD 1.6, umul64hi 6.4, F2I 15 lane-ops per
+// clock per SM, against ~100 for FFMA and ~136 for 32-bit IMAD), so the per-point and
+// per-cell paths here use 32-bit integer and FP32 operations only.
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -31,15 +38,15 @@ namespace {
 
 constexpr unsigned long long kEmptyKey = 0ull;
 constexpr unsigned long long kZeroKey = 0x8000000000000000ull;   // key of +0.0
-constexpr unsigned long long kNoIndex = ~0ull;
 
 // One axis of the DSM grid.  dir = +1: a = v - off (columns), dir = -1: a = off - v (rows).
 struct Axis {
     double off, res;
     long long n;                 // cells along the axis
     const long long *thr;        // n + 1 integer thresholds (ulps of off), fast path only
-    unsigned long long top12;    // sign + exponent of off
-    unsigned long long mul;      // floor(2^64 * ulp(off) / res): row estimate = mulhi(d, mul)
+    unsigned top12;              // sign + exponent of off
+    unsigned mul;                // floor(2^32 * 2^shift * ulp(off) / res): estimate = mulhi(d >> shift, mul)
+    int shift;
     int neg;                     // off < 0
     int dir;
     int fast;                    // fast path usable
@@ -49,24 +56,23 @@ struct Tables {
     Axis row, col;
 };
 
-__device__ __forceinline__ long long axis_exact(const Axis &ax, double v) {
+__device__ __noinline__ int axis_exact(const Axis &ax, double v) {
     double a = ax.dir > 0 ? __dsub_rn(v, ax.off) : __dsub_rn(ax.off, v);
     double q = __ddiv_rn(a, ax.res);
     if (!(q >= 0.0 && q < static_cast<double>(ax.n))) return -1;
-    return static_cast<long long>(q);   // q >= 0: truncation is floor
+    return static_cast<int>(q);   // q >= 0: truncation is floor
 }
 
 // Cell index along one axis, or -1 when the point falls outside the grid.
-__device__ __forceinline__ long long axis_index(const Axis &ax, double v) {
-    unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
-    if (ax.fast && (b >> 52) == ax.top12) {
-        long long bo = static_cast<long long>(__double_as_longlong(ax.off));
-        long long bv = static_cast<long long>(b);
-        long long d = ((ax.dir > 0) != (ax.neg != 0)) ? (bv - bo) : (bo - bv);
+__device__ __forceinline__ int axis_index(const Axis &ax, double v) {
+    const long long bv = __double_as_longlong(v);
+    const unsigned hi = static_cast<unsigned>(static_cast<unsigned long long>(bv) >> 32);
+    if (ax.fast && (hi >> 20) == ax.top12) {
+        const long long bo = __double_as_longlong(ax.off);
+        const long long d = ((ax.dir > 0) != (ax.neg != 0)) ? (bv - bo) : (bo - bv);
         if (d < 0 || d >= __ldg(ax.thr + ax.n)) return -1;
-        // integer estimate (no conversion instructions: on GB300 they share the FP64 pipe)
-        long long r = static_cast<long long>(__umul64hi(static_cast<unsigned long long>(d), ax.mul));
-        r = r >= ax.n ? ax.n - 1 : r;
+        const unsigned q = static_cast<unsigned>(static_cast<unsigned long long>(d) >> ax.shift);
+        int r = static_cast<int>(min(__umulhi(q, ax.mul), static_cast<unsigned>(ax.n - 1)));
 #pragma unroll 1
         for (int it = 0; it < 8 && __ldg(ax.thr + r) > d; ++it) --r;
 #pragma unroll 1
@@ -98,115 +104,89 @@ __device__ __forceinline__ bool is_nan_bits(unsigned long long b) {
     return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
 }
 
-// Zero heights are collected in a side list during binning: (cell, point index) pairs.
-struct ZeroList {
-    unsigned long long *entries;   // [2 * kZeroCap]: cell, index
-    int *count;                    // number of zero points seen (may exceed kZeroCap)
-};
-constexpr int kZeroCap = 1 << 16;
+// "first zero" words: epoch tag in the top 24 bits, complemented point index below.
+constexpr unsigned long long kIdxMask = (1ull << 40) - 1;
+__host__ __device__ __forceinline__ unsigned long long epoch_tag(int view) {
+    return static_cast<unsigned long long>(view + 1) << 40;
+}
 
-// Pass 1: bin every point of one view and atomicMax its height key into the cell.
-// View v owns points [offsets[v], offsets[v+1]); vk is its key grid.
+constexpr int kPts = 4;   // consecutive points per thread (runs in the same cell merge)
+
+__device__ __forceinline__ void bin_point(const Tables &tb, double x, double y, double z, long long index,
+                                          unsigned long long *vk, unsigned long long *first,
+                                          unsigned long long tag, long long &run_cell,
+                                          unsigned long long &run_key) {
+    const unsigned long long zb = static_cast<unsigned long long>(__double_as_longlong(z));
+    if (is_nan_bits(zb)) return;
+    const int r = axis_index(tb.row, y);
+    if (r < 0) return;
+    const int c = axis_index(tb.col, x);
+    if (c < 0) return;
+    const long long cell = static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(r)) *
+                                                  static_cast<unsigned>(tb.col.n)) + c;
+    unsigned long long key;
+    if ((zb << 1) == 0) {            // +-0: one shared key; the sign comes from the first zero
+        key = kZeroKey;
+        atomicMax(first + cell, tag | (kIdxMask - static_cast<unsigned long long>(index)));
+    } else {
+        key = key_from_double(z);
+    }
+    if (cell == run_cell) {
+        run_key = max(run_key, key);
+    } else {
+        if (run_key) atomicMax(vk + run_cell, run_key);
+        run_cell = cell;
+        run_key = key;
+    }
+}
+
+// Bins one view's points: atomicMax of the height keys into the view's key grid.
+// View v owns points [offsets[v], offsets[v+1]).
 __global__ void __launch_bounds__(256) bin_max_kernel(const double *__restrict__ pts,
                                                       const long long *__restrict__ offsets, int v,
                                                       long long single_n, Tables tb,
-                                                      unsigned long long *__restrict__ vk, ZeroList zl) {
+                                                      unsigned long long *__restrict__ vk,
+                                                      unsigned long long *__restrict__ first) {
     const long long begin = offsets ? offsets[v] : 0;
     const long long end = offsets ? offsets[v + 1] : single_n;
-    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * 2;
-    for (long long i = begin + (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * 2;
-         i < end; i += stride) {
-        double p[6];
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * kPts;
+    const unsigned long long tag = epoch_tag(v);
+    for (long long i = begin + (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kPts; i < end;
+         i += stride) {
+        double p[3 * kPts];
         const double *src = pts + 3 * i;
-        if (i + 1 < end && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+        if (i + kPts <= end && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
             const double2 *s2 = reinterpret_cast<const double2 *>(src);
-            double2 a = __ldcs(s2), b = __ldcs(s2 + 1), c = __ldcs(s2 + 2);
-            p[0] = a.x; p[1] = a.y; p[2] = b.x; p[3] = b.y; p[4] = c.x; p[5] = c.y;
-        } else {
-            p[0] = __ldcs(src); p[1] = __ldcs(src + 1); p[2] = __ldcs(src + 2);
-            if (i + 1 < end) { p[3] = __ldcs(src + 3); p[4] = __ldcs(src + 4); p[5] = __ldcs(src + 5); }
-            else { p[3] = 0.0; p[4] = 0.0; p[5] = __longlong_as_double(0x7ff8000000000000ll); }
-        }
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const double x = p[3 * k], y = p[3 * k + 1], z = p[3 * k + 2];
-            unsigned long long zb = static_cast<unsigned long long>(__double_as_longlong(z));
-            if (is_nan_bits(zb)) continue;
-            long long r = axis_index(tb.row, y);
-            if (r < 0) continue;
-            long long c = axis_index(tb.col, x);
-            if (c < 0) continue;
-            const long long cell = r * tb.col.n + c;
-            unsigned long long key;
-            if ((zb << 1) == 0) {            // +-0: one shared key, sign resolved afterwards
-                key = kZeroKey;
-                const int slot = atomicAdd(zl.count, 1);
-                if (slot < kZeroCap) {
-                    zl.entries[2 * slot] = static_cast<unsigned long long>(cell);
-                    zl.entries[2 * slot + 1] = static_cast<unsigned long long>(i + k);
-                }
-            } else {
-                key = key_from_double(z);
+            for (int k = 0; k < 3 * kPts / 2; ++k) {
+                const double2 a = __ldcs(s2 + k);
+                p[2 * k] = a.x;
+                p[2 * k + 1] = a.y;
             }
-            atomicMax(vk + cell, key);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kPts; ++k) {
+                const bool in = i + k < end;
+                p[3 * k] = in ? __ldcs(src + 3 * k) : 0.0;
+                p[3 * k + 1] = in ? __ldcs(src + 3 * k + 1) : 0.0;
+                p[3 * k + 2] = in ? __ldcs(src + 3 * k + 2) : __longlong_as_double(0x7ff8000000000000ll);
+            }
         }
-    }
-}
-
-// Zero-sign resolution: first[cell] = smallest index of a zero point of a cell whose
-// maximum is zero.  Normally from the side list; a full pass if the list overflowed.
-__global__ void zero_list_init_kernel(const unsigned long long *__restrict__ keys,
-                                      unsigned long long *__restrict__ first, ZeroList zl) {
-    const int n = min(*zl.count, kZeroCap);
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const unsigned long long cell = zl.entries[2 * e];
-        if (keys[cell] == kZeroKey) first[cell] = kNoIndex;
-    }
-}
-
-__global__ void zero_list_min_kernel(const unsigned long long *__restrict__ keys,
-                                     unsigned long long *__restrict__ first, ZeroList zl) {
-    const int n = min(*zl.count, kZeroCap);
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const unsigned long long cell = zl.entries[2 * e];
-        if (keys[cell] == kZeroKey) atomicMin(first + cell, zl.entries[2 * e + 1]);
-    }
-}
-
-__global__ void zero_init_kernel(const unsigned long long *__restrict__ keys,
-                                 unsigned long long *__restrict__ first, long long total, ZeroList zl) {
-    if (*zl.count <= kZeroCap) return;
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < total;
-         c += static_cast<long long>(gridDim.x) * blockDim.x)
-        if (keys[c] == kZeroKey) first[c] = kNoIndex;
-}
-
-__global__ void zero_first_kernel(const double *__restrict__ pts, const long long *__restrict__ offsets, int v,
-                                  long long single_n, Tables tb,
-                                  const unsigned long long *__restrict__ keys,
-                                  unsigned long long *__restrict__ first, ZeroList zl) {
-    if (*zl.count <= kZeroCap) return;
-    const long long begin = offsets ? offsets[v] : 0;
-    const long long end = offsets ? offsets[v + 1] : single_n;
-    for (long long i = begin + blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < end;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        unsigned long long zb = static_cast<unsigned long long>(__double_as_longlong(pts[3 * i + 2]));
-        if ((zb << 1) != 0) continue;
-        long long r = axis_index(tb.row, pts[3 * i + 1]);
-        if (r < 0) continue;
-        long long c = axis_index(tb.col, pts[3 * i]);
-        if (c < 0) continue;
-        long long cell = r * tb.col.n + c;
-        if (keys[cell] == kZeroKey) atomicMin(first + cell, static_cast<unsigned long long>(i));
+        long long run_cell = -1;
+        unsigned long long run_key = 0;
+#pragma unroll
+        for (int k = 0; k < kPts; ++k)
+            bin_point(tb, p[3 * k], p[3 * k + 1], p[3 * k + 2], i + k, vk, first, tag, run_cell, run_key);
+        if (run_key) atomicMax(vk + run_cell, run_key);
     }
 }
 
 // Key of a cell's nanmax with the zero sign resolved (0 = empty cell).
 __device__ __forceinline__ unsigned long long cell_key(unsigned long long k, long long cell,
-                                                       const unsigned long long *first, const double *pts,
-                                                       int has_zero) {
-    if (k == kZeroKey && has_zero) return key_from_double(pts[3 * first[cell] + 2]);
-    return k;
+                                                       const unsigned long long *first, const double *pts) {
+    if (k != kZeroKey) return k;
+    const unsigned long long idx = kIdxMask - (first[cell] & kIdxMask);
+    return key_from_double(pts[3 * idx + 2]);
 }
 
 __device__ __forceinline__ double key_value(unsigned long long k) {
@@ -216,12 +196,10 @@ __device__ __forceinline__ double key_value(unsigned long long k) {
 // nanmax grid (FP64) from the keys.
 __global__ void decode_kernel(const unsigned long long *__restrict__ keys,
                               const unsigned long long *__restrict__ first,
-                              const double *__restrict__ pts, ZeroList zl,
-                              double *__restrict__ out, long long total) {
-    const int hz = *zl.count > 0;
+                              const double *__restrict__ pts, double *__restrict__ out, long long total) {
     for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < total;
          c += static_cast<long long>(gridDim.x) * blockDim.x)
-        out[c] = key_value(cell_key(keys[c], c, first, pts, hz));
+        out[c] = key_value(cell_key(keys[c], c, first, pts));
 }
 
 // numpy's median of the n <= 8 non-NaN neighbour values, given as order-preserving keys:
@@ -276,23 +254,24 @@ __global__ void hole_fill_kernel(const double *__restrict__ in, double *__restri
     }
 }
 
-// Round-to-nearest FP64 -> FP32 (astype(np.float32)) with integer operations; the
-// conversion instruction runs on GB300's narrow FP64 pipe, so it is kept for the
-// float-subnormal range only.
+// Round-to-nearest FP64 -> FP32 (astype(np.float32)) with 32-bit integer operations on the
+// two halves of the double; the conversion instruction runs on GB300's narrow pipe, so it
+// is kept for the float-subnormal range only.
 __device__ __forceinline__ float f64_to_f32(double v) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
-    const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
-    const int e = static_cast<int>((b >> 52) & 0x7ff);
-    const unsigned long long m = b & 0xfffffffffffffull;
-    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));   // inf / NaN
+    const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = static_cast<int>((hi >> 20) & 0x7ffu);
+    const unsigned mhi = hi & 0xfffffu;
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((mhi | lo) ? 0x400000u : 0u));   // inf / NaN
     const int e32 = e - 1023 + 127;
-    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);                          // overflow
-    if (e == 0 && m == 0) return __uint_as_float(sign);                                   // signed zero
-    if (e32 <= 0) return __double2float_rn(v);                                           // float-subnormal range
-    const unsigned m23 = static_cast<unsigned>(m >> 29);
-    const unsigned rem = static_cast<unsigned>(m & 0x1fffffffu);
+    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);                                     // overflow
+    if (e == 0 && (mhi | lo) == 0) return __uint_as_float(sign);                                     // signed zero
+    if (e32 <= 0) return __double2float_rn(v);                                                      // subnormal range
+    const unsigned m23 = (mhi << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
     const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
-    return __uint_as_float(sign | ((static_cast<unsigned>(e32) << 23) + m23 + up));       // carry may round to inf
+    return __uint_as_float(sign | ((static_cast<unsigned>(e32) << 23) + m23 + up));   // carry may round to inf
 }
 
 // ---- 3x3 median blur (float32, replicate border, NaN after every number) -----------------
@@ -353,13 +332,15 @@ __global__ void median_blur3x3_kernel(const T *__restrict__ in, float *__restric
 // 3x3 neighbourhood of each blurred cell's 3x3 neighbourhood).
 constexpr int TX = 32, TY = 8;
 
+// It also clears this tile of the idle key grid (the next view's), which nobody reads
+// concurrently, so no per-view memset is needed.
 __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
-    const double *__restrict__ pts, ZeroList zl, float *__restrict__ out, long long H, long long W) {
+    const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys,
+    long long H, long long W) {
     __shared__ unsigned long long raw[TY + 4][TX + 4];   // 0: empty cell or outside the image
     __shared__ float filled[TY + 2][TX + 2];
     const long long r0 = static_cast<long long>(blockIdx.y) * TY, c0 = static_cast<long long>(blockIdx.x) * TX;
-    const int hz = *zl.count > 0;
     const int tid = threadIdx.y * TX + threadIdx.x;
     for (int i = tid; i < (TY + 4) * (TX + 4); i += TX * TY) {
         int ly = i / (TX + 4), lx = i - ly * (TX + 4);
@@ -367,7 +348,7 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
         unsigned long long k = kEmptyKey;
         if (r >= 0 && r < H && c >= 0 && c < W) {
             long long cell = r * W + c;
-            k = cell_key(vk[cell], cell, first, pts, hz);
+            k = cell_key(vk[cell], cell, first, pts);
         }
         raw[ly][lx] = k;
     }
@@ -393,6 +374,7 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     __syncthreads();
     const long long r = r0 + threadIdx.y, c = c0 + threadIdx.x;
     if (r >= H || c >= W) return;
+    if (next_keys) next_keys[r * W + c] = kEmptyKey;
     // replicate border: clamp the neighbour coordinates into the image
     unsigned k[9];
 #pragma unroll
@@ -410,8 +392,7 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
 }
 
 // ---- host side --------------------------------------------------------------------------
-int make_axis(Axis &ax, double off, double res, long long n, int dir, long long *thr,
-              cudaStream_t st) {
+int make_axis(Axis &ax, double off, double res, long long n, int dir, long long *thr, cudaStream_t st) {
     ax.off = off;
     ax.res = res;
     ax.n = n;
@@ -420,38 +401,44 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
     ax.neg = off < 0;
     unsigned long long b;
     memcpy(&b, &off, sizeof b);
-    ax.top12 = b >> 52;
+    ax.top12 = static_cast<unsigned>(b >> 52);
     const unsigned e = static_cast<unsigned>((b >> 52) & 0x7ff);
     ax.fast = 0;
     ax.mul = 0;
+    ax.shift = 0;
     if (!(e >= 1 && e <= 2046 && isfinite(res) && res >= 1e-9 && res <= 1e9)) return VS_OK;
     const double ulp = ldexp(1.0, static_cast<int>(e) - 1075);
-    // thresholds below 2^52 ulps (same-exponent differences) and an estimate multiplier < 2^64
-    if (static_cast<double>(n + 1) * res / ulp >= 4503599627370496.0 || ulp >= res) return VS_OK;
+    const double dmax = static_cast<double>(n + 1) * res / ulp + 2.0;   // > thr[n]
+    // thresholds below 2^52 ulps (same-exponent differences)
+    if (dmax >= 4503599627370496.0) return VS_OK;
+    int bits = 0;
+    frexp(dmax, &bits);                              // dmax < 2^bits
+    ax.shift = bits > 32 ? bits - 32 : 0;            // d >> shift < 2^32
+    const double m = ldexp(ulp / res, 32 + ax.shift);
+    if (!(m < 4294967296.0)) return VS_OK;
+    ax.mul = static_cast<unsigned>(m);
     ax.fast = 1;
-    ax.mul = static_cast<unsigned long long>(ldexp(ulp / res, 64));
     const int threads = 256;
     axis_thresholds_kernel<<<static_cast<unsigned>(ceil_div(n + 1, threads)), threads, 0, st>>>(thr, n, ulp, res);
     return check_launch("axis_thresholds_kernel");
 }
 
 struct RasterWs {
-    unsigned long long *keys, *first;   // one grid, reused view after view
+    unsigned long long *keys[2];   // key grids, alternating view by view
+    unsigned long long *first;     // "first zero" words (epoch-tagged)
     long long *row_thr, *col_thr;
-    ZeroList zl;
     size_t bytes;
 };
 
-RasterWs carve_raster(void *ws, long long xsize, long long ysize) {
+RasterWs carve_raster(void *ws, long long xsize, long long ysize, bool two_grids) {
     Carver cv(ws);
     RasterWs r;
     const size_t cells = static_cast<size_t>(xsize) * ysize;
-    r.keys = cv.take<unsigned long long>(cells);
+    r.keys[0] = cv.take<unsigned long long>(cells);
+    r.keys[1] = two_grids ? cv.take<unsigned long long>(cells) : r.keys[0];
     r.first = cv.take<unsigned long long>(cells);
     r.row_thr = cv.take<long long>(ysize + 1);
     r.col_thr = cv.take<long long>(xsize + 1);
-    r.zl.entries = cv.take<unsigned long long>(2 * static_cast<size_t>(kZeroCap));
-    r.zl.count = cv.take<int>(1);
     r.bytes = cv.used;
     return r;
 }
@@ -464,33 +451,22 @@ int make_tables(double xoff, double yoff, double xres, double yres, long long xs
     return make_axis(tb.col, xoff, yres, xsize, +1, w.col_thr, st);
 }
 
-// Bins one view's points into the (reset) key grid and resolves zero signs.  Views are
-// processed in stream order so that the key grid being hit by the atomics stays in L2.
-int bin_view(const double *points, const long long *offsets, int v, long long single_n, long long max_points,
-             const Tables &tb, RasterWs &w, long long cells, cudaStream_t st) {
-    if (cudaMemsetAsync(w.keys, 0, sizeof(unsigned long long) * cells, st) != cudaSuccess ||
-        cudaMemsetAsync(w.zl.count, 0, sizeof(int), st) != cudaSuccess) {
+int bin_launch(const double *points, const long long *offsets, int v, long long single_n, long long max_points,
+               const Tables &tb, unsigned long long *keys, unsigned long long *first, cudaStream_t st) {
+    if (max_points <= 0) return VS_OK;
+    const int threads = 256;
+    long long want = ceil_div(ceil_div(max_points, kPts), threads);
+    long long cap = static_cast<long long>(sm_count()) * 8;
+    unsigned gx = static_cast<unsigned>(std::max(1LL, std::min(want, cap)));
+    bin_max_kernel<<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
+    return check_launch("bin_max_kernel");
+}
+
+int clear(void *p, size_t bytes, cudaStream_t st) {
+    if (cudaMemsetAsync(p, 0, bytes, st) != cudaSuccess) {
         set_error("cudaMemsetAsync failed");
         return VS_ERR_CUDA;
     }
-    if (max_points <= 0) return VS_OK;
-    const int threads = 256;
-    long long want = ceil_div(ceil_div(max_points, 2), threads);
-    long long cap = static_cast<long long>(sm_count()) * 8;
-    unsigned gx = static_cast<unsigned>(std::max(1LL, std::min(want, cap)));
-    bin_max_kernel<<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, w.keys, w.zl);
-    VS_LAUNCH_CHECK("bin_max_kernel");
-    const unsigned gl = static_cast<unsigned>(kZeroCap / threads);
-    zero_list_init_kernel<<<gl, threads, 0, st>>>(w.keys, w.first, w.zl);
-    VS_LAUNCH_CHECK("zero_list_init_kernel");
-    zero_list_min_kernel<<<gl, threads, 0, st>>>(w.keys, w.first, w.zl);
-    VS_LAUNCH_CHECK("zero_list_min_kernel");
-    unsigned gz = static_cast<unsigned>(std::min<long long>(ceil_div(cells, threads), sm_count() * 8LL));
-    zero_init_kernel<<<gz, threads, 0, st>>>(w.keys, w.first, cells, w.zl);
-    VS_LAUNCH_CHECK("zero_init_kernel");
-    zero_first_kernel<<<std::max<unsigned>(gx / 4, 1u), threads, 0, st>>>(points, offsets, v, single_n, tb, w.keys,
-                                                                          w.first, w.zl);
-    VS_LAUNCH_CHECK("zero_first_kernel");
     return VS_OK;
 }
 
@@ -510,13 +486,17 @@ using namespace vs;
 
 extern "C" size_t vs_proj_to_grid_workspace_size(int64_t xsize, int64_t ysize) {
     if (xsize <= 0 || ysize <= 0) return 0;
-    return carve_raster(nullptr, xsize, ysize).bytes + sizeof(double) * xsize * ysize + 512;
+    return carve_raster(nullptr, xsize, ysize, false).bytes + sizeof(double) * xsize * ysize + 512;
+}
+
+static bool grid_ok(int64_t xsize, int64_t ysize) {
+    return xsize > 0 && ysize > 0 && xsize < (1LL << 31) && ysize < (1LL << 31);
 }
 
 extern "C" int vs_proj_to_grid(const double *points, int64_t n, double xoff, double yoff,
                                double xresolution, double yresolution, int64_t xsize, int64_t ysize,
                                double *dsm, void *workspace, size_t workspace_bytes, void *stream) {
-    VS_REQUIRE(n >= 0 && xsize > 0 && ysize > 0, "vs_proj_to_grid: bad sizes n=%lld grid=%lldx%lld",
+    VS_REQUIRE(n >= 0 && n < (1LL << 40) && grid_ok(xsize, ysize), "vs_proj_to_grid: bad sizes n=%lld grid=%lldx%lld",
                (long long)n, (long long)xsize, (long long)ysize);
     VS_REQUIRE(dsm && (points || n == 0) && workspace, "vs_proj_to_grid: null pointer");
     const size_t need = vs_proj_to_grid_workspace_size(xsize, ysize);
@@ -525,18 +505,20 @@ extern "C" int vs_proj_to_grid(const double *points, int64_t n, double xoff, dou
         return VS_ERR_WORKSPACE;
     }
     cudaStream_t st = as_stream(stream);
-    RasterWs w = carve_raster(workspace, xsize, ysize);
+    RasterWs w = carve_raster(workspace, xsize, ysize, false);
     Carver cv(workspace);
     cv.used = w.bytes;
     double *nanmax = cv.take<double>(static_cast<size_t>(xsize) * ysize);
     Tables tb;
     const long long cells = xsize * ysize;
     int s = make_tables(xoff, yoff, xresolution, yresolution, xsize, ysize, w, tb, st);
-    if (s == VS_OK) s = bin_view(points, nullptr, 0, n, n, tb, w, cells, st);
+    if (s == VS_OK) s = clear(w.keys[0], sizeof(unsigned long long) * cells, st);
+    if (s == VS_OK) s = clear(w.first, sizeof(unsigned long long) * cells, st);
+    if (s == VS_OK) s = bin_launch(points, nullptr, 0, n, n, tb, w.keys[0], w.first, st);
     if (s != VS_OK) return s;
     const int threads = 256;
     unsigned g = static_cast<unsigned>(std::min<long long>(ceil_div(cells, threads), sm_count() * 16LL));
-    decode_kernel<<<g, threads, 0, st>>>(w.keys, w.first, points, w.zl, nanmax, cells);
+    decode_kernel<<<g, threads, 0, st>>>(w.keys[0], w.first, points, nanmax, cells);
     VS_LAUNCH_CHECK("decode_kernel");
     hole_fill_kernel<<<g, threads, 0, st>>>(nanmax, dsm, ysize, xsize, cells);
     VS_LAUNCH_CHECK("hole_fill_kernel");
@@ -545,15 +527,15 @@ extern "C" int vs_proj_to_grid(const double *points, int64_t n, double xoff, dou
 
 extern "C" size_t vs_dsm_from_points_workspace_size(int n_views, int64_t xsize, int64_t ysize) {
     if (n_views <= 0 || xsize <= 0 || ysize <= 0) return 0;
-    return carve_raster(nullptr, xsize, ysize).bytes + 256;
+    return carve_raster(nullptr, xsize, ysize, true).bytes + 256;
 }
 
 extern "C" int vs_dsm_from_points(const double *points, const int64_t *offsets, int n_views, double xoff,
                                   double yoff, double xresolution, double yresolution, int64_t xsize,
                                   int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
                                   void *stream) {
-    VS_REQUIRE(n_views > 0 && xsize > 0 && ysize > 0, "vs_dsm_from_points: bad sizes views=%d grid=%lldx%lld",
-               n_views, (long long)xsize, (long long)ysize);
+    VS_REQUIRE(n_views > 0 && n_views < (1 << 23) && grid_ok(xsize, ysize),
+               "vs_dsm_from_points: bad sizes views=%d grid=%lldx%lld", n_views, (long long)xsize, (long long)ysize);
     VS_REQUIRE(points && offsets && dsm && workspace, "vs_dsm_from_points: null pointer");
     const size_t need = vs_dsm_from_points_workspace_size(n_views, xsize, ysize);
     if (workspace_bytes < need) {
@@ -561,19 +543,21 @@ extern "C" int vs_dsm_from_points(const double *points, const int64_t *offsets, 
         return VS_ERR_WORKSPACE;
     }
     cudaStream_t st = as_stream(stream);
-    RasterWs w = carve_raster(workspace, xsize, ysize);
+    RasterWs w = carve_raster(workspace, xsize, ysize, true);
     Tables tb;
     const long long cells = xsize * ysize;
     int s = make_tables(xoff, yoff, xresolution, yresolution, xsize, ysize, w, tb, st);
+    if (s == VS_OK) s = clear(w.keys[0], sizeof(unsigned long long) * cells, st);
+    if (s == VS_OK) s = clear(w.first, sizeof(unsigned long long) * cells, st);
     if (s != VS_OK) return s;
     // per-view counts live on the device: launch for a full GPU and let the grid stride
-    const long long launch_points = static_cast<long long>(sm_count()) * 8 * 256 * 2;
+    const long long launch_points = static_cast<long long>(sm_count()) * 8 * 256 * kPts;
     const dim3 egrid(static_cast<unsigned>(ceil_div(xsize, TX)), static_cast<unsigned>(ceil_div(ysize, TY)));
     for (int v = 0; v < n_views; ++v) {
-        s = bin_view(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, w, cells, st);
+        unsigned long long *cur = w.keys[v & 1], *nxt = (v + 1 < n_views) ? w.keys[(v + 1) & 1] : nullptr;
+        s = bin_launch(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, cur, w.first, st);
         if (s != VS_OK) return s;
-        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(w.keys, w.first, points, w.zl, dsm + v * cells,
-                                                            ysize, xsize);
+        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(cur, w.first, points, dsm + v * cells, nxt, ysize, xsize);
         VS_LAUNCH_CHECK("dsm_epilogue_kernel");
     }
     return VS_OK;
