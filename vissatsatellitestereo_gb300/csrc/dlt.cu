@@ -226,32 +226,31 @@ __device__ __forceinline__ void store_block_moments(float (&m)[kMom], float coun
     }
 }
 
-// Normalised coordinates of one kept point from FP64 ENU and double-float pixels.
+// Normalised coordinates of one kept point from FP64 ENU and double-float pixels (FP32 is
+// enough here: the rounding acts like data noise of ~1e-4 px that the fit averages out).
 __device__ __forceinline__ void normalised_point(const NormF &nf, double X, double Y, double Z, df c, df r,
                                                  float &px, float &py, float &pz, float &pc, float &pr) {
-    const df x = centre(split_double(X), nf.cx, nf.inv_s);
-    const df y = centre(split_double(Y), nf.cy, nf.inv_s);
-    const df z = centre(split_double(Z), nf.cz, nf.inv_s);
-    const df cc = centre(c, nf.c0, nf.inv_sp);
-    const df rr = centre(r, nf.r0, nf.inv_sp);
-    px = x.hi + x.lo;
-    py = y.hi + y.lo;
-    pz = z.hi + z.lo;
-    pc = cc.hi + cc.lo;
-    pr = rr.hi + rr.lo;
+    const df x = split_double(X), y = split_double(Y), z = split_double(Z);
+    px = ((x.hi - nf.cx.hi) + (x.lo - nf.cx.lo)) * nf.inv_s.hi;
+    py = ((y.hi - nf.cy.hi) + (y.lo - nf.cy.lo)) * nf.inv_s.hi;
+    pz = ((z.hi - nf.cz.hi) + (z.lo - nf.cz.lo)) * nf.inv_s.hi;
+    pc = ((c.hi - nf.c0.hi) + (c.lo - nf.c0.lo)) * nf.inv_sp.hi;
+    pr = ((r.hi - nf.r0.hi) + (r.lo - nf.r0.lo)) * nf.inv_sp.hi;
 }
 
-// Moments of the drop-in fit: points and (col, row) are given (FP64).  Block b of view v
-// owns points [b * 128 * kChunk, (b + 1) * 128 * kChunk).
+// Moments of the kept points of view v.  Block b owns points [b * 128 * kChunk, ...);
+// (col, row) come as FP64 arrays (drop-in fit) or as the double-floats of the projection
+// pass (fused camera path, in-image mask from the image size).
 __global__ void __launch_bounds__(kMomThreads) moments_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
-    const double *__restrict__ col, const double *__restrict__ row, const uint8_t *__restrict__ keep, long long n,
-    const Norm *__restrict__ norm, double *__restrict__ partial) {
+    const double *__restrict__ col, const double *__restrict__ row, const float4 *__restrict__ colrow,
+    const uint8_t *__restrict__ keep, const float *__restrict__ wh, long long n, const Norm *__restrict__ norm,
+    double *__restrict__ partial) {
     __shared__ double red[(kMomThreads / 32) * kSlots];
     const int v = blockIdx.y;
     const NormF nf = make_normf(norm[v]);
     const double *xv = x + v * xyz_stride, *yv = y + v * xyz_stride, *zv = z + v * xyz_stride;
-    const double *cv = col + v * n, *rv = row + v * n;
+    const float w = wh ? wh[2 * v] : 0.f, h = wh ? wh[2 * v + 1] : 0.f;
     float m[kMom];
 #pragma unroll
     for (int k = 0; k < kMom; ++k) m[k] = 0.0f;
@@ -261,24 +260,34 @@ __global__ void __launch_bounds__(kMomThreads) moments_kernel(
     for (int j = 0; j < kChunk; ++j) {
         const long long i = base + static_cast<long long>(j) * kMomThreads;
         if (i >= n) break;
-        if (keep && !keep[v * n + i]) continue;
+        df c, r;
+        if (colrow) {
+            const float4 cr = colrow[static_cast<long long>(v) * n + i];
+            c = {cr.x, cr.y};
+            r = {cr.z, cr.w};
+            if (!(df_ge0(c) && df_ge0(r) && df_lt(c, w) && df_lt(r, h))) continue;
+        } else {
+            if (keep && !keep[v * n + i]) continue;
+            c = split_double(col[v * n + i]);
+            r = split_double(row[v * n + i]);
+        }
         float px, py, pz, pc, pr;
-        normalised_point(nf, xv[i], yv[i], zv[i], split_double(cv[i]), split_double(rv[i]), px, py, pz, pc, pr);
+        normalised_point(nf, xv[i], yv[i], zv[i], c, r, px, py, pz, pc, pr);
         add_moments(m, px, py, pz, pc, pr);
         count += 1.0f;
     }
     store_block_moments(m, count, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kSlots, red);
 }
 
-// Fused camera path: project the grid through view v's RPC, apply the in-image mask,
-// accumulate the moments and keep the projections (double-float) for the error pass.
+// Projection pass of the fused camera path: (col, row) of every grid point through view
+// v's RPC camera as double-floats.
 template <int MODE>
-__global__ void __launch_bounds__(kMomThreads) project_moments_kernel(
-    const VsRpcCamera *__restrict__ cams, const double *__restrict__ lat, const double *__restrict__ lon,
-    const double *__restrict__ alt, const double *__restrict__ x, const double *__restrict__ y,
-    const double *__restrict__ z, long long n, long long stride, const Norm *__restrict__ norm,
-    double *__restrict__ partial, float4 *__restrict__ colrow) {
-    __shared__ double red[(kMomThreads / 32) * kSlots];
+__global__ void __launch_bounds__(256) project_view_kernel(const VsRpcCamera *__restrict__ cams,
+                                                           const double *__restrict__ lat,
+                                                           const double *__restrict__ lon,
+                                                           const double *__restrict__ alt, long long n,
+                                                           long long stride, float4 *__restrict__ colrow,
+                                                           float *__restrict__ wh) {
     __shared__ VsRpcCamera cam;
     __shared__ RpcFast fast;
     const int v = blockIdx.y;
@@ -288,38 +297,26 @@ __global__ void __launch_bounds__(kMomThreads) project_moments_kernel(
         for (int i = threadIdx.x; i < static_cast<int>(sizeof(VsRpcCamera) / 8); i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
-    if (threadIdx.x == 0) prepare_fast(cam, fast);
+    if (threadIdx.x == 0) {
+        prepare_fast(cam, fast);
+        if (blockIdx.x == 0) wh[2 * v] = fast.width, wh[2 * v + 1] = fast.height;
+    }
     __syncthreads();
-    const NormF nf = make_normf(norm[v]);
     const long long off = v * stride;
-    float m[kMom];
-#pragma unroll
-    for (int k = 0; k < kMom; ++k) m[k] = 0.0f;
-    float count = 0.0f;
-    const long long base = static_cast<long long>(blockIdx.x) * kMomThreads * kChunk + threadIdx.x;
-#pragma unroll 1
-    for (int j = 0; j < kChunk; ++j) {
-        const long long i = base + static_cast<long long>(j) * kMomThreads;
-        if (i >= n) break;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
         df dc, dr;
         if (MODE == VS_PROJ_EXACT) {
             double cc, rr;
-            project_exact(cam, lat[off + i], lon[off + i], alt[off + i], cc, rr);
+            project_exact(cam, __ldcs(lat + off + i), __ldcs(lon + off + i), __ldcs(alt + off + i), cc, rr);
             dc = split_double(cc);
             dr = split_double(rr);
         } else {
-            project_fast(fast, split_double(lat[off + i]), split_double(lon[off + i]), split_double(alt[off + i]),
-                         dc, dr);
+            project_fast(fast, split_double(__ldcs(lat + off + i)), split_double(__ldcs(lon + off + i)),
+                         split_double(__ldcs(alt + off + i)), dc, dr);
         }
         colrow[static_cast<long long>(v) * n + i] = make_float4(dc.hi, dc.lo, dr.hi, dr.lo);
-        const bool k = df_ge0(dc) && df_ge0(dr) && df_lt(dc, fast.width) && df_lt(dr, fast.height);
-        if (!k) continue;
-        float px, py, pz, pc, pr;
-        normalised_point(nf, x[off + i], y[off + i], z[off + i], dc, dr, px, py, pz, pc, pr);
-        add_moments(m, px, py, pz, pc, pr);
-        count += 1.0f;
     }
-    store_block_moments(m, count, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kSlots, red);
 }
 
 // ---- 12x12 solve (one thread per view; FP64) -------------------------------------------
@@ -617,30 +614,47 @@ __global__ void errcam_kernel(const double *K, const double *R, const double *t,
     make_errcam(K + 9 * v, R + 9 * v, t + 3 * v, norm[v], 0.f, 0.f, 1, ec[v]);
 }
 
+// Radix selection over the float bits of the per-point errors (non-negative floats, so
+// the bits order like the values), 11 + 11 + 10 bits.  Targets per view: 0/1 = the
+// low/high middle order statistic of the pixel errors, 2/3 = of the metric errors.
+__host__ __device__ constexpr int digit_bits(int pass) { return pass == 2 ? 10 : 11; }
+__host__ __device__ constexpr int digit_shift(int pass) { return pass == 0 ? 21 : (pass == 1 ? 10 : 0); }
+constexpr int kBins = 2048;
+
 struct ErrWs {
     unsigned *keys;          // [2][V][n] float bits of the per-point errors (kept points only)
     double *sums;            // [V][blocks][3]: pixel sum, metric sum, count
     unsigned *maxk;          // [V][2]
-    unsigned *hist;          // [V][4][256]
-    unsigned *sel;           // [V][4][3]: prefix, mask, k
+    unsigned *hist;          // [V][2][kBins] histogram of the current digit (pixel, metric)
+    unsigned *sel;           // [V][4][3]: prefix, mask, rank
     double *cnt;             // [V]
 };
 
 constexpr int kErrThreads = 256;
 
-__device__ __forceinline__ df dot4(const df *q, df x, df y, df z) {
-    df s = df_add(df_mul(q[0], x), df_mul(q[1], y));
-    s = df_add(s, df_mul(q[2], z));
-    return df_add(s, q[3]);
+// compensated dot product of a double-float 4-vector with (x, y, z, 1), FP32 exact inputs
+__device__ __forceinline__ df dot2(const df *q, float x, float y, float z) {
+    df p0 = two_prod(q[0].hi, x), p1 = two_prod(q[1].hi, y), p2 = two_prod(q[2].hi, z);
+    float err = __fmaf_rn(q[0].lo, x, p0.lo) + __fmaf_rn(q[1].lo, y, p1.lo) + __fmaf_rn(q[2].lo, z, p2.lo) + q[3].lo;
+    df s = two_sum(p0.hi, p1.hi);
+    err += s.lo;
+    s = two_sum(s.hi, p2.hi);
+    err += s.lo;
+    s = two_sum(s.hi, q[3].hi);
+    err += s.lo;
+    return fast_two_sum(s.hi, err);
 }
 
-// Per kept point: pixel reprojection error and metric inverse-projection error.
-//  * reprojection: in the fit's normalised frame, est' = (q1.X', q2.X') / q3.X' in
-//    double-float, minus the normalised observation, times the pixel scale;
-//  * inverse projection: the reference's |scale*ray - cam| is the distance from the camera-
-//    frame point to the ray d = K^-1 [c r 1].  The point lies on the ray through its own
-//    projection, cam = h * K^-1 [c^ r^ 1] with h = (P^ X)_3, so the distance equals
-//    |h| |delta x d| / |d| with delta = K^-1 [c^ - c, r^ - r, 0]: the pixel residual
+// Per kept point: pixel reprojection error and metric inverse-projection error, written
+// as float bits for the median selection, plus block sums/maxima and the histogram of
+// the leading digit.
+//  * reprojection: in the fit's normalised frame, with the ENU point rounded to FP32
+//    (|error| <~ 1e-4 px): h = q.X' by compensated dot products, residual
+//    (h0 - c' h2) / h2 with c' the double-float normalised observation;
+//  * inverse projection: the reference's |scale*ray - cam| is the distance from the
+//    camera-frame point to the ray d = K^-1 [c r 1].  The point lies on the ray through
+//    its own projection, cam = h2 K^-1 [c^ r^ 1], so the distance is
+//    |h2| |delta x d| / |d| with delta = K^-1 [c^ - c, r^ - r, 0]: the pixel residual
 //    enters directly and nothing of the camera's ~1e5-1e6 m depth cancels.
 __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
@@ -648,9 +662,11 @@ __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
     const uint8_t *__restrict__ keep, long long n, const ErrCam *__restrict__ cams, ErrWs w) {
     __shared__ ErrCam ec;
     __shared__ double red[3][kErrThreads / 32];
+    __shared__ unsigned hist[2][kBins];
     const int v = blockIdx.y;
     const int V = gridDim.y;
     if (threadIdx.x == 0) ec = cams[v];
+    for (int i = threadIdx.x; i < 2 * kBins; i += blockDim.x) (&hist[0][0])[i] = 0;
     __syncthreads();
     float ps = 0.0f, is = 0.0f, cnt = 0.0f;
     unsigned pmax = 0, imax = 0;
@@ -671,13 +687,16 @@ __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
         }
         unsigned pk = 0xffffffffu, ik = 0xffffffffu;
         if (k && ec.ok) {
-            const df X = centre(split_double(xv[i]), ec.nf.cx, ec.nf.inv_s);
-            const df Y = centre(split_double(yv[i]), ec.nf.cy, ec.nf.inv_s);
-            const df Z = centre(split_double(zv[i]), ec.nf.cz, ec.nf.inv_s);
-            const df h0 = dot4(ec.q, X, Y, Z), h1 = dot4(ec.q + 4, X, Y, Z), h2 = dot4(ec.q + 8, X, Y, Z);
-            const df ec_ = df_add(df_div(h0, h2), df_mul({-1.0f, 0.0f}, centre(c, ec.nf.c0, ec.nf.inv_sp)));
-            const df er_ = df_add(df_div(h1, h2), df_mul({-1.0f, 0.0f}, centre(r, ec.nf.r0, ec.nf.inv_sp)));
-            const float dc = ec.nf.sp * (ec_.hi + ec_.lo), dr = ec.nf.sp * (er_.hi + er_.lo);
+            float X, Y, Z, cf_, rf_;
+            normalised_point(ec.nf, xv[i], yv[i], zv[i], c, r, X, Y, Z, cf_, rf_);
+            const df h0 = dot2(ec.q, X, Y, Z), h1 = dot2(ec.q + 4, X, Y, Z), h2 = dot2(ec.q + 8, X, Y, Z);
+            // observation in the normalised frame as a double-float: (c - c0) / sp
+            const df cn = df_mul(df_add(c, {-ec.nf.c0.hi, -ec.nf.c0.lo}), ec.nf.inv_sp);
+            const df rn = df_mul(df_add(r, {-ec.nf.r0.hi, -ec.nf.r0.lo}), ec.nf.inv_sp);
+            const df nc = df_add(h0, df_mul({-cn.hi, -cn.lo}, h2));
+            const df nr = df_add(h1, df_mul({-rn.hi, -rn.lo}, h2));
+            const float h2f = h2.hi + h2.lo;
+            const float dc = ec.nf.sp * ((nc.hi + nc.lo) / h2f), dr = ec.nf.sp * ((nr.hi + nr.lo) / h2f);
             const float pe = sqrtf(__fmaf_rn(dr, dr, dc * dc));
             const float *ki = ec.kinv;
             const float cf = c.hi, rf = r.hi;
@@ -688,7 +707,7 @@ __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
             const float e1 = __fmaf_rn(ki[3], dc, ki[4] * dr);
             const float e2 = __fmaf_rn(ki[6], dc, ki[7] * dr);
             const float x0 = e1 * d2 - e2 * d1, x1 = e2 * d0 - e0 * d2, x2 = e0 * d1 - e1 * d0;
-            const float hz = fabsf((h2.hi + h2.lo) / ec.qscale);
+            const float hz = fabsf(h2f / ec.qscale);
             const float ie = hz * sqrtf((x0 * x0 + x1 * x1 + x2 * x2) / (d0 * d0 + d1 * d1 + d2 * d2));
             ps += pe;
             is += ie;
@@ -697,6 +716,8 @@ __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
             ik = __float_as_uint(ie);
             pmax = max(pmax, pk);
             imax = max(imax, ik);
+            atomicAdd(&hist[0][pk >> digit_shift(0)], 1u);
+            atomicAdd(&hist[1][ik >> digit_shift(0)], 1u);
         }
         w.keys[static_cast<long long>(v) * n + i] = pk;
         w.keys[(static_cast<long long>(V) + v) * n + i] = ik;
@@ -723,6 +744,10 @@ __global__ void __launch_bounds__(kErrThreads) error_points_kernel(
         for (int i = 0; i < kErrThreads / 32; ++i) s += red[threadIdx.x][i];
         w.sums[(static_cast<long long>(v) * gridDim.x + blockIdx.x) * 3 + threadIdx.x] = s;
     }
+    for (int i = threadIdx.x; i < 2 * kBins; i += blockDim.x) {
+        const unsigned c = (&hist[0][0])[i];
+        if (c) atomicAdd(w.hist + static_cast<long long>(v) * 2 * kBins + i, c);
+    }
 }
 
 // per-view totals of the block sums (fixed order) and the selection ranks
@@ -741,12 +766,13 @@ __global__ void error_count_kernel(ErrWs w, int n_views, int n_blocks) {
     }
 }
 
-// Radix selection of the two middle order statistics of both error arrays, 8 bits a pass.
-// Targets per view: 0/1 = low/high middle of the pixel errors, 2/3 = of the metric errors.
-__global__ void __launch_bounds__(256) select_hist_kernel(ErrWs w, long long n, int shift) {
-    __shared__ unsigned h[4][256];
+// Histograms of digit `pass` (1, 2) of the keys matching each target's prefix.
+__global__ void __launch_bounds__(256) select_hist_kernel(ErrWs w, long long n, int pass) {
+    __shared__ unsigned h[4][kBins];
     const int v = blockIdx.y, V = gridDim.y;
-    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&h[0][0])[i] = 0;
+    const int shift = digit_shift(pass);
+    const unsigned dmask = (1u << digit_bits(pass)) - 1u;
+    for (int i = threadIdx.x; i < 4 * kBins; i += blockDim.x) (&h[0][0])[i] = 0;
     __syncthreads();
     unsigned pre[4], msk[4];
     for (int t = 0; t < 4; ++t) pre[t] = w.sel[3 * (v * 4 + t)], msk[t] = w.sel[3 * (v * 4 + t) + 1];
@@ -754,33 +780,48 @@ __global__ void __launch_bounds__(256) select_hist_kernel(ErrWs w, long long n, 
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
         const unsigned kp = w.keys[static_cast<long long>(v) * n + i];
         const unsigned kq = w.keys[(static_cast<long long>(V) + v) * n + i];
-        const unsigned dp = (kp >> shift) & 255u, dq = (kq >> shift) & 255u;
+        const unsigned dp = (kp >> shift) & dmask, dq = (kq >> shift) & dmask;
         if ((kp & msk[0]) == pre[0]) atomicAdd(&h[0][dp], 1u);
-        if ((kp & msk[1]) == pre[1]) atomicAdd(&h[1][dp], 1u);
+        if ((kp & msk[1]) == pre[1] && pre[1] != pre[0]) atomicAdd(&h[1][dp], 1u);
         if ((kq & msk[2]) == pre[2]) atomicAdd(&h[2][dq], 1u);
-        if ((kq & msk[3]) == pre[3]) atomicAdd(&h[3][dq], 1u);
+        if ((kq & msk[3]) == pre[3] && pre[3] != pre[2]) atomicAdd(&h[3][dq], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) {
+    for (int i = threadIdx.x; i < 4 * kBins; i += blockDim.x) {
         const unsigned c = (&h[0][0])[i];
-        if (c) atomicAdd(w.hist + v * 1024 + i, c);
+        if (c) atomicAdd(w.hist + static_cast<long long>(v) * 4 * kBins + i, c);
     }
 }
 
-__global__ void select_step_kernel(ErrWs w, int n_views, int shift) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_views * 4) return;
-    unsigned *hist = w.hist + i * 256;
-    unsigned k = w.sel[3 * i + 2];
-    unsigned d = 0, below = 0;
-    for (; d < 255; ++d) {
-        if (below + hist[d] > k) break;
-        below += hist[d];
+// Picks the digit of the four targets of one view (one thread per view, so every prefix is
+// read before any is updated).  Pass 0 reads the two histograms the error kernel built
+// (pixel, metric); later passes read one histogram per target, except that the high
+// target shares its low partner's histogram while their prefixes agree.
+__global__ void select_step_kernel(ErrWs w, int n_views, int pass) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_views) return;
+    unsigned pre[4];
+    for (int t = 0; t < 4; ++t) pre[t] = w.sel[3 * (v * 4 + t)];
+    const int bins = 1 << digit_bits(pass);
+    for (int t = 0; t < 4; ++t) {
+        const int i = v * 4 + t;
+        const unsigned *hist;
+        if (pass == 0) {
+            hist = w.hist + static_cast<long long>(v) * 2 * kBins + (t >> 1) * kBins;
+        } else {
+            const bool shared_h = (t & 1) && pre[t] == pre[t ^ 1];
+            hist = w.hist + static_cast<long long>(v) * 4 * kBins + (shared_h ? (t ^ 1) : t) * kBins;
+        }
+        unsigned k = w.sel[3 * i + 2];
+        unsigned d = 0, below = 0;
+        for (; d < static_cast<unsigned>(bins - 1); ++d) {
+            if (below + hist[d] > k) break;
+            below += hist[d];
+        }
+        w.sel[3 * i] = pre[t] | (d << digit_shift(pass));
+        w.sel[3 * i + 1] |= static_cast<unsigned>(bins - 1) << digit_shift(pass);
+        w.sel[3 * i + 2] = k - below;
     }
-    w.sel[3 * i] |= d << shift;
-    w.sel[3 * i + 1] |= 255u << shift;
-    w.sel[3 * i + 2] = k - below;
-    for (int j = 0; j < 256; ++j) hist[j] = 0;
 }
 
 __global__ void error_final_kernel(ErrWs w, int n_views, int n_blocks, double *err) {
@@ -804,8 +845,8 @@ __global__ void error_final_kernel(ErrWs w, int n_views, int n_blocks, double *e
 }
 
 int err_blocks(long long n) {
-    long long want = ceil_div(n, kErrThreads);
-    return static_cast<int>(std::max<long long>(1, std::min<long long>(want, sm_count() * 4LL)));
+    long long want = ceil_div(n, kErrThreads * 4);
+    return static_cast<int>(std::max<long long>(1, std::min<long long>(want, sm_count() * 2LL)));
 }
 
 ErrWs carve_err(Carver &cv, int V, long long n, int blocks) {
@@ -813,7 +854,7 @@ ErrWs carve_err(Carver &cv, int V, long long n, int blocks) {
     w.keys = cv.take<unsigned>(2 * static_cast<size_t>(V) * n);
     w.sums = cv.take<double>(static_cast<size_t>(V) * blocks * 3);
     w.maxk = cv.take<unsigned>(2 * V);
-    w.hist = cv.take<unsigned>(static_cast<size_t>(V) * 1024);
+    w.hist = cv.take<unsigned>(static_cast<size_t>(V) * 4 * kBins);
     w.sel = cv.take<unsigned>(static_cast<size_t>(V) * 12);
     w.cnt = cv.take<double>(V);
     return w;
@@ -823,8 +864,9 @@ int run_error_stats(const double *x, const double *y, const double *z, long long
                     const double *row, const float4 *colrow, const uint8_t *keep, int V, long long n,
                     const ErrCam *cams, double *err, ErrWs &w, cudaStream_t st) {
     const int blocks = err_blocks(n);
+    const size_t hist_bytes = sizeof(unsigned) * 4 * kBins * V;
     if (cudaMemsetAsync(w.maxk, 0, sizeof(unsigned) * 2 * V, st) != cudaSuccess ||
-        cudaMemsetAsync(w.hist, 0, sizeof(unsigned) * 1024 * V, st) != cudaSuccess) {
+        cudaMemsetAsync(w.hist, 0, hist_bytes, st) != cudaSuccess) {
         set_error("cudaMemsetAsync failed");
         return VS_ERR_CUDA;
     }
@@ -839,11 +881,16 @@ int run_error_stats(const double *x, const double *y, const double *z, long long
     const unsigned vg = static_cast<unsigned>(ceil_div(V, 128));
     error_count_kernel<<<vg, 128, 0, st>>>(w, V, blocks);
     VS_LAUNCH_CHECK("error_count_kernel");
-    const unsigned sg = static_cast<unsigned>(ceil_div(V * 4, 128));
-    for (int shift = 24; shift >= 0 && n > 0; shift -= 8) {
-        select_hist_kernel<<<dim3(blocks, V), 256, 0, st>>>(w, n, shift);
-        VS_LAUNCH_CHECK("select_hist_kernel");
-        select_step_kernel<<<sg, 128, 0, st>>>(w, V, shift);
+    for (int pass = 0; pass < 3 && n > 0; ++pass) {
+        if (pass > 0) {
+            if (cudaMemsetAsync(w.hist, 0, hist_bytes, st) != cudaSuccess) {
+                set_error("cudaMemsetAsync failed");
+                return VS_ERR_CUDA;
+            }
+            select_hist_kernel<<<dim3(blocks, V), 256, 0, st>>>(w, n, pass);
+            VS_LAUNCH_CHECK("select_hist_kernel");
+        }
+        select_step_kernel<<<vg, 128, 0, st>>>(w, V, pass);
         VS_LAUNCH_CHECK("select_step_kernel");
     }
     error_final_kernel<<<vg, 128, 0, st>>>(w, V, blocks, err);
@@ -868,6 +915,7 @@ struct FitWs {
     double *partial;
     ErrCam *errcam;
     float4 *colrow;
+    float *wh;
 };
 
 FitWs carve_fit(Carver &cv, int V, long long n, bool fused) {
@@ -877,6 +925,7 @@ FitWs carve_fit(Carver &cv, int V, long long n, bool fused) {
     f.partial = cv.take<double>(static_cast<size_t>(V) * mom_blocks(n) * kSlots);
     f.errcam = cv.take<ErrCam>(V);
     f.colrow = fused ? cv.take<float4>(static_cast<size_t>(V) * n) : nullptr;
+    f.wh = cv.take<float>(2 * static_cast<size_t>(V));
     return f;
 }
 
@@ -942,8 +991,8 @@ extern "C" int vs_dlt_fit(const double *x, const double *y, const double *z, int
     int s = launch_norm(x, y, z, xyz_stride, col, row, keep, nullptr, n_views, n, f, st);
     if (s != VS_OK) return s;
     const int blocks = mom_blocks(n);
-    moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, xyz_stride, col, row, keep, n, f.norm,
-                                                                   f.partial);
+    moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, xyz_stride, col, row, nullptr, keep,
+                                                                   nullptr, n, f.norm, f.partial);
     VS_LAUNCH_CHECK("moments_kernel");
     solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, nullptr, K, R, t, nullptr, nullptr, status);
     VS_LAUNCH_CHECK("solve_kernel");
@@ -1017,13 +1066,19 @@ extern "C" int vs_camera_approx_perspective(const VsRpcCamera *cams, int n_views
     int s = launch_norm(x, y, z, point_stride, nullptr, nullptr, nullptr, cams, n_views, n, f, st);
     if (s != VS_OK) return s;
     const int blocks = mom_blocks(n);
-    if (proj_mode == VS_PROJ_EXACT)
-        project_moments_kernel<VS_PROJ_EXACT><<<dim3(blocks, n_views), kMomThreads, 0, st>>>(
-            cams, lat, lon, alt, x, y, z, n, point_stride, f.norm, f.partial, f.colrow);
-    else
-        project_moments_kernel<VS_PROJ_FAST><<<dim3(blocks, n_views), kMomThreads, 0, st>>>(
-            cams, lat, lon, alt, x, y, z, n, point_stride, f.norm, f.partial, f.colrow);
-    VS_LAUNCH_CHECK("project_moments_kernel");
+    if (n > 0) {
+        const unsigned pg = static_cast<unsigned>(std::min<long long>(ceil_div(n, 256), sm_count() * 8LL / n_views + 8));
+        if (proj_mode == VS_PROJ_EXACT)
+            project_view_kernel<VS_PROJ_EXACT><<<dim3(pg, n_views), 256, 0, st>>>(cams, lat, lon, alt, n,
+                                                                                  point_stride, f.colrow, f.wh);
+        else
+            project_view_kernel<VS_PROJ_FAST><<<dim3(pg, n_views), 256, 0, st>>>(cams, lat, lon, alt, n,
+                                                                                 point_stride, f.colrow, f.wh);
+        VS_LAUNCH_CHECK("project_view_kernel");
+    }
+    moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, point_stride, nullptr, nullptr, f.colrow,
+                                                                   nullptr, f.wh, n, f.norm, f.partial);
+    VS_LAUNCH_CHECK("moments_kernel");
     solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, cams, K, R, t, params, f.errcam, status);
     VS_LAUNCH_CHECK("solve_kernel");
     if (!err) return VS_OK;

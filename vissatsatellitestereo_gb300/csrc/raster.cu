@@ -44,9 +44,11 @@ struct Axis {
     double off, res;
     long long n;                 // cells along the axis
     const long long *thr;        // n + 1 integer thresholds (ulps of off), fast path only
+    long long tmax;              // thr[n]: first difference beyond the grid
     unsigned top12;              // sign + exponent of off
-    unsigned mul;                // floor(2^32 * 2^shift * ulp(off) / res): estimate = mulhi(d >> shift, mul)
-    int shift;
+    int shift;                   // d >> shift < 2^32
+    float scale;                 // 2^shift * ulp(off) / res, so that q ~ (d >> shift) * scale
+    float err_abs, err_rel;      // bound of |q - d * ulp / res|: err_abs + err_rel * q
     int neg;                     // off < 0
     int dir;
     int fast;                    // fast path usable
@@ -63,16 +65,25 @@ __device__ __noinline__ int axis_exact(const Axis &ax, double v) {
     return static_cast<int>(q);   // q >= 0: truncation is floor
 }
 
-// Cell index along one axis, or -1 when the point falls outside the grid.
+// Cell index along one axis, or -1 when the point falls outside the grid.  The FP32
+// estimate q carries a proven error bound; unless q lies within that bound of an integer,
+// its floor is the reference's floor(fl(d*ulp/res)).  Near a boundary the integer
+// threshold table decides (about 0.1% of points).
 __device__ __forceinline__ int axis_index(const Axis &ax, double v) {
     const long long bv = __double_as_longlong(v);
     const unsigned hi = static_cast<unsigned>(static_cast<unsigned long long>(bv) >> 32);
     if (ax.fast && (hi >> 20) == ax.top12) {
         const long long bo = __double_as_longlong(ax.off);
         const long long d = ((ax.dir > 0) != (ax.neg != 0)) ? (bv - bo) : (bo - bv);
-        if (d < 0 || d >= __ldg(ax.thr + ax.n)) return -1;
-        const unsigned q = static_cast<unsigned>(static_cast<unsigned long long>(d) >> ax.shift);
-        int r = static_cast<int>(min(__umulhi(q, ax.mul), static_cast<unsigned>(ax.n - 1)));
+        if (d < 0 || d >= ax.tmax) return -1;
+        const unsigned u = static_cast<unsigned>(static_cast<unsigned long long>(d) >> ax.shift);
+        const float q = __fmul_rn(__uint2float_rn(u), ax.scale);
+        const float big = __fadd_rn(q, 12582912.0f);                  // 1.5 * 2^23: rounds q to an integer
+        const float rn = __fsub_rn(big, 12582912.0f);
+        const float fr = __fsub_rn(q, rn);                            // exact, in [-0.5, 0.5]
+        int r = (__float_as_int(big) - 0x4b400000) - (fr < 0.0f ? 1 : 0);
+        if (fabsf(fr) > __fmaf_rn(ax.err_rel, q, ax.err_abs)) return min(max(r, 0), static_cast<int>(ax.n - 1));
+        r = min(max(r, 0), static_cast<int>(ax.n - 1));
 #pragma unroll 1
         for (int it = 0; it < 8 && __ldg(ax.thr + r) > d; ++it) --r;
 #pragma unroll 1
@@ -329,69 +340,84 @@ __global__ void median_blur3x3_kernel(const T *__restrict__ in, float *__restric
 
 // ---- fused produce_dsm epilogue: keys -> nanmax -> hole fill -> float32 -> blur ---------
 // One 32x8 output tile per CTA; the key tile carries a 2-cell halo (hole fill needs the
-// 3x3 neighbourhood of each blurred cell's 3x3 neighbourhood).
+// 3x3 neighbourhood of each blurred cell's 3x3 neighbourhood).  32-bit indexing (grid
+// dimensions < 2^31); the hole-filled float32 values are staged as blur keys.
 constexpr int TX = 32, TY = 8;
+
+// The hole-filled, float32-rounded value of the tile cell whose 3x3 neighbourhood sits at
+// raw[ly..ly+2][lx..lx+2], as a blur key.
+__device__ __forceinline__ unsigned filled_key(const unsigned long long (*raw)[TX + 4], int ly, int lx) {
+    const unsigned long long k = raw[ly + 1][lx + 1];
+    float f;
+    if (k != kEmptyKey) {
+        f = f64_to_f32(double_from_key(k));
+    } else {
+        unsigned long long s[8];
+        int n = 0;
+#pragma unroll
+        for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 3; ++dk) {
+                const unsigned long long u = raw[ly + dj][lx + dk];
+                if (u != kEmptyKey) s[n++] = u;
+            }
+        if (!n) return 0xffffffffu;                    // stays NaN
+        f = f64_to_f32(median_keys(s, n));
+    }
+    return blur_key(f);
+}
 
 // It also clears this tile of the idle key grid (the next view's), which nobody reads
 // concurrently, so no per-view memset is needed.
 __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
-    const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys,
-    long long H, long long W) {
+    const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys, int H,
+    int W) {
     __shared__ unsigned long long raw[TY + 4][TX + 4];   // 0: empty cell or outside the image
-    __shared__ float filled[TY + 2][TX + 2];
-    const long long r0 = static_cast<long long>(blockIdx.y) * TY, c0 = static_cast<long long>(blockIdx.x) * TX;
+    __shared__ unsigned fk[TY + 2][TX + 2];              // blur keys of the hole-filled cells
+    const int r0 = blockIdx.y * TY, c0 = blockIdx.x * TX;
     const int tid = threadIdx.y * TX + threadIdx.x;
     for (int i = tid; i < (TY + 4) * (TX + 4); i += TX * TY) {
-        int ly = i / (TX + 4), lx = i - ly * (TX + 4);
-        long long r = r0 + ly - 2, c = c0 + lx - 2;
+        const int ly = i / (TX + 4), lx = i - ly * (TX + 4);
+        const int r = r0 + ly - 2, c = c0 + lx - 2;
         unsigned long long k = kEmptyKey;
         if (r >= 0 && r < H && c >= 0 && c < W) {
-            long long cell = r * W + c;
+            const long long cell = static_cast<long long>(r) * W + c;
             k = cell_key(vk[cell], cell, first, pts);
         }
         raw[ly][lx] = k;
     }
     __syncthreads();
     for (int i = tid; i < (TY + 2) * (TX + 2); i += TX * TY) {
-        int ly = i / (TX + 2), lx = i - ly * (TX + 2);
-        const unsigned long long k = raw[ly + 1][lx + 1];
-        float f;
-        if (k != kEmptyKey) {
-            f = f64_to_f32(double_from_key(k));
-        } else {
-            unsigned long long s[8];
-            int n = 0;
-            for (int dj = 0; dj < 3; ++dj)
-                for (int dk = 0; dk < 3; ++dk) {
-                    const unsigned long long u = raw[ly + dj][lx + dk];
-                    if (u != kEmptyKey) s[n++] = u;
-                }
-            f = n ? f64_to_f32(median_keys(s, n)) : __uint_as_float(0x7fffffffu);
-        }
-        filled[ly][lx] = f;
+        const int ly = i / (TX + 2), lx = i - ly * (TX + 2);
+        fk[ly][lx] = filled_key(raw, ly, lx);
     }
     __syncthreads();
-    const long long r = r0 + threadIdx.y, c = c0 + threadIdx.x;
+    const int r = r0 + threadIdx.y, c = c0 + threadIdx.x;
     if (r >= H || c >= W) return;
-    if (next_keys) next_keys[r * W + c] = kEmptyKey;
-    // replicate border: clamp the neighbour coordinates into the image
-    unsigned k[9];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        long long rr = r + a - 1;
-        rr = rr < 0 ? 0 : (rr >= H ? H - 1 : rr);
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            long long cc = c + b - 1;
-            cc = cc < 0 ? 0 : (cc >= W ? W - 1 : cc);
-            k[3 * b + a] = blur_key(filled[rr - r0 + 1][cc - c0 + 1]);
-        }
-    }
-    out[r * W + c] = median9(k[0], k[1], k[2], k[3], k[4], k[5], k[6], k[7], k[8]);
+    const long long cell = static_cast<long long>(r) * W + c;
+    if (next_keys) next_keys[cell] = kEmptyKey;
+    int ya = threadIdx.y, yb = threadIdx.y + 1, yc = threadIdx.y + 2;
+    int xa = threadIdx.x, xb = threadIdx.x + 1, xc = threadIdx.x + 2;
+    if (r == 0) ya = yb;                 // replicate border: clamp the neighbours into the image
+    if (r == H - 1) yc = yb;
+    if (c == 0) xa = xb;
+    if (c == W - 1) xc = xb;
+    out[cell] = median9(fk[ya][xa], fk[yb][xa], fk[yc][xa], fk[ya][xb], fk[yb][xb], fk[yc][xb], fk[ya][xc],
+                        fk[yb][xc], fk[yc][xc]);
 }
 
 // ---- host side --------------------------------------------------------------------------
+// Host copy of the threshold search of axis_thresholds_kernel (same IEEE FP64 expression).
+long long host_threshold(long long r, double ulp, double res) {
+    const double rd = static_cast<double>(r);
+    long long d = static_cast<long long>(ceil(rd * res / ulp));
+    if (d < 0) d = 0;
+    for (int it = 0; it < 64 && d > 0 && floor((static_cast<double>(d - 1) * ulp) / res) >= rd; ++it) --d;
+    for (int it = 0; it < 64 && floor((static_cast<double>(d) * ulp) / res) < rd; ++it) ++d;
+    return d;
+}
+
 int make_axis(Axis &ax, double off, double res, long long n, int dir, long long *thr, cudaStream_t st) {
     ax.off = off;
     ax.res = res;
@@ -404,19 +430,25 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
     ax.top12 = static_cast<unsigned>(b >> 52);
     const unsigned e = static_cast<unsigned>((b >> 52) & 0x7ff);
     ax.fast = 0;
-    ax.mul = 0;
     ax.shift = 0;
-    if (!(e >= 1 && e <= 2046 && isfinite(res) && res >= 1e-9 && res <= 1e9)) return VS_OK;
+    ax.scale = 0.f;
+    ax.err_abs = ax.err_rel = 0.f;
+    ax.tmax = 0;
+    // the FP32 estimate needs cell indices below 2^22 and sane resolutions
+    if (!(e >= 1 && e <= 2046 && isfinite(res) && res >= 1e-9 && res <= 1e9 && n < (1LL << 22))) return VS_OK;
     const double ulp = ldexp(1.0, static_cast<int>(e) - 1075);
     const double dmax = static_cast<double>(n + 1) * res / ulp + 2.0;   // > thr[n]
-    // thresholds below 2^52 ulps (same-exponent differences)
-    if (dmax >= 4503599627370496.0) return VS_OK;
+    if (dmax >= 4503599627370496.0) return VS_OK;                       // differences below 2^52 ulps
     int bits = 0;
     frexp(dmax, &bits);                              // dmax < 2^bits
     ax.shift = bits > 32 ? bits - 32 : 0;            // d >> shift < 2^32
-    const double m = ldexp(ulp / res, 32 + ax.shift);
-    if (!(m < 4294967296.0)) return VS_OK;
-    ax.mul = static_cast<unsigned>(m);
+    const double scale = ldexp(ulp / res, ax.shift);
+    ax.scale = static_cast<float>(scale);
+    // |q - d*ulp/res| <= dropped low bits (< 2^shift ulps) + rounding of u, scale and the
+    // product (3 x 2^-24 relative), plus the half-ulp of the reference's own FP64 quotient
+    ax.err_abs = static_cast<float>(1.01 * scale + 1e-9);
+    ax.err_rel = static_cast<float>(4.0 * ldexp(1.0, -24));
+    ax.tmax = host_threshold(n, ulp, res);
     ax.fast = 1;
     const int threads = 256;
     axis_thresholds_kernel<<<static_cast<unsigned>(ceil_div(n + 1, threads)), threads, 0, st>>>(thr, n, ulp, res);
@@ -557,7 +589,8 @@ extern "C" int vs_dsm_from_points(const double *points, const int64_t *offsets, 
         unsigned long long *cur = w.keys[v & 1], *nxt = (v + 1 < n_views) ? w.keys[(v + 1) & 1] : nullptr;
         s = bin_launch(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, cur, w.first, st);
         if (s != VS_OK) return s;
-        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(cur, w.first, points, dsm + v * cells, nxt, ysize, xsize);
+        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(cur, w.first, points, dsm + v * cells, nxt,
+                                                            static_cast<int>(ysize), static_cast<int>(xsize));
         VS_LAUNCH_CHECK("dsm_epilogue_kernel");
     }
     return VS_OK;
