@@ -7,7 +7,7 @@
 // The fit solves the reference's problem -- the unit vector p minimising |A p| for the
 // 2N x 12 DLT matrix A -- without forming A.  A^T A only depends on 40 point moments
 // (sum X X^T weighted by 1, c, r, c^2 + r^2 with X = [x y z 1]), so one streaming pass
-// accumulates them in coordinates centred and scaled per view (FP32 sums over at most 32
+// accumulates them in coordinates centred and scaled per view (FP32 sums over at most 16
 // points per thread and across a warp, FP64 beyond).  The 12x12 problem is then solved in
 // FP64 by inverse iteration on the normalised Gram matrix, with the centring/scaling map M
 // applied exactly, so the minimiser is the reference's un-normalised one.  Factorisation is
@@ -187,7 +187,7 @@ __device__ __forceinline__ df centre(df v, df off, df inv) { return df_mul(df_ad
 constexpr int kMom = 40;            // 4 weights x 10 unique entries of X X^T
 constexpr int kSlots = 41;          // + kept-point count
 constexpr int kMomThreads = 128;
-constexpr int kChunk = 32;          // points per thread (FP32 partial sums)
+constexpr int kChunk = 16;          // points per thread (FP32 partial sums)
 
 // Accumulates one point's 40 moment terms into FP32 partial sums.
 __device__ __forceinline__ void add_moments(float (&m)[kMom], float x, float y, float z, float c, float r) {
@@ -793,34 +793,57 @@ __global__ void __launch_bounds__(256) select_hist_kernel(ErrWs w, long long n, 
     }
 }
 
-// Picks the digit of the four targets of one view (one thread per view, so every prefix is
-// read before any is updated).  Pass 0 reads the two histograms the error kernel built
-// (pixel, metric); later passes read one histogram per target, except that the high
-// target shares its low partner's histogram while their prefixes agree.
-__global__ void select_step_kernel(ErrWs w, int n_views, int pass) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n_views) return;
-    unsigned pre[4];
-    for (int t = 0; t < 4; ++t) pre[t] = w.sel[3 * (v * 4 + t)];
+// Picks the digit of the four targets of one view: one block per view, one warp per
+// target, the bins scanned 32 at a time with warp prefix sums.  Every prefix is read
+// before the barrier and written after it.  Pass 0 reads the two histograms the error
+// kernel built (pixel, metric); later passes read one histogram per target, except that
+// the high target shares its low partner's histogram while their prefixes agree.
+__global__ void __launch_bounds__(128) select_step_kernel(ErrWs w, int pass) {
+    const int v = blockIdx.x;
+    const int t = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = v * 4 + t;
+    __shared__ unsigned pre[4];
+    if (lane == 0) pre[t] = w.sel[3 * i];
+    __syncthreads();
+    const unsigned *hist;
+    if (pass == 0) {
+        hist = w.hist + static_cast<long long>(v) * 2 * kBins + (t >> 1) * kBins;
+    } else {
+        const bool shared_h = (t & 1) && pre[t] == pre[t ^ 1];
+        hist = w.hist + static_cast<long long>(v) * 4 * kBins + (shared_h ? (t ^ 1) : t) * kBins;
+    }
     const int bins = 1 << digit_bits(pass);
-    for (int t = 0; t < 4; ++t) {
-        const int i = v * 4 + t;
-        const unsigned *hist;
-        if (pass == 0) {
-            hist = w.hist + static_cast<long long>(v) * 2 * kBins + (t >> 1) * kBins;
-        } else {
-            const bool shared_h = (t & 1) && pre[t] == pre[t ^ 1];
-            hist = w.hist + static_cast<long long>(v) * 4 * kBins + (shared_h ? (t ^ 1) : t) * kBins;
+    const unsigned k = w.sel[3 * i + 2];
+    unsigned below = 0;          // count of keys in earlier chunks
+    int digit = -1;
+    unsigned skip = 0;
+    for (int base = 0; base < bins; base += 32) {
+        const unsigned c = hist[base + lane];
+        unsigned incl = c;       // inclusive warp scan
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned u = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += u;
         }
-        unsigned k = w.sel[3 * i + 2];
-        unsigned d = 0, below = 0;
-        for (; d < static_cast<unsigned>(bins - 1); ++d) {
-            if (below + hist[d] > k) break;
-            below += hist[d];
+        const unsigned excl = incl - c;
+        const unsigned hit = __ballot_sync(0xffffffffu, below + incl > k);
+        if (hit) {
+            const int l = __ffs(hit) - 1;
+            digit = base + l;
+            skip = below + __shfl_sync(0xffffffffu, excl, l);
+            break;
         }
-        w.sel[3 * i] = pre[t] | (d << digit_shift(pass));
+        below += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (digit < 0) {             // rank beyond the counts (no kept points): the last bin
+        digit = bins - 1;
+        skip = below - hist[bins - 1];
+    }
+    __syncthreads();
+    if (lane == 0) {
+        w.sel[3 * i] = pre[t] | (static_cast<unsigned>(digit) << digit_shift(pass));
         w.sel[3 * i + 1] |= static_cast<unsigned>(bins - 1) << digit_shift(pass);
-        w.sel[3 * i + 2] = k - below;
+        w.sel[3 * i + 2] = k - skip;
     }
 }
 
@@ -890,7 +913,7 @@ int run_error_stats(const double *x, const double *y, const double *z, long long
             select_hist_kernel<<<dim3(blocks, V), 256, 0, st>>>(w, n, pass);
             VS_LAUNCH_CHECK("select_hist_kernel");
         }
-        select_step_kernel<<<vg, 128, 0, st>>>(w, V, pass);
+        select_step_kernel<<<V, 128, 0, st>>>(w, pass);
         VS_LAUNCH_CHECK("select_step_kernel");
     }
     error_final_kernel<<<vg, 128, 0, st>>>(w, V, blocks, err);

@@ -213,25 +213,45 @@ __global__ void decode_kernel(const unsigned long long *__restrict__ keys,
         out[c] = key_value(cell_key(keys[c], c, first, pts));
 }
 
-// numpy's median of the n <= 8 non-NaN neighbour values, given as order-preserving keys:
-// sorted s, odd n -> (0 + s[n/2]) / 1, even n -> ((0 + s[n/2-1]) + s[n/2]) / 2 (the sum
-// reduction starts from its identity 0, which also turns -0 into +0).
-__device__ __forceinline__ double median_keys(unsigned long long *s, int n) {
-    for (int i = 1; i < n; ++i) {          // insertion sort
-        const unsigned long long v = s[i];
-        int j = i - 1;
-        while (j >= 0 && s[j] > v) {
-            s[j + 1] = s[j];
-            --j;
-        }
-        s[j + 1] = v;
+// numpy's median of the non-empty keys among 8 (empty = 0), without local memory: the
+// keys are sorted by an 8-input network with empty slots ordered last, and the middle
+// one(s) selected by the count.
+__device__ __forceinline__ void cswap(unsigned long long &a, unsigned long long &b) {
+    const unsigned long long lo = a < b ? a : b, hi = a < b ? b : a;
+    a = lo;
+    b = hi;
+}
+
+// s[idx] through a select tree on the index bits (an indexed read would move s to local memory)
+__device__ __forceinline__ unsigned long long select8(const unsigned long long (&s)[8], int idx) {
+    const bool b0 = idx & 1, b1 = idx & 2, b2 = idx & 4;
+    const unsigned long long a0 = b0 ? s[1] : s[0], a1 = b0 ? s[3] : s[2];
+    const unsigned long long a2 = b0 ? s[5] : s[4], a3 = b0 ? s[7] : s[6];
+    const unsigned long long c0 = b1 ? a1 : a0, c1 = b1 ? a3 : a2;
+    return b2 ? c1 : c0;
+}
+
+__device__ __forceinline__ double median8_keys(unsigned long long (&s)[8]) {
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        n += s[i] != kEmptyKey;
+        s[i] = s[i] == kEmptyKey ? ~0ull : s[i];      // empty sorts last
     }
+    // Batcher's odd-even merge sort for 8 inputs (19 comparators)
+    cswap(s[0], s[1]); cswap(s[2], s[3]); cswap(s[4], s[5]); cswap(s[6], s[7]);
+    cswap(s[0], s[2]); cswap(s[1], s[3]); cswap(s[4], s[6]); cswap(s[5], s[7]);
+    cswap(s[1], s[2]); cswap(s[5], s[6]);
+    cswap(s[0], s[4]); cswap(s[1], s[5]); cswap(s[2], s[6]); cswap(s[3], s[7]);
+    cswap(s[2], s[4]); cswap(s[3], s[5]);
+    cswap(s[1], s[2]); cswap(s[3], s[4]); cswap(s[5], s[6]);
+    const unsigned long long lo = select8(s, (n - 1) >> 1);
+    unsigned long long hi = select8(s, n >> 1);
     if (n & 1) {
-        unsigned long long k = s[n >> 1];
-        if (k == 0x7fffffffffffffffull) k = kZeroKey;   // -0 + 0 = +0
-        return double_from_key(k);
+        if (hi == 0x7fffffffffffffffull) hi = kZeroKey;   // -0 + 0 = +0
+        return double_from_key(hi);
     }
-    return __dmul_rn(__dadd_rn(__dadd_rn(0.0, double_from_key(s[(n >> 1) - 1])), double_from_key(s[n >> 1])), 0.5);
+    return __dmul_rn(__dadd_rn(__dadd_rn(0.0, double_from_key(lo)), double_from_key(hi)), 0.5);
 }
 
 __device__ __forceinline__ bool nan_double(double v) {
@@ -253,15 +273,23 @@ __global__ void hole_fill_kernel(const double *__restrict__ in, double *__restri
             continue;
         }
         unsigned long long s[8];
-        int n = 0;
+        int m = 0;
+        bool any = false;
+#pragma unroll
         for (int dj = -1; dj <= 1; ++dj)
+#pragma unroll
             for (int dk = -1; dk <= 1; ++dk) {
-                long long j = r + dj, k = col + dk;
-                if (j < 0 || j >= H || k < 0 || k >= W) continue;
-                double u = img[j * W + k];
-                if (!nan_double(u)) s[n++] = key_from_double(u);
+                if (dj == 0 && dk == 0) continue;
+                const long long j = r + dj, k = col + dk;
+                unsigned long long key = kEmptyKey;
+                if (j >= 0 && j < H && k >= 0 && k < W) {
+                    const double u = img[j * W + k];
+                    if (!nan_double(u)) key = key_from_double(u);
+                }
+                any |= key != kEmptyKey;
+                s[m++] = key;
             }
-        out[c] = n ? median_keys(s, n) : v;
+        out[c] = any ? median8_keys(s) : v;
     }
 }
 
@@ -344,39 +372,22 @@ __global__ void median_blur3x3_kernel(const T *__restrict__ in, float *__restric
 // dimensions < 2^31); the hole-filled float32 values are staged as blur keys.
 constexpr int TX = 32, TY = 8;
 
-// The hole-filled, float32-rounded value of the tile cell whose 3x3 neighbourhood sits at
-// raw[ly..ly+2][lx..lx+2], as a blur key.
-__device__ __forceinline__ unsigned filled_key(const unsigned long long (*raw)[TX + 4], int ly, int lx) {
-    const unsigned long long k = raw[ly + 1][lx + 1];
-    float f;
-    if (k != kEmptyKey) {
-        f = f64_to_f32(double_from_key(k));
-    } else {
-        unsigned long long s[8];
-        int n = 0;
-#pragma unroll
-        for (int dj = 0; dj < 3; ++dj)
-#pragma unroll
-            for (int dk = 0; dk < 3; ++dk) {
-                const unsigned long long u = raw[ly + dj][lx + dk];
-                if (u != kEmptyKey) s[n++] = u;
-            }
-        if (!n) return 0xffffffffu;                    // stays NaN
-        f = f64_to_f32(median_keys(s, n));
-    }
-    return blur_key(f);
-}
-
 // It also clears this tile of the idle key grid (the next view's), which nobody reads
-// concurrently, so no per-view memset is needed.
+// concurrently, so no per-view memset is needed.  Empty cells (a few percent) are
+// collected in a shared list and filled by consecutive threads, so the hole-fill work does
+// not diverge every warp that happens to hold one.
 __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
     const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys, int H,
     int W) {
+    constexpr int FW = TX + 2, FH = TY + 2;
     __shared__ unsigned long long raw[TY + 4][TX + 4];   // 0: empty cell or outside the image
-    __shared__ unsigned fk[TY + 2][TX + 2];              // blur keys of the hole-filled cells
+    __shared__ unsigned fk[FH][FW];                      // blur keys of the hole-filled cells
+    __shared__ unsigned short holes[FH * FW];
+    __shared__ int n_holes;
     const int r0 = blockIdx.y * TY, c0 = blockIdx.x * TX;
     const int tid = threadIdx.y * TX + threadIdx.x;
+    if (tid == 0) n_holes = 0;
     for (int i = tid; i < (TY + 4) * (TX + 4); i += TX * TY) {
         const int ly = i / (TX + 4), lx = i - ly * (TX + 4);
         const int r = r0 + ly - 2, c = c0 + lx - 2;
@@ -388,9 +399,30 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
         raw[ly][lx] = k;
     }
     __syncthreads();
-    for (int i = tid; i < (TY + 2) * (TX + 2); i += TX * TY) {
-        const int ly = i / (TX + 2), lx = i - ly * (TX + 2);
-        fk[ly][lx] = filled_key(raw, ly, lx);
+    for (int i = tid; i < FH * FW; i += TX * TY) {
+        const int ly = i / FW, lx = i - ly * FW;
+        const unsigned long long k = raw[ly + 1][lx + 1];
+        if (k != kEmptyKey) {
+            fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
+        } else {
+            holes[atomicAdd(&n_holes, 1)] = static_cast<unsigned short>(i);
+        }
+    }
+    __syncthreads();
+    for (int h = tid; h < n_holes; h += TX * TY) {
+        const int i = holes[h];
+        const int ly = i / FW, lx = i - ly * FW;
+        unsigned long long s[8];
+        int m = 0;
+#pragma unroll
+        for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 3; ++dk)
+                if (dj != 1 || dk != 1) s[m++] = raw[ly + dj][lx + dk];
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) any |= s[q] != kEmptyKey;
+        fk[ly][lx] = any ? blur_key(f64_to_f32(median8_keys(s))) : 0xffffffffu;
     }
     __syncthreads();
     const int r = r0 + threadIdx.y, c = c0 + threadIdx.x;
