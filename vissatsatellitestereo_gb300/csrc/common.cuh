@@ -48,6 +48,43 @@ struct Carver {
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// ---- rare-path FP64 operations --------------------------------------------------------
+// GB300 runs FP64 arithmetic and the float<->double conversions on a narrow pipe.  The
+// per-element kernels keep them off the common path, but the compiler would if-convert a
+// cheap-looking fallback (hoist it out of its branch and execute it for every element);
+// volatile asm has side effects as far as the compiler knows, so these stay in their
+// branch.
+__device__ __forceinline__ double rare_dsub(double a, double b) {
+    double r;
+    asm volatile("sub.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double rare_dadd(double a, double b) {
+    double r;
+    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double rare_dmul(double a, double b) {
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double rare_ddiv(double a, double b) {
+    double r;
+    asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ float rare_d2f(double a) {
+    float r;
+    asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(r) : "d"(a));
+    return r;
+}
+__device__ __forceinline__ double rare_f2d(float a) {
+    double r;
+    asm volatile("cvt.f64.f32 %0, %1;" : "=d"(r) : "f"(a));
+    return r;
+}
+
 // ---- double-float arithmetic ---------------------------------------------------------
 // A value hi + lo with |lo| <= ulp(hi)/2 carried in two floats (about 48 significant
 // bits).  Error-free transformations after Knuth (TwoSum) and Dekker (TwoProduct with
@@ -111,7 +148,7 @@ __device__ __forceinline__ double f32_to_f64(float f) {
     const unsigned e = (u >> 23) & 0xffu;
     if (e == 0 || e == 0xffu) {
         if ((u << 1) == 0) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(u) << 32));
-        return static_cast<double>(f);
+        return rare_f2d(f);
     }
     const unsigned long long b = (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
                                  (static_cast<unsigned long long>(e + 1023u - 127u) << 52) |

@@ -58,9 +58,9 @@ struct Tables {
     Axis row, col;
 };
 
-__device__ __noinline__ int axis_exact(const Axis &ax, double v) {
-    double a = ax.dir > 0 ? __dsub_rn(v, ax.off) : __dsub_rn(ax.off, v);
-    double q = __ddiv_rn(a, ax.res);
+__device__ __forceinline__ int axis_exact(const Axis &ax, double v) {
+    const double a = ax.dir > 0 ? rare_dsub(v, ax.off) : rare_dsub(ax.off, v);
+    const double q = rare_ddiv(a, ax.res);
     if (!(q >= 0.0 && q < static_cast<double>(ax.n))) return -1;
     return static_cast<int>(q);   // q >= 0: truncation is floor
 }
@@ -251,7 +251,7 @@ __device__ __forceinline__ double median8_keys(unsigned long long (&s)[8]) {
         if (hi == 0x7fffffffffffffffull) hi = kZeroKey;   // -0 + 0 = +0
         return double_from_key(hi);
     }
-    return __dmul_rn(__dadd_rn(__dadd_rn(0.0, double_from_key(lo)), double_from_key(hi)), 0.5);
+    return rare_dmul(rare_dadd(rare_dadd(0.0, double_from_key(lo)), double_from_key(hi)), 0.5);
 }
 
 __device__ __forceinline__ bool nan_double(double v) {
@@ -306,7 +306,7 @@ __device__ __forceinline__ float f64_to_f32(double v) {
     const int e32 = e - 1023 + 127;
     if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);                                     // overflow
     if (e == 0 && (mhi | lo) == 0) return __uint_as_float(sign);                                     // signed zero
-    if (e32 <= 0) return __double2float_rn(v);                                                      // subnormal range
+    if (e32 <= 0) return rare_d2f(v);                                                               // subnormal range
     const unsigned m23 = (mhi << 3) | (lo >> 29);
     const unsigned rem = lo & 0x1fffffffu;
     const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));

@@ -77,8 +77,8 @@ __device__ __forceinline__ df split_double(double v) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
     const int e = static_cast<int>((b >> 52) & 0x7ff);
     if (e < 1023 - 100 || e > 1023 + 100) {      // rare: zero/denormal/huge/inf/nan
-        const float hi = __double2float_rn(v);
-        return {hi, isfinite(hi) ? __double2float_rn(v - static_cast<double>(hi)) : 0.0f};
+        const float hi = rare_d2f(v);
+        return {hi, isfinite(hi) ? rare_d2f(rare_dsub(v, rare_f2d(hi))) : 0.0f};
     }
     const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
     const unsigned mant_hi = static_cast<unsigned>((b >> 29) & 0x7fffffu);   // top 23 fraction bits
