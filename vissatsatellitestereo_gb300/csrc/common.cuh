@@ -141,19 +141,53 @@ __host__ __device__ inline df df_from_double(double v) {
     float hi = static_cast<float>(v);
     return {hi, static_cast<float>(v - static_cast<double>(hi))};
 }
-// float -> double by bit manipulation (exact; the conversion instruction shares GB300's
-// narrow FP64 pipe).  Subnormal, infinite and NaN floats take the instruction.
+// float -> double by bit manipulation, exact (the conversion instruction shares GB300's
+// narrow FP64 pipe, and even a never-taken branch holding one slows the kernel).
 __device__ __forceinline__ double f32_to_f64(float f) {
     const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xffu;
-    if (e == 0 || e == 0xffu) {
-        if ((u << 1) == 0) return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(u) << 32));
-        return rare_f2d(f);
+    const unsigned long long sign = static_cast<unsigned long long>(u & 0x80000000u) << 32;
+    unsigned e = (u >> 23) & 0xffu;
+    unsigned m = u & 0x7fffffu;
+    unsigned long long b;
+    if (e == 0xffu) {                 // inf / NaN
+        b = sign | 0x7ff0000000000000ull | (static_cast<unsigned long long>(m) << 29) | (m ? (1ull << 51) : 0ull);
+    } else if (e == 0) {              // zero / subnormal: normalise the mantissa
+        if (m == 0) {
+            b = sign;
+        } else {
+            const int lz = __clz(m) - 8;          // m < 2^23: shift until bit 23 is set
+            m = (m << lz) & 0x7fffffu;
+            b = sign | (static_cast<unsigned long long>(1023 - 126 - lz) << 52) | (static_cast<unsigned long long>(m) << 29);
+        }
+    } else {
+        b = sign | (static_cast<unsigned long long>(e + 1023u - 127u) << 52) | (static_cast<unsigned long long>(m) << 29);
     }
-    const unsigned long long b = (static_cast<unsigned long long>(u & 0x80000000u) << 32) |
-                                 (static_cast<unsigned long long>(e + 1023u - 127u) << 52) |
-                                 (static_cast<unsigned long long>(u & 0x7fffffu) << 29);
     return __longlong_as_double(static_cast<long long>(b));
+}
+
+// Round-to-nearest-even double -> float (astype(np.float32)) with 32/64-bit integer
+// operations only, including the float-subnormal range.
+__device__ __forceinline__ float f64_to_f32(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
+    const unsigned sign = hi & 0x80000000u;
+    const int e = static_cast<int>((hi >> 20) & 0x7ffu);
+    const unsigned mhi = hi & 0xfffffu;
+    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((mhi | lo) ? 0x400000u : 0u));   // inf / NaN
+    const int e32 = e - 1023 + 127;
+    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);                                     // overflow
+    if (e32 <= 0) {                   // float subnormal range (or zero): units of 2^-149
+        const int shift = 926 - e;    // value = M * 2^(e - 1075), M = 2^52 + mantissa
+        if (e == 0 || shift >= 64) return __uint_as_float(sign);                                     // rounds to 0
+        const unsigned long long M = (1ull << 52) | (b & 0xfffffffffffffull);
+        const unsigned long long q = M >> shift, rem = M & ((1ull << shift) - 1), half = 1ull << (shift - 1);
+        const unsigned up = (rem > half) || (rem == half && (q & 1ull));
+        return __uint_as_float(sign | static_cast<unsigned>(q + up));   // may round up to the least normal
+    }
+    const unsigned m23 = (mhi << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
+    return __uint_as_float(sign | ((static_cast<unsigned>(e32) << 23) + m23 + up));   // carry may round to inf
 }
 __device__ __forceinline__ double df_to_double(df a) { return __dadd_rn(f32_to_f64(a.hi), f32_to_f64(a.lo)); }
 

@@ -52,6 +52,7 @@ struct Axis {
     int neg;                     // off < 0
     int dir;
     int fast;                    // fast path usable
+    int contained;               // grid range (+-2 cells) inside off's sign/exponent interval
 };
 
 struct Tables {
@@ -68,7 +69,10 @@ __device__ __forceinline__ int axis_exact(const Axis &ax, double v) {
 // Cell index along one axis, or -1 when the point falls outside the grid.  The FP32
 // estimate q carries a proven error bound; unless q lies within that bound of an integer,
 // its floor is the reference's floor(fl(d*ulp/res)).  Near a boundary the integer
-// threshold table decides (about 0.1% of points).
+// threshold table decides (about 0.1% of points).  A point with another sign or exponent
+// than the origin is off-grid when the grid lies inside the origin's exponent interval;
+// otherwise (EXACT instantiation) it takes the literal FP64 expression.
+template <bool EXACT>
 __device__ __forceinline__ int axis_index(const Axis &ax, double v) {
     const long long bv = __double_as_longlong(v);
     const unsigned hi = static_cast<unsigned>(static_cast<unsigned long long>(bv) >> 32);
@@ -90,7 +94,11 @@ __device__ __forceinline__ int axis_index(const Axis &ax, double v) {
         for (int it = 0; it < 8 && __ldg(ax.thr + r + 1) <= d; ++it) ++r;
         return r;
     }
-    return axis_exact(ax, v);
+    if constexpr (EXACT) {
+        return axis_exact(ax, v);
+    } else {
+        return -1;
+    }
 }
 
 // T[r] = smallest d >= 0 with floor(fl(d*ulp / res)) >= r, for r = 0..n.  d*ulp is exact,
@@ -123,15 +131,16 @@ __host__ __device__ __forceinline__ unsigned long long epoch_tag(int view) {
 
 constexpr int kPts = 4;   // consecutive points per thread (runs in the same cell merge)
 
+template <bool EXACT>
 __device__ __forceinline__ void bin_point(const Tables &tb, double x, double y, double z, long long index,
                                           unsigned long long *vk, unsigned long long *first,
                                           unsigned long long tag, long long &run_cell,
                                           unsigned long long &run_key) {
     const unsigned long long zb = static_cast<unsigned long long>(__double_as_longlong(z));
     if (is_nan_bits(zb)) return;
-    const int r = axis_index(tb.row, y);
+    const int r = axis_index<EXACT>(tb.row, y);
     if (r < 0) return;
-    const int c = axis_index(tb.col, x);
+    const int c = axis_index<EXACT>(tb.col, x);
     if (c < 0) return;
     const long long cell = static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(r)) *
                                                   static_cast<unsigned>(tb.col.n)) + c;
@@ -153,6 +162,7 @@ __device__ __forceinline__ void bin_point(const Tables &tb, double x, double y, 
 
 // Bins one view's points: atomicMax of the height keys into the view's key grid.
 // View v owns points [offsets[v], offsets[v+1]).
+template <bool EXACT>
 __global__ void __launch_bounds__(256) bin_max_kernel(const double *__restrict__ pts,
                                                       const long long *__restrict__ offsets, int v,
                                                       long long single_n, Tables tb,
@@ -187,7 +197,7 @@ __global__ void __launch_bounds__(256) bin_max_kernel(const double *__restrict__
         unsigned long long run_key = 0;
 #pragma unroll
         for (int k = 0; k < kPts; ++k)
-            bin_point(tb, p[3 * k], p[3 * k + 1], p[3 * k + 2], i + k, vk, first, tag, run_cell, run_key);
+            bin_point<EXACT>(tb, p[3 * k], p[3 * k + 1], p[3 * k + 2], i + k, vk, first, tag, run_cell, run_key);
         if (run_key) atomicMax(vk + run_cell, run_key);
     }
 }
@@ -291,26 +301,6 @@ __global__ void hole_fill_kernel(const double *__restrict__ in, double *__restri
             }
         out[c] = any ? median8_keys(s) : v;
     }
-}
-
-// Round-to-nearest FP64 -> FP32 (astype(np.float32)) with 32-bit integer operations on the
-// two halves of the double; the conversion instruction runs on GB300's narrow pipe, so it
-// is kept for the float-subnormal range only.
-__device__ __forceinline__ float f64_to_f32(double v) {
-    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
-    const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
-    const unsigned sign = hi & 0x80000000u;
-    const int e = static_cast<int>((hi >> 20) & 0x7ffu);
-    const unsigned mhi = hi & 0xfffffu;
-    if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((mhi | lo) ? 0x400000u : 0u));   // inf / NaN
-    const int e32 = e - 1023 + 127;
-    if (e32 >= 255) return __uint_as_float(sign | 0x7f800000u);                                     // overflow
-    if (e == 0 && (mhi | lo) == 0) return __uint_as_float(sign);                                     // signed zero
-    if (e32 <= 0) return rare_d2f(v);                                                               // subnormal range
-    const unsigned m23 = (mhi << 3) | (lo >> 29);
-    const unsigned rem = lo & 0x1fffffffu;
-    const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
-    return __uint_as_float(sign | ((static_cast<unsigned>(e32) << 23) + m23 + up));   // carry may round to inf
 }
 
 // ---- 3x3 median blur (float32, replicate border, NaN after every number) -----------------
@@ -462,6 +452,7 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
     ax.top12 = static_cast<unsigned>(b >> 52);
     const unsigned e = static_cast<unsigned>((b >> 52) & 0x7ff);
     ax.fast = 0;
+    ax.contained = 0;
     ax.shift = 0;
     ax.scale = 0.f;
     ax.err_abs = ax.err_rel = 0.f;
@@ -482,6 +473,14 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
     ax.err_rel = static_cast<float>(4.0 * ldexp(1.0, -24));
     ax.tmax = host_threshold(n, ulp, res);
     ax.fast = 1;
+    // the grid spans off .. off -/+ (n + 2) * res; contained when both ends keep off's sign
+    // and exponent, so that any point with another sign/exponent lies >= 2 cells outside
+    const double far = dir > 0 ? off + (static_cast<double>(n) + 2.0) * res : off - (static_cast<double>(n) + 2.0) * res;
+    const double near = dir > 0 ? off - 2.0 * res : off + 2.0 * res;
+    unsigned long long bf, bn;
+    memcpy(&bf, &far, sizeof bf);
+    memcpy(&bn, &near, sizeof bn);
+    ax.contained = (bf >> 52) == (b >> 52) && (bn >> 52) == (b >> 52);
     const int threads = 256;
     axis_thresholds_kernel<<<static_cast<unsigned>(ceil_div(n + 1, threads)), threads, 0, st>>>(thr, n, ulp, res);
     return check_launch("axis_thresholds_kernel");
@@ -522,7 +521,10 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
     long long want = ceil_div(ceil_div(max_points, kPts), threads);
     long long cap = static_cast<long long>(sm_count()) * 8;
     unsigned gx = static_cast<unsigned>(std::max(1LL, std::min(want, cap)));
-    bin_max_kernel<<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
+    if (tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained)
+        bin_max_kernel<false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
+    else
+        bin_max_kernel<true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
     return check_launch("bin_max_kernel");
 }
 

@@ -71,15 +71,12 @@ __device__ __forceinline__ float u29_to_float(unsigned u) {
 
 // Splits an FP64 value into hi + lo floats with integer operations only (no FP64 pipe):
 // hi keeps the top 24 significant bits (truncated, so the remainder is exact), lo is the
-// remaining 29 bits rounded to a float.  Non-finite and out-of-float-range values take
-// the conversion instructions instead.
+// remaining 29 bits rounded to a float.  Magnitudes outside 2^+-100 (zero, tiny, huge,
+// inf, NaN) become the nearest float with lo = 0.
 __device__ __forceinline__ df split_double(double v) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
     const int e = static_cast<int>((b >> 52) & 0x7ff);
-    if (e < 1023 - 100 || e > 1023 + 100) {      // rare: zero/denormal/huge/inf/nan
-        const float hi = rare_d2f(v);
-        return {hi, isfinite(hi) ? rare_d2f(rare_dsub(v, rare_f2d(hi))) : 0.0f};
-    }
+    if (e < 1023 - 100 || e > 1023 + 100) return {f64_to_f32(v), 0.0f};
     const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
     const unsigned mant_hi = static_cast<unsigned>((b >> 29) & 0x7fffffu);   // top 23 fraction bits
     const float hi = __uint_as_float(sign | (static_cast<unsigned>(e - 1023 + 127) << 23) | mant_hi);
