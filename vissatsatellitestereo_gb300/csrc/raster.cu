@@ -202,6 +202,107 @@ __global__ void __launch_bounds__(256) bin_max_kernel(const double *__restrict__
     }
 }
 
+// ---- the common-case binning kernel -------------------------------------------------------
+// Both axes on the fast path and the grid inside the origins' exponent intervals: every
+// point is handled with integer and FP32 operations, the coordinates are carried as raw
+// 64-bit patterns (double-typed values make the compiler emit FP64 moves), the axis
+// constants live in registers, the row/column estimates are branch-free, and the four
+// points of a thread are merged into runs before their atomics.
+struct FastAxis {
+    long long off_bits, tmax;
+    const long long *thr;
+    unsigned top12;
+    int shift, nm1;
+    float scale, err_abs, err_rel;
+};
+
+template <bool FLIP>   // FLIP: d = off - v (rows of a positive origin, columns of a negative one)
+__device__ __forceinline__ bool axis_fast(const FastAxis &a, long long bv, int &r, long long &d, bool &sure) {
+    const unsigned hi = static_cast<unsigned>(static_cast<unsigned long long>(bv) >> 32);
+    d = FLIP ? (a.off_bits - bv) : (bv - a.off_bits);
+    const bool ok = ((hi >> 20) == a.top12) & (d >= 0) & (d < a.tmax);
+    const unsigned u = static_cast<unsigned>(static_cast<unsigned long long>(d) >> a.shift);
+    const float q = __fmul_rn(__uint2float_rn(u), a.scale);
+    const float big = __fadd_rn(q, 12582912.0f);
+    const float fr = __fsub_rn(q, __fsub_rn(big, 12582912.0f));
+    const int rn = static_cast<int>(static_cast<unsigned>(__float_as_int(big)) - 0x4b400000u);
+    r = min(max(rn - (fr < 0.0f ? 1 : 0), 0), a.nm1);
+    sure = fabsf(fr) > __fmaf_rn(a.err_rel, q, a.err_abs);
+    return ok;
+}
+
+__device__ __noinline__ int axis_correct(const long long *thr, int r, long long d) {
+    for (int it = 0; it < 8 && __ldg(thr + r) > d; ++it) --r;
+    for (int it = 0; it < 8 && __ldg(thr + r + 1) <= d; ++it) ++r;
+    return r;
+}
+
+template <bool FLIP_ROW, bool FLIP_COL>
+__global__ void __launch_bounds__(256) bin_fast_kernel(const double *__restrict__ pts,
+                                                       const long long *__restrict__ offsets, int v,
+                                                       long long single_n, FastAxis ra, FastAxis ca,
+                                                       unsigned long long *__restrict__ vk,
+                                                       unsigned long long *__restrict__ first) {
+    const long long begin = offsets ? offsets[v] : 0;
+    const long long end = offsets ? offsets[v + 1] : single_n;
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * kPts;
+    const unsigned long long tag = epoch_tag(v);
+    const FastAxis R = ra, C = ca;
+    const unsigned long long ncols = static_cast<unsigned>(C.nm1 + 1);
+    const long long *bits = reinterpret_cast<const long long *>(pts);
+    for (long long i = begin + (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kPts; i < end;
+         i += stride) {
+        long long p[3 * kPts];
+        const long long *src = bits + 3 * i;
+        if (i + kPts <= end && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+            const longlong2 *s2 = reinterpret_cast<const longlong2 *>(src);
+#pragma unroll
+            for (int k = 0; k < 3 * kPts / 2; ++k) {
+                const longlong2 a = __ldcs(s2 + k);
+                p[2 * k] = a.x;
+                p[2 * k + 1] = a.y;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kPts; ++k) {
+                const bool in = i + k < end;
+                p[3 * k] = in ? __ldcs(src + 3 * k) : 0ll;
+                p[3 * k + 1] = in ? __ldcs(src + 3 * k + 1) : 0ll;
+                p[3 * k + 2] = in ? __ldcs(src + 3 * k + 2) : 0x7ff8000000000000ll;
+            }
+        }
+        long long cell[kPts];
+        unsigned long long key[kPts];
+#pragma unroll
+        for (int k = 0; k < kPts; ++k) {
+            const unsigned long long zb = static_cast<unsigned long long>(p[3 * k + 2]);
+            int r, c;
+            long long dr, dc;
+            bool sr, sc;
+            bool ok = axis_fast<FLIP_ROW>(R, p[3 * k + 1], r, dr, sr);
+            ok &= axis_fast<FLIP_COL>(C, p[3 * k], c, dc, sc);
+            ok &= !is_nan_bits(zb);
+            if (ok && !sr) r = axis_correct(R.thr, r, dr);
+            if (ok && !sc) c = axis_correct(C.thr, c, dc);
+            const long long cl = static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(r)) * ncols) + c;
+            const bool zero = (zb << 1) == 0;
+            if (ok && zero) atomicMax(first + cl, tag | (kIdxMask - static_cast<unsigned long long>(i + k)));
+            const unsigned long long kz = (zb >> 63) ? ~zb : (zb | 0x8000000000000000ull);
+            key[k] = ok ? (zero ? kZeroKey : kz) : kEmptyKey;
+            cell[k] = ok ? cl : -1 - k;
+        }
+#pragma unroll
+        for (int k = 1; k < kPts; ++k) {     // merge runs of consecutive points in one cell
+            const bool same = cell[k] == cell[k - 1];
+            key[k] = same ? max(key[k], key[k - 1]) : key[k];
+            key[k - 1] = same ? kEmptyKey : key[k - 1];
+        }
+#pragma unroll
+        for (int k = 0; k < kPts; ++k)
+            if (key[k] != kEmptyKey) atomicMax(vk + cell[k], key[k]);
+    }
+}
+
 // Key of a cell's nanmax with the zero sign resolved (0 = empty cell).
 __device__ __forceinline__ unsigned long long cell_key(unsigned long long k, long long cell,
                                                        const unsigned long long *first, const double *pts) {
@@ -521,10 +622,33 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
     long long want = ceil_div(ceil_div(max_points, kPts), threads);
     long long cap = static_cast<long long>(sm_count()) * 8;
     unsigned gx = static_cast<unsigned>(std::max(1LL, std::min(want, cap)));
-    if (tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained)
-        bin_max_kernel<false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
-    else
+    if (tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained) {
+        FastAxis fa[2];
+        const Axis *ax[2] = {&tb.row, &tb.col};
+        for (int a = 0; a < 2; ++a) {
+            memcpy(&fa[a].off_bits, &ax[a]->off, sizeof(long long));
+            fa[a].tmax = ax[a]->tmax;
+            fa[a].thr = ax[a]->thr;
+            fa[a].top12 = ax[a]->top12;
+            fa[a].shift = ax[a]->shift;
+            fa[a].nm1 = static_cast<int>(ax[a]->n - 1);
+            fa[a].scale = ax[a]->scale;
+            fa[a].err_abs = ax[a]->err_abs;
+            fa[a].err_rel = ax[a]->err_rel;
+        }
+        // rows: a = off - v unless the origin is negative; columns: a = v - off unless negative
+        const bool flip_row = !tb.row.neg, flip_col = tb.col.neg != 0;
+        if (flip_row && !flip_col)
+            bin_fast_kernel<true, false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
+        else if (flip_row && flip_col)
+            bin_fast_kernel<true, true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
+        else if (!flip_row && !flip_col)
+            bin_fast_kernel<false, false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
+        else
+            bin_fast_kernel<false, true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
+    } else {
         bin_max_kernel<true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
+    }
     return check_launch("bin_max_kernel");
 }
 
