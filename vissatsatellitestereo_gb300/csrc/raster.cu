@@ -458,10 +458,12 @@ __global__ void median_blur3x3_kernel(const T *__restrict__ in, float *__restric
 }
 
 // ---- fused produce_dsm epilogue: keys -> nanmax -> hole fill -> float32 -> blur ---------
-// One 32x8 output tile per CTA; the key tile carries a 2-cell halo (hole fill needs the
-// 3x3 neighbourhood of each blurred cell's 3x3 neighbourhood).  32-bit indexing (grid
-// dimensions < 2^31); the hole-filled float32 values are staged as blur keys.
-constexpr int TX = 32, TY = 8;
+// One 32x32 output tile per CTA of 32x8 threads (4 outputs per thread, rows ty + 8j).  The
+// key tile carries a 2-cell halo (hole fill needs the 3x3 neighbourhood of each blurred
+// cell's 3x3 neighbourhood); the hole-filled float32 values are staged as blur keys;
+// 32-bit indexing (grid dimensions < 2^31).
+constexpr int TX = 32, TY = 8, TILE_Y = 32;
+constexpr int RAW_W = TX + 4, RAW_H = TILE_Y + 4, FK_W = TX + 2, FK_H = TILE_Y + 2;
 
 // It also clears this tile of the idle key grid (the next view's), which nobody reads
 // concurrently, so no per-view memset is needed.  Empty cells (a few percent) are
@@ -471,38 +473,35 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
     const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys, int H,
     int W) {
-    constexpr int FW = TX + 2, FH = TY + 2;
-    __shared__ unsigned long long raw[TY + 4][TX + 4];   // 0: empty cell or outside the image
-    __shared__ unsigned fk[FH][FW];                      // blur keys of the hole-filled cells
-    __shared__ unsigned short holes[FH * FW];
+    __shared__ unsigned long long raw[RAW_H][RAW_W];   // 0: empty cell or outside the image
+    __shared__ unsigned fk[FK_H][FK_W];                // blur keys of the hole-filled cells
+    __shared__ unsigned short holes[FK_H * FK_W];
     __shared__ int n_holes;
-    const int r0 = blockIdx.y * TY, c0 = blockIdx.x * TX;
-    const int tid = threadIdx.y * TX + threadIdx.x;
-    if (tid == 0) n_holes = 0;
-    for (int i = tid; i < (TY + 4) * (TX + 4); i += TX * TY) {
-        const int ly = i / (TX + 4), lx = i - ly * (TX + 4);
-        const int r = r0 + ly - 2, c = c0 + lx - 2;
-        unsigned long long k = kEmptyKey;
-        if (r >= 0 && r < H && c >= 0 && c < W) {
-            const long long cell = static_cast<long long>(r) * W + c;
-            k = cell_key(vk[cell], cell, first, pts);
-        }
-        raw[ly][lx] = k;
-    }
-    __syncthreads();
-    for (int i = tid; i < FH * FW; i += TX * TY) {
-        const int ly = i / FW, lx = i - ly * FW;
-        const unsigned long long k = raw[ly + 1][lx + 1];
-        if (k != kEmptyKey) {
-            fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
-        } else {
-            holes[atomicAdd(&n_holes, 1)] = static_cast<unsigned short>(i);
+    const int r0 = blockIdx.y * TILE_Y, c0 = blockIdx.x * TX;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    if (tx == 0 && ty == 0) n_holes = 0;
+    for (int ly = ty; ly < RAW_H; ly += TY) {
+        const int r = r0 + ly - 2;
+        const bool row_in = r >= 0 && r < H;
+        const long long rowbase = static_cast<long long>(r) * W;
+        for (int lx = tx; lx < RAW_W; lx += TX) {
+            const int c = c0 + lx - 2;
+            unsigned long long k = kEmptyKey;
+            if (row_in && c >= 0 && c < W) k = cell_key(vk[rowbase + c], rowbase + c, first, pts);
+            raw[ly][lx] = k;
         }
     }
     __syncthreads();
-    for (int h = tid; h < n_holes; h += TX * TY) {
+    for (int ly = ty; ly < FK_H; ly += TY)
+        for (int lx = tx; lx < FK_W; lx += TX) {
+            const unsigned long long k = raw[ly + 1][lx + 1];
+            if (k != kEmptyKey) fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
+            else holes[atomicAdd(&n_holes, 1)] = static_cast<unsigned short>(ly * FK_W + lx);
+        }
+    __syncthreads();
+    for (int h = ty * TX + tx; h < n_holes; h += TX * TY) {
         const int i = holes[h];
-        const int ly = i / FW, lx = i - ly * FW;
+        const int ly = i / FK_W, lx = i - ly * FK_W;
         unsigned long long s[8];
         int m = 0;
 #pragma unroll
@@ -516,18 +515,23 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
         fk[ly][lx] = any ? blur_key(f64_to_f32(median8_keys(s))) : 0xffffffffu;
     }
     __syncthreads();
-    const int r = r0 + threadIdx.y, c = c0 + threadIdx.x;
-    if (r >= H || c >= W) return;
-    const long long cell = static_cast<long long>(r) * W + c;
-    if (next_keys) next_keys[cell] = kEmptyKey;
-    int ya = threadIdx.y, yb = threadIdx.y + 1, yc = threadIdx.y + 2;
-    int xa = threadIdx.x, xb = threadIdx.x + 1, xc = threadIdx.x + 2;
-    if (r == 0) ya = yb;                 // replicate border: clamp the neighbours into the image
-    if (r == H - 1) yc = yb;
-    if (c == 0) xa = xb;
+    const int c = c0 + tx;
+    if (c >= W) return;
+    int xa = tx, xb = tx + 1, xc = tx + 2;
+    if (c == 0) xa = xb;                 // replicate border: clamp the neighbours into the image
     if (c == W - 1) xc = xb;
-    out[cell] = median9(fk[ya][xa], fk[yb][xa], fk[yc][xa], fk[ya][xb], fk[yb][xb], fk[yc][xb], fk[ya][xc],
-                        fk[yb][xc], fk[yc][xc]);
+#pragma unroll
+    for (int j = 0; j < TILE_Y / TY; ++j) {
+        const int oy = ty + TY * j, r = r0 + oy;
+        if (r >= H) break;
+        int ya = oy, yb = oy + 1, yc = oy + 2;
+        if (r == 0) ya = yb;
+        if (r == H - 1) yc = yb;
+        const long long cell = static_cast<long long>(r) * W + c;
+        if (next_keys) next_keys[cell] = kEmptyKey;
+        out[cell] = median9(fk[ya][xa], fk[yb][xa], fk[yc][xa], fk[ya][xb], fk[yb][xb], fk[yc][xb], fk[ya][xc],
+                            fk[yb][xc], fk[yc][xc]);
+    }
 }
 
 // ---- host side --------------------------------------------------------------------------
@@ -742,7 +746,7 @@ extern "C" int vs_dsm_from_points(const double *points, const int64_t *offsets, 
     if (s != VS_OK) return s;
     // per-view counts live on the device: launch for a full GPU and let the grid stride
     const long long launch_points = static_cast<long long>(sm_count()) * 8 * 256 * kPts;
-    const dim3 egrid(static_cast<unsigned>(ceil_div(xsize, TX)), static_cast<unsigned>(ceil_div(ysize, TY)));
+    const dim3 egrid(static_cast<unsigned>(ceil_div(xsize, TX)), static_cast<unsigned>(ceil_div(ysize, TILE_Y)));
     for (int v = 0; v < n_views; ++v) {
         unsigned long long *cur = w.keys[v & 1], *nxt = (v + 1 < n_views) ? w.keys[(v + 1) & 1] : nullptr;
         s = bin_launch(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, cur, w.first, st);
