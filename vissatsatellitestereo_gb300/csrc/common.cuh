@@ -166,8 +166,10 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 }
 
 // Round-to-nearest-even double -> float (astype(np.float32)) with 32/64-bit integer
-// operations only, including the float-subnormal range.
-__device__ __forceinline__ float f64_to_f32(double v) {
+// operations only.  f64_to_f32_slow covers every input; f64_to_f32 runs the straight-line
+// normal-range path and branches to it only for inf/NaN, overflow and the float-subnormal
+// range.
+__device__ __noinline__ float f64_to_f32_slow(double v) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
     const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
     const unsigned sign = hi & 0x80000000u;
@@ -187,8 +189,22 @@ __device__ __forceinline__ float f64_to_f32(double v) {
     const unsigned m23 = (mhi << 3) | (lo >> 29);
     const unsigned rem = lo & 0x1fffffffu;
     const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
-    return __uint_as_float(sign | ((static_cast<unsigned>(e32) << 23) + m23 + up));   // carry may round to inf
+    return __uint_as_float(sign | ((static_cast<unsigned>(e32) << 23) + m23 + up));
 }
+
+__device__ __forceinline__ float f64_to_f32(double v) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+    const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
+    const unsigned ebits = (hi >> 20) & 0x7ffu;
+    // normal float range: 897 <= e <= 1150 (e32 = e - 896 in 1..254)
+    if (ebits - 897u > 253u) return f64_to_f32_slow(v);
+    const unsigned m23 = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    const unsigned up = (rem > 0x10000000u) | ((rem == 0x10000000u) & m23);
+    // the carry of a round-up may step into the next binade or to inf: both are correct
+    return __uint_as_float((hi & 0x80000000u) | (((ebits - 896u) << 23) + m23 + (up & 1u)));
+}
+
 __device__ __forceinline__ double df_to_double(df a) { return __dadd_rn(f32_to_f64(a.hi), f32_to_f64(a.lo)); }
 
 // ---- order-preserving keys --------------------------------------------------------------

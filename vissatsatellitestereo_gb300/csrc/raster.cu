@@ -304,11 +304,15 @@ __global__ void __launch_bounds__(256) bin_fast_kernel(const double *__restrict_
 }
 
 // Key of a cell's nanmax with the zero sign resolved (0 = empty cell).
-__device__ __forceinline__ unsigned long long cell_key(unsigned long long k, long long cell,
-                                                       const unsigned long long *first, const double *pts) {
-    if (k != kZeroKey) return k;
+__device__ __noinline__ unsigned long long zero_key(long long cell, const unsigned long long *first,
+                                                    const double *pts) {
     const unsigned long long idx = kIdxMask - (first[cell] & kIdxMask);
     return key_from_double(pts[3 * idx + 2]);
+}
+
+__device__ __forceinline__ unsigned long long cell_key(unsigned long long k, long long cell,
+                                                       const unsigned long long *first, const double *pts) {
+    return k != kZeroKey ? k : zero_key(cell, first, pts);
 }
 
 __device__ __forceinline__ double key_value(unsigned long long k) {
@@ -473,33 +477,42 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
     const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys, int H,
     int W) {
-    __shared__ unsigned long long raw[RAW_H][RAW_W];   // 0: empty cell or outside the image
-    __shared__ unsigned fk[FK_H][FK_W];                // blur keys of the hole-filled cells
+    __shared__ unsigned long long raw[RAW_H * RAW_W];   // 0: empty cell or outside the image
+    __shared__ unsigned fk[FK_H][FK_W];                 // blur keys of the hole-filled cells
     __shared__ unsigned short holes[FK_H * FK_W];
     __shared__ int n_holes;
     const int r0 = blockIdx.y * TILE_Y, c0 = blockIdx.x * TX;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    if (tx == 0 && ty == 0) n_holes = 0;
-    for (int ly = ty; ly < RAW_H; ly += TY) {
-        const int r = r0 + ly - 2;
-        const bool row_in = r >= 0 && r < H;
-        const long long rowbase = static_cast<long long>(r) * W;
-        for (int lx = tx; lx < RAW_W; lx += TX) {
-            const int c = c0 + lx - 2;
-            unsigned long long k = kEmptyKey;
-            if (row_in && c >= 0 && c < W) k = cell_key(vk[rowbase + c], rowbase + c, first, pts);
-            raw[ly][lx] = k;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx, lane = tid & 31;
+    if (tid == 0) n_holes = 0;
+    for (int i = tid; i < RAW_H * RAW_W; i += TX * TY) {
+        const int ly = i / RAW_W, lx = i - ly * RAW_W;
+        const int r = r0 + ly - 2, c = c0 + lx - 2;
+        unsigned long long k = kEmptyKey;
+        if (static_cast<unsigned>(r) < static_cast<unsigned>(H) && static_cast<unsigned>(c) < static_cast<unsigned>(W)) {
+            const long long cell = static_cast<long long>(r) * W + c;
+            k = cell_key(vk[cell], cell, first, pts);
+        }
+        raw[i] = k;
+    }
+    __syncthreads();
+    for (int base = 0; base < FK_H * FK_W; base += TX * TY) {
+        const int i = base + tid;
+        const bool in = i < FK_H * FK_W;
+        const int ly = i / FK_W, lx = i - ly * FK_W;
+        const unsigned long long k = in ? raw[(ly + 1) * RAW_W + lx + 1] : 1ull;
+        if (in && k != kEmptyKey) fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
+        // warp-aggregated append of the empty cells to the hole list
+        const unsigned empty = __ballot_sync(0xffffffffu, in && k == kEmptyKey);
+        if (empty) {
+            int slot = 0;
+            if (lane == __ffs(empty) - 1) slot = atomicAdd(&n_holes, __popc(empty));
+            slot = __shfl_sync(0xffffffffu, slot, __ffs(empty) - 1);
+            if (in && k == kEmptyKey)
+                holes[slot + __popc(empty & ((1u << lane) - 1u))] = static_cast<unsigned short>(i);
         }
     }
     __syncthreads();
-    for (int ly = ty; ly < FK_H; ly += TY)
-        for (int lx = tx; lx < FK_W; lx += TX) {
-            const unsigned long long k = raw[ly + 1][lx + 1];
-            if (k != kEmptyKey) fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
-            else holes[atomicAdd(&n_holes, 1)] = static_cast<unsigned short>(ly * FK_W + lx);
-        }
-    __syncthreads();
-    for (int h = ty * TX + tx; h < n_holes; h += TX * TY) {
+    for (int h = tid; h < n_holes; h += TX * TY) {
         const int i = holes[h];
         const int ly = i / FK_W, lx = i - ly * FK_W;
         unsigned long long s[8];
@@ -508,7 +521,7 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
         for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
             for (int dk = 0; dk < 3; ++dk)
-                if (dj != 1 || dk != 1) s[m++] = raw[ly + dj][lx + dk];
+                if (dj != 1 || dk != 1) s[m++] = raw[(ly + dj) * RAW_W + lx + dk];
         bool any = false;
 #pragma unroll
         for (int q = 0; q < 8; ++q) any |= s[q] != kEmptyKey;
