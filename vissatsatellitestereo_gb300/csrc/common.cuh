@@ -169,7 +169,7 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 // operations only.  f64_to_f32_slow covers every input; f64_to_f32 runs the straight-line
 // normal-range path and branches to it only for inf/NaN, overflow and the float-subnormal
 // range.
-__device__ __noinline__ float f64_to_f32_slow(double v) {
+static __device__ __noinline__ float f64_to_f32_slow(double v) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
     const unsigned hi = static_cast<unsigned>(b >> 32), lo = static_cast<unsigned>(b);
     const unsigned sign = hi & 0x80000000u;
