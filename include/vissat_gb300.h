@@ -154,6 +154,20 @@ size_t vs_fuse_dsms_workspace_size(int64_t h, int64_t w);
 int vs_fuse_dsms(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
                  int median_blur, void *workspace, size_t workspace_bytes, void *stream);
 
+/* vs_fuse_dsms without a workspace, for callers that cannot allocate device memory where
+ * they call it (a stream-ordered pipeline that forbids allocation after start-up, a
+ * foreign host without a device allocator).  No counterpart in the reference: it is the
+ * same fusion as vs_fuse_dsms, with the blur's intermediate grid in a library-owned
+ * static device array of VS_FUSE_STATIC_MAX_CELLS floats (16 MiB, held by every GPU that
+ * loads the library until exit); larger grids are rejected with VS_ERR_ARG.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  All calls share the array: calls whose
+ * GPU work overlaps (different streams, concurrent threads) race on it.  The array needs
+ * no clearing; each call overwrites what it reads.  No cudaMalloc/cudaFree is called. */
+#define VS_FUSE_STATIC_MAX_CELLS 4194304
+int vs_fuse_dsms_static(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
+                        int median_blur, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,7 @@ VS_LAYOUT_HWV = 0
 VS_LAYOUT_VHW = 1
 VS_CAMERA_PARAMS = 14
 VS_ERROR_STATS = 6
+VS_FUSE_STATIC_MAX_CELLS = 4194304
 
 # VsRpcCamera: 92 doubles in declaration order
 CAMERA_DOUBLES = 92
@@ -55,6 +56,7 @@ SIGNATURES = {
     'vs_dsm_from_points': (_int, [_vp, _vp, _int, _dbl, _dbl, _dbl, _dbl, _i64, _i64, _vp, _vp, _sz, _vp]),
     'vs_fuse_dsms_workspace_size': (_sz, [_i64, _i64]),
     'vs_fuse_dsms': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp, _sz, _vp]),
+    'vs_fuse_dsms_static': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp]),
 }
 
 

@@ -16,6 +16,7 @@
 // local-memory path with the same arithmetic.
 #include <algorithm>
 #include <math.h>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -279,4 +280,51 @@ extern "C" int vs_fuse_dsms(const float *dsm, int layout, int64_t n_views, int64
     VS_LAUNCH_CHECK("fuse_kernel");
     if (median_blur) return launch_blur_f32(dst, out, h, w, st);
     return VS_OK;
+}
+
+// ---- fusion without any device allocation -------------------------------------------------
+// Some callers cannot allocate device memory where they call the fusion: code running in a
+// stream-ordered pipeline that forbids allocation after start-up, or a foreign host with no
+// device allocator of its own.  vs_fuse_dsms_static keeps the blur's intermediate grid in
+// this file-scope array instead of a caller workspace.  Every GPU that loads the library
+// holds the array (16 MiB) until the process exits.
+static __device__ __align__(256) float g_fuse_scratch[VS_FUSE_STATIC_MAX_CELLS + 64];   // + vs_fuse_dsms' 256 B slack
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+float *g_scratch_ptr[kMaxDevices] = {};
+}  // namespace
+
+extern "C" int vs_fuse_dsms_static(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
+                                   int median_blur, void *stream) {
+    VS_REQUIRE(h > 0 && w > 0, "vs_fuse_dsms_static: bad grid %lldx%lld", (long long)h, (long long)w);
+    VS_REQUIRE(h * w <= VS_FUSE_STATIC_MAX_CELLS,
+               "vs_fuse_dsms_static: grid %lldx%lld = %lld cells exceeds the static scratch of %d cells",
+               (long long)h, (long long)w, (long long)(h * w), VS_FUSE_STATIC_MAX_CELLS);
+    if (!median_blur) return vs_fuse_dsms(dsm, layout, n_views, h, w, out, 0, nullptr, 0, stream);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        set_error("vs_fuse_dsms_static: no usable current device");
+        return VS_ERR_CUDA;
+    }
+    float *scratch = nullptr;
+    {
+        // device address of the array on the current device, looked up once per device
+        // (the array's name in host code is only a host-side stand-in)
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        if (!g_scratch_ptr[dev]) {
+            const cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&g_scratch_ptr[dev]), g_fuse_scratch);
+            if (e != cudaSuccess) {
+                g_scratch_ptr[dev] = nullptr;
+                set_error("vs_fuse_dsms_static: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+                return VS_ERR_CUDA;
+            }
+        }
+        scratch = g_scratch_ptr[dev];
+    }
+    // the fusion kernel writes every cell of the scratch grid before the blur reads it, so
+    // nothing has to be cleared between calls
+    return vs_fuse_dsms(dsm, layout, n_views, h, w, out, 1, scratch,
+                        sizeof(float) * static_cast<size_t>(VS_FUSE_STATIC_MAX_CELLS + 64), stream);
 }
