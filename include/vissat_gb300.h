@@ -76,6 +76,25 @@ int vs_rpc_project(const VsRpcCamera *cams, int n_cams, const double *lat, const
                    const double *alt, int64_t n, int64_t point_stride, double *col, double *row,
                    uint8_t *keep, int mode, void *stream);
 
+/* Precision form of the same projection for n_cams cameras over ONE point set given in the
+ * normalised frame (RPCModel.projection after its normalisation, lib/rpc_model.py:164-168
+ * with apply_poly :40-63 and apply_rfm :66-79), evaluated as the contraction
+ * [n x 20 monomials] x [20 x 4*n_cams coefficients] with FP32 accumulation.
+ * xyz: device float32 [3][n] (x = normalised latitude, y = longitude, z = altitude).
+ * colrow: device float32 [n_cams][2][n] (col plane, then row plane, per camera).
+ * variant: VS_CUBE_*.  Max. pixel error against the FP64 projection of the same points
+ * (cameras with line/sample scale 2048, 16 M points): FP32 and BF16X6 below 1e-3 px,
+ * TF32X3 ~1.3e-3 px (two tf32 pieces keep 22 bits), BF16X3 ~0.04 px (two bf16 pieces
+ * keep ~17 bits).  No counterpart in the reference, which evaluates per camera in FP64. */
+#define VS_CUBE_FP32 0     /* CUDA cores, FP32 FMA                                         */
+#define VS_CUBE_BF16X3 1   /* tensor cores, 2 bf16 pieces per factor, 3 products             */
+#define VS_CUBE_TF32X3 2   /* tensor cores, 2 tf32 pieces per factor, 3 products             */
+#define VS_CUBE_BF16X6 3   /* tensor cores, 3 bf16 pieces per factor, 6 products             */
+#define VS_CUBE_MAX_CAMERAS 128
+size_t vs_rpc_project_cube_workspace_size(int n_cams);
+int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const float *xyz, int64_t n, float *colrow,
+                        int variant, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- (b) perspective fit ------------------------------------------------------------ */
 
 /* Replaces solve_perspective (lib/solve_perspective.py:82-126) and its factorize

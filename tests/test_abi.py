@@ -39,6 +39,8 @@ def test_workspace_queries_need_no_gpu():
     assert lib.vs_fuse_dsms_workspace_size(10, 10) >= 400
     assert lib.vs_dlt_fit_workspace_size(0, 10) == 0
     assert lib.vs_camera_approx_workspace_size(50, 800000) > 50 * 800000 * 16
+    assert lib.vs_rpc_project_cube_workspace_size(50) >= 25 * 32 * 64
+    assert lib.vs_rpc_project_cube_workspace_size(0) == 0
 
 
 def test_camera_array_layout():

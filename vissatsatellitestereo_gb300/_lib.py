@@ -25,6 +25,11 @@ VS_LAYOUT_VHW = 1
 VS_CAMERA_PARAMS = 14
 VS_ERROR_STATS = 6
 VS_FUSE_STATIC_MAX_CELLS = 4194304
+VS_CUBE_FP32 = 0
+VS_CUBE_BF16X3 = 1
+VS_CUBE_TF32X3 = 2
+VS_CUBE_BF16X6 = 3
+VS_CUBE_MAX_CAMERAS = 128
 
 # VsRpcCamera: 92 doubles in declaration order
 CAMERA_DOUBLES = 92
@@ -40,6 +45,8 @@ SIGNATURES = {
     'vs_version': (ctypes.c_char_p, []),
     'vs_last_error': (ctypes.c_char_p, []),
     'vs_rpc_project': (_int, [_vp, _int, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
+    'vs_rpc_project_cube_workspace_size': (_sz, [_int]),
+    'vs_rpc_project_cube': (_int, [_vp, _int, _vp, _i64, _vp, _int, _vp, _sz, _vp]),
     'vs_dlt_fit_workspace_size': (_sz, [_int, _i64]),
     'vs_dlt_fit': (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _int, _i64, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     'vs_perspective_error_workspace_size': (_sz, [_int, _i64]),

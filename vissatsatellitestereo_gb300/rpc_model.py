@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._dev import as_device, is_cuda_tensor, ptr, require_cuda, stream_handle
+from ._dev import as_device, is_cuda_tensor, ptr, require_cuda, stream_handle, workspace
 
 MODES = {'exact': _lib.VS_PROJ_EXACT, 'fast': _lib.VS_PROJ_FAST}
 
@@ -83,3 +83,38 @@ def project_cameras(meta_dicts, lat, lon, alt, mode='fast', shared=True, keep=Fa
         _lib.call('vs_rpc_project', ptr(cams), C, ptr(la), ptr(lo), ptr(al), n, stride, ptr(col), ptr(row), ptr(kp),
                   MODES[mode], stream_handle())
     return (col, row, kp) if keep else (col, row)
+
+
+CUBE_VARIANTS = {'fp32': _lib.VS_CUBE_FP32, 'bf16x3': _lib.VS_CUBE_BF16X3, 'tf32x3': _lib.VS_CUBE_TF32X3,
+                 'bf16x6': _lib.VS_CUBE_BF16X6}
+
+
+def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
+    """Precision form of ``RPCModel.projection`` for C cameras over one point set already in
+    the normalised frame (the monomial x coefficient contraction of lib/rpc_model.py:40-79,
+    denormalised as in :164-168).
+
+    xyz: (3, N) float32 (normalised latitude, longitude, altitude), numpy or CUDA tensor.
+    Returns a CUDA float32 tensor (C, 2, N): col plane then row plane per camera.
+    ``variant``: 'fp32' (CUDA cores), 'bf16x3', 'tf32x3', 'bf16x6' (tensor-core split forms).
+    ``out``: optional preallocated (C, 2, N) float32 CUDA tensor.
+    """
+    require_cuda()
+    if variant not in CUBE_VARIANTS:
+        raise ValueError(f'variant must be one of {sorted(CUBE_VARIANTS)}')
+    cams = meta_dicts if isinstance(meta_dicts, torch.Tensor) else torch.from_numpy(_lib.camera_array(meta_dicts))
+    cams = cams.to(device='cuda', dtype=torch.float64).contiguous()
+    C = cams.shape[0]
+    pts = as_device(xyz, torch.float32)
+    if pts.dim() != 2 or pts.shape[0] != 3:
+        raise ValueError(f'xyz must have shape (3, N), got {tuple(pts.shape)}')
+    n = pts.shape[1]
+    if out is None:
+        out = torch.empty((C, 2, n), dtype=torch.float32, device='cuda')
+    elif out.shape != (C, 2, n) or out.dtype != torch.float32 or not out.is_cuda or not out.is_contiguous():
+        raise ValueError('out must be a contiguous CUDA float32 tensor of shape (C, 2, N)')
+    ws_bytes = _lib.lib().vs_rpc_project_cube_workspace_size(C)
+    ws_ptr, ws_len = workspace(ws_bytes)
+    _lib.call('vs_rpc_project_cube', ptr(cams), C, ptr(pts), n, ptr(out), CUBE_VARIANTS[variant], ws_ptr, ws_len,
+              stream_handle())
+    return out
