@@ -162,6 +162,57 @@ int vs_dsm_from_points(const double *points, const int64_t *offsets, int n_views
                        int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
                        void *stream);
 
+/* ---- (c') batched form: many AOIs, per-view FP32 height maps ----------------------------
+ * The per-view point lists of aggregate_2p5d_util.py:75-98 (pixel -> UTM of a height map)
+ * feeding produce_dsm_from_points (produce_dsm.py:46-58) and the per-AOI fusion of
+ * aggregate_2p5d.py:65-81, for many AOIs in one plan.  A view is an FP32 height map with a
+ * pixel -> UTM affine map in fixed point (units of 2^-VS_MAP_FRAC_BITS m):
+ *   easting(i, j)  = (e0 + ej*(2j+1-W) + ei*(2i+1-H)) * 2^-28
+ *   northing(i, j) = (n0 + nj*(2j+1-W) + ni*(2i+1-H)) * 2^-28
+ *   height(i, j)   = heights[i*row_stride + j]   (NaN: no point)
+ * for pixel row i < H, column j < W; the point index (first-of-equal order of the nanmax)
+ * is i*W + j.  These coordinates are exact doubles, so the result is bit-identical to
+ * materialising the FP64 point list and running proj_to_grid + the float32 3x3 median
+ * blur per view, then the fusion per AOI.  The plan rejects (VS_ERR_ARG) grids whose
+ * origin is not positive or whose extent crosses a power of two, and views whose
+ * coordinates would not stay exact. */
+#define VS_MAP_FRAC_BITS 28
+typedef struct VsAoi {
+    double xoff, yoff, xres, yres;   /* DSM grid, as proj_to_grid's arguments */
+    int64_t xsize, ysize;
+    int32_t first_view, n_views;     /* the AOI's views: consecutive entries of the view array */
+} VsAoi;
+typedef struct VsMapView {
+    const float *heights;            /* device, row-major [height][row_stride] */
+    int64_t row_stride;              /* elements, >= width */
+    int32_t width, height;
+    int32_t aoi, reserved;
+    int64_t e0, n0;                  /* fixed-point origin terms (|.| < 2^53) */
+    int32_t ej, ei, nj, ni;          /* fixed-point half-pixel steps */
+} VsMapView;
+/* Opaque host-side plan: validated descriptors and per-AOI binning tables uploaded into the
+ * plan workspace.  Planning synchronises `stream`; running does not, and launches kernels
+ * only (a run can be captured in a CUDA graph).  One plan serves one stream at a time. */
+typedef struct VsAoiBatch VsAoiBatch;
+size_t vs_aoi_batch_plan_workspace_size(const VsAoi *aois, int n_aois, int n_views);
+int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView *views, int n_views,
+                      int rows_per_item, void *workspace, size_t workspace_bytes, VsAoiBatch **plan,
+                      void *stream);
+/* Cells of all views' DSMs (view v at the sum of the cells of views < v), of all fused
+ * DSMs (AOI a at the sum of the cells of AOIs < a), and the scratch a run needs. */
+int vs_aoi_batch_query(const VsAoiBatch *plan, int64_t *view_cells, int64_t *fused_cells,
+                       size_t *scratch_bytes);
+/* Rasterises views [view_begin, view_end) into their float32 DSMs: one persistent binning
+ * launch over all their pixels (work items of rows_per_item map rows, taken from a
+ * device-side counter by bin_blocks_per_sm CTAs per SM) and one epilogue launch over all
+ * their 32x32 tiles (nanmax decode, hole fill, blur).  A single view is the per-view form. */
+int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int bin_blocks_per_sm,
+                     void *scratch, size_t scratch_bytes, float *view_dsm, void *stream);
+/* Fuses AOIs [aoi_begin, aoi_end) from their views' DSMs (vs_fuse_dsms per AOI). */
+int vs_aoi_batch_fuse(const VsAoiBatch *plan, int aoi_begin, int aoi_end, const float *view_dsm,
+                      float *fused, int median_blur, void *scratch, size_t scratch_bytes, void *stream);
+void vs_aoi_batch_destroy(VsAoiBatch *plan);
+
 /* ---- (d) fusion ----------------------------------------------------------------------- */
 
 /* Replaces the fusion block of run_fuse (aggregate_2p5d.py:65-81): per cell, reject

@@ -1,0 +1,170 @@
+"""Batched form over many AOIs: per-view FP32 height maps -> per-view DSMs -> fused DSMs.
+
+The reference produces one AOI at a time: per view, the depth map's pixels become UTM
+points (aggregate_2p5d_util.py:75-98), ``produce_dsm_from_points`` rasterises them
+(produce_dsm.py:46-58: proj_to_grid + the float32 3x3 median blur), and ``run_fuse``
+fuses the AOI's views (aggregate_2p5d.py:65-81).  ``AoiBatch`` plans many AOIs at once:
+the rasterisation of all their views is one persistent binning launch and one epilogue
+launch (``run``), and the fusion follows per AOI (``fuse``).  A view's points are its
+height-map pixels placed by a fixed-point affine pixel -> UTM map (``MapAffine``), whose
+coordinates are exact doubles, so every DSM is bit-identical to materialising the FP64
+point list and running the per-view reference path.
+"""
+import ctypes
+import math
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib
+from ._dev import require_cuda, stream_handle
+
+FRAC_BITS = 28
+
+
+class VsAoi(ctypes.Structure):
+    _fields_ = [('xoff', ctypes.c_double), ('yoff', ctypes.c_double), ('xres', ctypes.c_double),
+                ('yres', ctypes.c_double), ('xsize', ctypes.c_int64), ('ysize', ctypes.c_int64),
+                ('first_view', ctypes.c_int32), ('n_views', ctypes.c_int32)]
+
+
+class VsMapView(ctypes.Structure):
+    _fields_ = [('heights', ctypes.c_void_p), ('row_stride', ctypes.c_int64), ('width', ctypes.c_int32),
+                ('height', ctypes.c_int32), ('aoi', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('e0', ctypes.c_int64), ('n0', ctypes.c_int64), ('ej', ctypes.c_int32), ('ei', ctypes.c_int32),
+                ('nj', ctypes.c_int32), ('ni', ctypes.c_int32)]
+
+
+@dataclass
+class MapAffine:
+    """Pixel (i, j) of a W x H map -> easting (e0 + ej(2j+1-W) + ei(2i+1-H)) 2^-28 and
+    northing (n0 + nj(2j+1-W) + ni(2i+1-H)) 2^-28 metres (integers)."""
+    e0: int
+    n0: int
+    ej: int
+    ei: int
+    nj: int
+    ni: int
+
+    @staticmethod
+    def rotated(ce, cn, gsd, theta):
+        """The synthetic view geometry: pixel centres on a grid of spacing ``gsd`` rotated
+        by ``theta`` about the image centre (ce, cn), rows running south."""
+        s = float(1 << FRAC_BITS)
+        c, sn = math.cos(theta), math.sin(theta)
+        return MapAffine(e0=int(round(ce * s)), n0=int(round(cn * s)), ej=int(round(gsd * c / 2 * s)),
+                         ei=int(round(-gsd * sn / 2 * s)), nj=int(round(-gsd * sn / 2 * s)),
+                         ni=int(round(-gsd * c / 2 * s)))
+
+
+@dataclass
+class AoiGrid:
+    xoff: float
+    yoff: float
+    xres: float
+    yres: float
+    xsize: int
+    ysize: int
+
+
+@dataclass
+class MapView:
+    heights: torch.Tensor      # CUDA float32, (H, stride) storage; the view uses [:height, :width]
+    width: int
+    height: int
+    affine: MapAffine
+
+
+class AoiBatch:
+    """A plan over ``grids`` (one per AOI) and ``views`` (a list per AOI of ``MapView``).
+
+    ``run()`` rasterises all views (or a range) into the per-view DSM buffer;
+    ``fuse()`` fuses each AOI's views into the fused buffer.  ``view_dsm(v)`` and
+    ``fused_dsm(a)`` return the (H, W) slices."""
+
+    def __init__(self, grids, views, rows_per_item=8):
+        require_cuda()
+        self.grids = list(grids)
+        self.views = [list(vs) for vs in views]
+        if len(self.grids) != len(self.views):
+            raise ValueError('one view list per AOI grid')
+        self.rows_per_item = int(rows_per_item)
+        n_aois = len(self.grids)
+        flat = [(a, v) for a, vs in enumerate(self.views) for v in vs]
+        self.n_views = len(flat)
+        self.aoi_arr = (VsAoi * n_aois)()
+        first = 0
+        for a, (g, vs) in enumerate(zip(self.grids, self.views)):
+            self.aoi_arr[a] = VsAoi(g.xoff, g.yoff, g.xres, g.yres, g.xsize, g.ysize, first, len(vs))
+            first += len(vs)
+        self.view_arr = (VsMapView * self.n_views)()
+        self._keep = []
+        for i, (a, v) in enumerate(flat):
+            h = v.heights
+            if not (h.is_cuda and h.dtype == torch.float32 and h.dim() == 2 and h.stride(1) == 1):
+                raise ValueError('heights must be a 2-D CUDA float32 tensor with unit column stride')
+            if h.shape[0] < v.height or h.shape[1] < v.width:
+                raise ValueError('heights smaller than the view')
+            self._keep.append(h)
+            m = v.affine
+            self.view_arr[i] = VsMapView(h.data_ptr(), h.stride(0), v.width, v.height, a, 0, m.e0, m.n0, m.ej, m.ei,
+                                         m.nj, m.ni)
+        lib = _lib.lib()
+        nbytes = lib.vs_aoi_batch_plan_workspace_size(self.aoi_arr, n_aois, self.n_views)
+        self._plan_ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device='cuda')
+        self._plan = ctypes.c_void_p()
+        _lib.call('vs_aoi_batch_plan', self.aoi_arr, n_aois, self.view_arr, self.n_views, self.rows_per_item,
+                  self._plan_ws.data_ptr(), self._plan_ws.numel(), ctypes.byref(self._plan), stream_handle())
+        vc, fc, sb = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_size_t()
+        _lib.call('vs_aoi_batch_query', self._plan, ctypes.byref(vc), ctypes.byref(fc), ctypes.byref(sb))
+        self.view_cells, self.fused_cells, self.scratch_bytes = vc.value, fc.value, sb.value
+        self.view_off = [0]
+        self.fused_off = [0]
+        for a, (g, vs) in enumerate(zip(self.grids, self.views)):
+            for _ in vs:
+                self.view_off.append(self.view_off[-1] + g.xsize * g.ysize)
+            self.fused_off.append(self.fused_off[-1] + g.xsize * g.ysize)
+        self.first_view = [self.aoi_arr[a].first_view for a in range(n_aois)]
+        self.view_aoi = [a for a, _ in flat]
+        self.pixels = sum(v.width * v.height for _, v in flat)
+
+    def close(self):
+        if self._plan:
+            _lib.lib().vs_aoi_batch_destroy(self._plan)
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def new_view_dsm(self):
+        return torch.empty(self.view_cells, dtype=torch.float32, device='cuda')
+
+    def new_fused(self):
+        return torch.empty(self.fused_cells, dtype=torch.float32, device='cuda')
+
+    def new_scratch(self):
+        return torch.empty(self.scratch_bytes, dtype=torch.uint8, device='cuda')
+
+    def run(self, view_dsm, scratch, views=None, bin_blocks_per_sm=4):
+        """Rasterise views[0]..views[1]-1 (all by default) into ``view_dsm``."""
+        v0, v1 = (0, self.n_views) if views is None else views
+        _lib.call('vs_aoi_batch_run', self._plan, v0, v1, int(bin_blocks_per_sm), scratch.data_ptr(),
+                  scratch.numel(), view_dsm.data_ptr(), stream_handle())
+        return view_dsm
+
+    def fuse(self, view_dsm, fused, scratch, aois=None, median_blur=True):
+        a0, a1 = (0, len(self.grids)) if aois is None else aois
+        _lib.call('vs_aoi_batch_fuse', self._plan, a0, a1, view_dsm.data_ptr(), fused.data_ptr(),
+                  int(bool(median_blur)), scratch.data_ptr(), scratch.numel(), stream_handle())
+        return fused
+
+    def view_dsm(self, buf, v):
+        g = self.grids[self.view_aoi[v]]
+        return buf[self.view_off[v]:self.view_off[v + 1]].view(g.ysize, g.xsize)
+
+    def fused_dsm(self, buf, a):
+        g = self.grids[a]
+        return buf[self.fused_off[a]:self.fused_off[a + 1]].view(g.ysize, g.xsize)

@@ -30,6 +30,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "common.cuh"
 
@@ -469,63 +470,69 @@ __global__ void median_blur3x3_kernel(const T *__restrict__ in, float *__restric
 constexpr int TX = 32, TY = 8, TILE_Y = 32;
 constexpr int RAW_W = TX + 4, RAW_H = TILE_Y + 4, FK_W = TX + 2, FK_H = TILE_Y + 2;
 
-// It also clears this tile of the idle key grid (the next view's), which nobody reads
+// Shared-memory working set of one epilogue tile.
+struct EpilogueSmem {
+    unsigned long long raw[RAW_H * RAW_W];   // 0: empty cell or outside the image
+    unsigned fk[FK_H][FK_W];                 // blur keys of the hole-filled cells
+    unsigned short holes[FK_H * FK_W];
+    int n_holes;
+};
+
+// One 32 x 32 output tile: keys (decoded by `dec(key, cell)`, which resolves zero keys to
+// their signed value) -> nanmax values -> hole fill -> float32 -> 3x3 median blur.
+// Threads are TX x TY; the caller synchronises before reusing `sm`.  With `next_keys` it
+// also clears this tile of the idle key grid (the next view's), which nobody reads
 // concurrently, so no per-view memset is needed.  Empty cells (a few percent) are
 // collected in a shared list and filled by consecutive threads, so the hole-fill work does
 // not diverge every warp that happens to hold one.
-__global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
-    const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
-    const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys, int H,
-    int W) {
-    __shared__ unsigned long long raw[RAW_H * RAW_W];   // 0: empty cell or outside the image
-    __shared__ unsigned fk[FK_H][FK_W];                 // blur keys of the hole-filled cells
-    __shared__ unsigned short holes[FK_H * FK_W];
-    __shared__ int n_holes;
-    const int r0 = blockIdx.y * TILE_Y, c0 = blockIdx.x * TX;
+template <class Dec>
+__device__ __forceinline__ void epilogue_tile(const unsigned long long *__restrict__ vk, const Dec &dec,
+                                              float *__restrict__ out, unsigned long long *__restrict__ next_keys,
+                                              int H, int W, int r0, int c0, EpilogueSmem &sm) {
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx, lane = tid & 31;
-    if (tid == 0) n_holes = 0;
+    if (tid == 0) sm.n_holes = 0;
     for (int i = tid; i < RAW_H * RAW_W; i += TX * TY) {
         const int ly = i / RAW_W, lx = i - ly * RAW_W;
         const int r = r0 + ly - 2, c = c0 + lx - 2;
         unsigned long long k = kEmptyKey;
         if (static_cast<unsigned>(r) < static_cast<unsigned>(H) && static_cast<unsigned>(c) < static_cast<unsigned>(W)) {
             const long long cell = static_cast<long long>(r) * W + c;
-            k = cell_key(vk[cell], cell, first, pts);
+            k = dec(vk[cell], cell);
         }
-        raw[i] = k;
+        sm.raw[i] = k;
     }
     __syncthreads();
     for (int base = 0; base < FK_H * FK_W; base += TX * TY) {
         const int i = base + tid;
         const bool in = i < FK_H * FK_W;
         const int ly = i / FK_W, lx = i - ly * FK_W;
-        const unsigned long long k = in ? raw[(ly + 1) * RAW_W + lx + 1] : 1ull;
-        if (in && k != kEmptyKey) fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
+        const unsigned long long k = in ? sm.raw[(ly + 1) * RAW_W + lx + 1] : 1ull;
+        if (in && k != kEmptyKey) sm.fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
         // warp-aggregated append of the empty cells to the hole list
         const unsigned empty = __ballot_sync(0xffffffffu, in && k == kEmptyKey);
         if (empty) {
             int slot = 0;
-            if (lane == __ffs(empty) - 1) slot = atomicAdd(&n_holes, __popc(empty));
+            if (lane == __ffs(empty) - 1) slot = atomicAdd(&sm.n_holes, __popc(empty));
             slot = __shfl_sync(0xffffffffu, slot, __ffs(empty) - 1);
             if (in && k == kEmptyKey)
-                holes[slot + __popc(empty & ((1u << lane) - 1u))] = static_cast<unsigned short>(i);
+                sm.holes[slot + __popc(empty & ((1u << lane) - 1u))] = static_cast<unsigned short>(i);
         }
     }
     __syncthreads();
-    for (int h = tid; h < n_holes; h += TX * TY) {
-        const int i = holes[h];
+    for (int h = tid; h < sm.n_holes; h += TX * TY) {
+        const int i = sm.holes[h];
         const int ly = i / FK_W, lx = i - ly * FK_W;
-        unsigned long long s[8];
+        unsigned long long s8[8];
         int m = 0;
 #pragma unroll
         for (int dj = 0; dj < 3; ++dj)
 #pragma unroll
             for (int dk = 0; dk < 3; ++dk)
-                if (dj != 1 || dk != 1) s[m++] = raw[(ly + dj) * RAW_W + lx + dk];
+                if (dj != 1 || dk != 1) s8[m++] = sm.raw[(ly + dj) * RAW_W + lx + dk];
         bool any = false;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) any |= s[q] != kEmptyKey;
-        fk[ly][lx] = any ? blur_key(f64_to_f32(median8_keys(s))) : 0xffffffffu;
+        for (int q = 0; q < 8; ++q) any |= s8[q] != kEmptyKey;
+        sm.fk[ly][lx] = any ? blur_key(f64_to_f32(median8_keys(s8))) : 0xffffffffu;
     }
     __syncthreads();
     const int c = c0 + tx;
@@ -542,9 +549,26 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
         if (r == H - 1) yc = yb;
         const long long cell = static_cast<long long>(r) * W + c;
         if (next_keys) next_keys[cell] = kEmptyKey;
-        out[cell] = median9(fk[ya][xa], fk[yb][xa], fk[yc][xa], fk[ya][xb], fk[yb][xb], fk[yc][xb], fk[ya][xc],
-                            fk[yb][xc], fk[yc][xc]);
+        out[cell] = median9(sm.fk[ya][xa], sm.fk[yb][xa], sm.fk[yc][xa], sm.fk[ya][xb], sm.fk[yb][xb], sm.fk[yc][xb],
+                            sm.fk[ya][xc], sm.fk[yb][xc], sm.fk[yc][xc]);
     }
+}
+
+// Zero keys resolved through the per-cell "first zero" word and the point list.
+struct PointsZeroDecoder {
+    const unsigned long long *first;
+    const double *pts;
+    __device__ __forceinline__ unsigned long long operator()(unsigned long long k, long long cell) const {
+        return cell_key(k, cell, first, pts);
+    }
+};
+
+__global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
+    const unsigned long long *__restrict__ vk, const unsigned long long *__restrict__ first,
+    const double *__restrict__ pts, float *__restrict__ out, unsigned long long *__restrict__ next_keys, int H,
+    int W) {
+    __shared__ EpilogueSmem sm;
+    epilogue_tile(vk, PointsZeroDecoder{first, pts}, out, next_keys, H, W, blockIdx.y * TILE_Y, blockIdx.x * TX, sm);
 }
 
 // ---- host side --------------------------------------------------------------------------
@@ -667,6 +691,175 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
         bin_max_kernel<true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
     }
     return check_launch("bin_max_kernel");
+}
+
+// ---- batched form: per-view FP32 height maps, many AOIs -----------------------------------
+// A view's points are its height-map pixels, placed by a fixed-point affine pixel -> UTM
+// map (units of 2^-28 m).  Coordinates are exact doubles, and in the binade of the grid
+// origin (contained grid) the double bit pattern of x = x_fx * 2^-28 is
+//     bits(x) = ((E + 1023) << 52) - 2^52 + (x_fx << (24 - E)),   E = exponent of the origin,
+// an integer expression that is monotone in x_fx; outside the binade it leaves the origin's
+// exponent field, which the axis test rejects (off-grid, as the containment guarantees).
+// So each pixel is binned with integer and FP32 operations only, reading 4 bytes.
+constexpr unsigned long long kMapIdxLimit = 1ull << 28;   // pixels per view
+constexpr unsigned long long kMapZeroSpan = kMapIdxLimit << 1;
+
+struct MapViewDev {
+    const float *map;
+    long long stride;
+    long long e0, n0;
+    int ej, ei, nj, ni;
+    int W, H;
+    int aoi;
+    int vec;                  // rows are 16-byte aligned: float4 loads
+    long long off;            // cell offset of the view's key grid / DSM
+};
+
+struct AoiDev {
+    FastAxis row, col;
+    long long bx, by;         // bit-pattern bases of the origins' binades
+    int shx, shy;
+    int xsize, ysize;
+};
+
+// 64-bit key of double(h) from the float's bits; zeros carry their complemented pixel index
+// and sign in the low bits (kZeroKey + 2*(limit-1-idx) + sign), so the largest zero key is
+// the first zero and no per-cell "first zero" word is needed.  Non-zero FP32 values have
+// keys at least 2^61 away from kZeroKey.
+__device__ __noinline__ unsigned long long map_key_rare(unsigned hb) {
+    return key_from_double(f32_to_f64(__uint_as_float(hb)));
+}
+
+__device__ __forceinline__ unsigned long long map_key(unsigned hb, unsigned long long idx) {
+    const unsigned mag = hb & 0x7fffffffu;
+    if (mag == 0u) return kZeroKey + (((kMapIdxLimit - 1ull - idx) << 1) | (hb >> 31));
+    if ((mag >> 23) - 1u >= 254u) return map_key_rare(hb);     // subnormal or infinite
+    const unsigned long long db = (static_cast<unsigned long long>(mag) << 29) + (896ull << 52);
+    return (hb >> 31) ? (0x7fffffffffffffffull - db) : (db | 0x8000000000000000ull);
+}
+
+// Resolves the zero keys of a map-fed key grid to the keys of +0.0 / -0.0.
+struct MapZeroDecoder {
+    __device__ __forceinline__ unsigned long long operator()(unsigned long long k, long long) const {
+        if (k - kZeroKey < kMapZeroSpan) return (k & 1ull) ? 0x7fffffffffffffffull : kZeroKey;
+        return k;
+    }
+};
+
+// Largest index i in [lo, hi] with starts[i] <= x (starts ascending, starts[lo] <= x).
+__device__ __forceinline__ int find_range(const long long *starts, int lo, int hi, long long x) {
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(starts + mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+constexpr int kMapThreads = 256;
+
+// Persistent binning of many views: a CTA takes work items (rows_per_item map rows of one
+// view) from a device counter until none are left.  Items [item_begin, item_end) of the
+// plan's item list.
+__global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
+    const MapViewDev *__restrict__ views, const AoiDev *__restrict__ aois, const long long *__restrict__ item_start,
+    int v_lo, int v_hi, long long item_begin, long long item_end, int rows_per_item,
+    unsigned long long *__restrict__ keys, unsigned long long *__restrict__ counter) {
+    __shared__ long long s_item;
+    __shared__ int s_view;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long it = item_begin + static_cast<long long>(atomicAdd(counter, 1ull));
+            s_item = it;
+            s_view = it < item_end ? find_range(item_start, v_lo, v_hi, it) : -1;
+        }
+        __syncthreads();
+        const long long it = s_item;
+        const int v = s_view;
+        __syncthreads();
+        if (it >= item_end) return;
+        const MapViewDev mv = views[v];
+        const AoiDev &ad = aois[mv.aoi];
+        const FastAxis R = ad.row, C = ad.col;
+        const long long bx = ad.bx, by = ad.by;
+        const int shx = ad.shx, shy = ad.shy;
+        const unsigned long long ncols = static_cast<unsigned>(ad.xsize);
+        unsigned long long *vk = keys + mv.off;
+        const int i0 = static_cast<int>(it - __ldg(item_start + v)) * rows_per_item;
+        const int i1 = min(i0 + rows_per_item, mv.H);
+        const int groups = (mv.W + 3) >> 2;          // 4-pixel groups per row
+        int i = i0, g = threadIdx.x;
+        while (g >= groups && i < i1) { g -= groups; ++i; }
+        for (; i < i1;) {
+            const int j0 = g << 2;
+            const float *row = mv.map + static_cast<long long>(i) * mv.stride;
+            unsigned hb[4];
+            if (mv.vec && j0 + 4 <= mv.W) {
+                const float4 q = __ldcs(reinterpret_cast<const float4 *>(row + j0));
+                hb[0] = __float_as_uint(q.x); hb[1] = __float_as_uint(q.y);
+                hb[2] = __float_as_uint(q.z); hb[3] = __float_as_uint(q.w);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) hb[k] = j0 + k < mv.W ? __float_as_uint(__ldcs(row + j0 + k)) : 0x7fc00000u;
+            }
+            const int di2 = 2 * i + 1 - mv.H;
+            const long long rx = mv.e0 + static_cast<long long>(mv.ei) * di2;
+            const long long ry = mv.n0 + static_cast<long long>(mv.ni) * di2;
+            long long cell[4];
+            unsigned long long key[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int dj2 = 2 * (j0 + k) + 1 - mv.W;
+                const long long xf = rx + static_cast<long long>(mv.ej) * dj2;
+                const long long yf = ry + static_cast<long long>(mv.nj) * dj2;
+                int r, c;
+                long long dr, dc;
+                bool sr, sc;
+                bool ok = axis_fast<true>(R, by + (yf << shy), r, dr, sr);
+                ok &= axis_fast<false>(C, bx + (xf << shx), c, dc, sc);
+                ok &= (hb[k] & 0x7fffffffu) <= 0x7f800000u;     // not NaN
+                if (ok && !sr) r = axis_correct(R.thr, r, dr);
+                if (ok && !sc) c = axis_correct(C.thr, c, dc);
+                const long long cl = static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(r)) * ncols) + c;
+                const unsigned long long idx = static_cast<unsigned long long>(i) * static_cast<unsigned>(mv.W) + (j0 + k);
+                key[k] = ok ? map_key(hb[k], idx) : kEmptyKey;
+                cell[k] = ok ? cl : -1 - k;
+            }
+#pragma unroll
+            for (int k = 1; k < 4; ++k) {     // merge runs of consecutive pixels in one cell
+                const bool same = cell[k] == cell[k - 1];
+                key[k] = same ? max(key[k], key[k - 1]) : key[k];
+                key[k - 1] = same ? kEmptyKey : key[k - 1];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (key[k] != kEmptyKey) atomicMax(vk + cell[k], key[k]);
+            g += kMapThreads;
+            while (g >= groups && i < i1) { g -= groups; ++i; }
+        }
+    }
+}
+
+// Persistent epilogue over the 32x32 tiles of many views: tiles [tile_begin, tile_end).
+__global__ void __launch_bounds__(TX *TY) map_epilogue_kernel(
+    const MapViewDev *__restrict__ views, const AoiDev *__restrict__ aois, const long long *__restrict__ tile_start,
+    int v_lo, int v_hi, long long tile_begin, long long tile_end, const unsigned long long *__restrict__ keys,
+    float *__restrict__ dsm) {
+    __shared__ EpilogueSmem sm;
+    __shared__ int s_view;
+    for (long long t = tile_begin + blockIdx.x; t < tile_end; t += gridDim.x) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) s_view = find_range(tile_start, v_lo, v_hi, t);
+        __syncthreads();
+        const int v = s_view;
+        const MapViewDev &mv = views[v];
+        const AoiDev &ad = aois[mv.aoi];
+        const int W = ad.xsize, H = ad.ysize;
+        const int tiles_x = (W + TX - 1) / TX;
+        const long long local = t - __ldg(tile_start + v);
+        const int ty = static_cast<int>(local / tiles_x), tx = static_cast<int>(local - static_cast<long long>(ty) * tiles_x);
+        epilogue_tile(keys + mv.off, MapZeroDecoder{}, dsm + mv.off, nullptr, H, W, ty * TILE_Y, tx * TX, sm);
+        __syncthreads();
+    }
 }
 
 int clear(void *p, size_t bytes, cudaStream_t st) {
@@ -792,3 +985,279 @@ extern "C" int vs_median_blur3x3_f64(const double *in, float *out, int64_t h, in
     VS_LAUNCH_CHECK("median_blur3x3_kernel<double>");
     return VS_OK;
 }
+
+// ---- batched form: plan and run ------------------------------------------------------------
+struct VsAoiBatch {
+    int n_aois = 0, n_views = 0, rows_per_item = 0;
+    std::vector<VsAoi> aois;
+    std::vector<long long> view_off, fused_off, item_start, tile_start;
+    long long view_cells = 0, fused_cells = 0, max_fuse_cells = 0;
+    vs::MapViewDev *d_views = nullptr;
+    vs::AoiDev *d_aois = nullptr;
+    long long *d_item_start = nullptr, *d_tile_start = nullptr;
+    unsigned long long *d_counter = nullptr;
+    std::vector<vs::MapViewDev> h_views;   // host copies, alive while their upload runs
+    std::vector<vs::AoiDev> h_aois;
+};
+
+namespace vs {
+namespace {
+
+struct PlanLayout {
+    MapViewDev *views;
+    AoiDev *aois;
+    long long *item_start, *tile_start;
+    unsigned long long *counter;
+    long long *thr;
+    size_t bytes;
+};
+
+PlanLayout carve_plan(void *ws, const VsAoi *aois, int n_aois, int n_views) {
+    Carver cv(ws);
+    PlanLayout p;
+    p.views = cv.take<MapViewDev>(n_views);
+    p.aois = cv.take<AoiDev>(n_aois);
+    p.item_start = cv.take<long long>(n_views + 1);
+    p.tile_start = cv.take<long long>(n_views + 1);
+    p.counter = cv.take<unsigned long long>(2);
+    size_t thr = 0;
+    for (int a = 0; a < n_aois; ++a) thr += static_cast<size_t>(aois[a].xsize + 1) + static_cast<size_t>(aois[a].ysize + 1);
+    p.thr = cv.take<long long>(thr);
+    p.bytes = cv.used;
+    return p;
+}
+
+// Fixed-point view coordinates stay exact doubles and shifted bit patterns stay in range.
+bool map_axis_ok(long long o, int sj, int si, int W, int H, int sh) {
+    const long long lim = 1LL << 52;
+    if (o <= -lim || o >= lim) return false;
+    const long long dj = W - 1, di = H - 1;
+    for (int a = -1; a <= 1; a += 2)
+        for (int b = -1; b <= 1; b += 2) {
+            const long long v = o + static_cast<long long>(sj) * dj * a + static_cast<long long>(si) * di * b;
+            if (v <= -lim || v >= lim) return false;
+            const long long mag = v < 0 ? -v : v;
+            if (mag >= (1LL << (62 - sh))) return false;
+        }
+    return true;
+}
+
+}  // namespace
+}  // namespace vs
+
+extern "C" size_t vs_aoi_batch_plan_workspace_size(const VsAoi *aois, int n_aois, int n_views) {
+    if (!aois || n_aois <= 0 || n_views <= 0) return 0;
+    for (int a = 0; a < n_aois; ++a)
+        if (aois[a].xsize <= 0 || aois[a].ysize <= 0) return 0;
+    return carve_plan(nullptr, aois, n_aois, n_views).bytes + 256;
+}
+
+extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView *views, int n_views,
+                                 int rows_per_item, void *workspace, size_t workspace_bytes, VsAoiBatch **plan,
+                                 void *stream) {
+    VS_REQUIRE(aois && views && plan && workspace && n_aois > 0 && n_views > 0 && n_views < (1 << 30) &&
+                   rows_per_item > 0 && rows_per_item <= 65536,
+               "vs_aoi_batch_plan: bad arguments");
+    *plan = nullptr;
+    const size_t need = vs_aoi_batch_plan_workspace_size(aois, n_aois, n_views);
+    VS_REQUIRE(need > 0, "vs_aoi_batch_plan: empty grid");
+    if (workspace_bytes < need) {
+        set_error("vs_aoi_batch_plan: workspace %zu < %zu bytes", workspace_bytes, need);
+        return VS_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream);
+    PlanLayout L = carve_plan(workspace, aois, n_aois, n_views);
+    VsAoiBatch *p = new VsAoiBatch();
+    p->n_aois = n_aois;
+    p->n_views = n_views;
+    p->rows_per_item = rows_per_item;
+    p->aois.assign(aois, aois + n_aois);
+    p->h_aois.resize(n_aois);
+    p->h_views.resize(n_views);
+    p->view_off.resize(n_views + 1);
+    p->item_start.resize(n_views + 1);
+    p->tile_start.resize(n_views + 1);
+    p->fused_off.resize(n_aois + 1);
+    auto fail = [&](int code) {
+        delete p;
+        return code;
+    };
+    long long *thr = L.thr;
+    p->fused_off[0] = 0;
+    int expect_view = 0;
+    for (int a = 0; a < n_aois; ++a) {
+        const VsAoi &A = aois[a];
+        if (!(grid_ok(A.xsize, A.ysize) && A.xsize < (1LL << 22) && A.ysize < (1LL << 22) && A.n_views > 0 &&
+              A.first_view == expect_view && A.xoff > 0.0 && A.yoff > 0.0)) {
+            set_error("vs_aoi_batch_plan: AOI %d: bad grid or view range (views must be consecutive, origin positive)", a);
+            return fail(VS_ERR_ARG);
+        }
+        expect_view += A.n_views;
+        Tables tb;
+        int s = make_axis(tb.row, A.yoff, A.xres, A.ysize, -1, thr, st);
+        thr += A.ysize + 1;
+        if (s == VS_OK) s = make_axis(tb.col, A.xoff, A.yres, A.xsize, +1, thr, st);
+        thr += A.xsize + 1;
+        if (s != VS_OK) return fail(s);
+        if (!(tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained)) {
+            set_error("vs_aoi_batch_plan: AOI %d: grid extent crosses a power of two of its origin", a);
+            return fail(VS_ERR_ARG);
+        }
+        AoiDev &ad = p->h_aois[a];
+        const Axis *ax[2] = {&tb.row, &tb.col};
+        FastAxis *fa[2] = {&ad.row, &ad.col};
+        for (int k = 0; k < 2; ++k) {
+            memcpy(&fa[k]->off_bits, &ax[k]->off, sizeof(long long));
+            fa[k]->tmax = ax[k]->tmax;
+            fa[k]->thr = ax[k]->thr;
+            fa[k]->top12 = ax[k]->top12;
+            fa[k]->shift = ax[k]->shift;
+            fa[k]->nm1 = static_cast<int>(ax[k]->n - 1);
+            fa[k]->scale = ax[k]->scale;
+            fa[k]->err_abs = ax[k]->err_abs;
+            fa[k]->err_rel = ax[k]->err_rel;
+        }
+        int ex = 0, ey = 0;
+        frexp(A.xoff, &ex);
+        frexp(A.yoff, &ey);
+        ex -= 1;   // 2^ex <= xoff < 2^(ex+1)
+        ey -= 1;
+        if (ex < 0 || ex > 24 || ey < 0 || ey > 24) {
+            set_error("vs_aoi_batch_plan: AOI %d: origin outside [1, 2^25) m", a);
+            return fail(VS_ERR_ARG);
+        }
+        ad.shx = 24 - ex;
+        ad.shy = 24 - ey;
+        ad.bx = (static_cast<long long>(ex + 1023) << 52) - (1LL << 52);
+        ad.by = (static_cast<long long>(ey + 1023) << 52) - (1LL << 52);
+        ad.xsize = static_cast<int>(A.xsize);
+        ad.ysize = static_cast<int>(A.ysize);
+        const long long cells = A.xsize * A.ysize;
+        p->fused_off[a + 1] = p->fused_off[a] + cells;
+        p->max_fuse_cells = std::max(p->max_fuse_cells, cells);
+    }
+    if (expect_view != n_views) {
+        set_error("vs_aoi_batch_plan: the AOIs cover %d views, %d given", expect_view, n_views);
+        return fail(VS_ERR_ARG);
+    }
+    p->view_off[0] = p->item_start[0] = p->tile_start[0] = 0;
+    for (int v = 0; v < n_views; ++v) {
+        const VsMapView &V = views[v];
+        const bool aoi_ok = V.aoi >= 0 && V.aoi < n_aois && v >= aois[V.aoi].first_view &&
+                            v < aois[V.aoi].first_view + aois[V.aoi].n_views;
+        if (!(aoi_ok && V.heights && V.width > 0 && V.height > 0 && V.row_stride >= V.width &&
+              static_cast<unsigned long long>(V.width) * static_cast<unsigned long long>(V.height) <= kMapIdxLimit)) {
+            set_error("vs_aoi_batch_plan: view %d: bad size, stride, map or AOI index", v);
+            return fail(VS_ERR_ARG);
+        }
+        const AoiDev &ad = p->h_aois[V.aoi];
+        if (!map_axis_ok(V.e0, V.ej, V.ei, V.width, V.height, ad.shx) ||
+            !map_axis_ok(V.n0, V.nj, V.ni, V.width, V.height, ad.shy)) {
+            set_error("vs_aoi_batch_plan: view %d: fixed-point coordinates out of the exact range", v);
+            return fail(VS_ERR_ARG);
+        }
+        MapViewDev &d = p->h_views[v];
+        d.map = V.heights;
+        d.stride = V.row_stride;
+        d.e0 = V.e0;
+        d.n0 = V.n0;
+        d.ej = V.ej;
+        d.ei = V.ei;
+        d.nj = V.nj;
+        d.ni = V.ni;
+        d.W = V.width;
+        d.H = V.height;
+        d.aoi = V.aoi;
+        d.vec = ((reinterpret_cast<uintptr_t>(V.heights) & 15) == 0) && (V.row_stride % 4 == 0);
+        d.off = p->view_off[v];
+        const VsAoi &A = aois[V.aoi];
+        const long long cells = A.xsize * A.ysize;
+        p->view_off[v + 1] = p->view_off[v] + cells;
+        p->item_start[v + 1] = p->item_start[v] + ceil_div(V.height, rows_per_item);
+        p->tile_start[v + 1] = p->tile_start[v] + ceil_div(A.xsize, TX) * ceil_div(A.ysize, TILE_Y);
+    }
+    p->view_cells = p->view_off[n_views];
+    p->fused_cells = p->fused_off[n_aois];
+    p->d_views = L.views;
+    p->d_aois = L.aois;
+    p->d_item_start = L.item_start;
+    p->d_tile_start = L.tile_start;
+    p->d_counter = L.counter;
+    bool ok = cudaMemcpyAsync(L.views, p->h_views.data(), sizeof(MapViewDev) * n_views, cudaMemcpyHostToDevice, st) == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(L.aois, p->h_aois.data(), sizeof(AoiDev) * n_aois, cudaMemcpyHostToDevice, st) == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(L.item_start, p->item_start.data(), sizeof(long long) * (n_views + 1),
+                               cudaMemcpyHostToDevice, st) == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(L.tile_start, p->tile_start.data(), sizeof(long long) * (n_views + 1),
+                               cudaMemcpyHostToDevice, st) == cudaSuccess;
+    ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+    if (!ok) {
+        set_error("vs_aoi_batch_plan: descriptor upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+        return fail(VS_ERR_CUDA);
+    }
+    *plan = p;
+    return VS_OK;
+}
+
+extern "C" int vs_aoi_batch_query(const VsAoiBatch *plan, int64_t *view_cells, int64_t *fused_cells,
+                                  size_t *scratch_bytes) {
+    VS_REQUIRE(plan, "vs_aoi_batch_query: null plan");
+    if (view_cells) *view_cells = plan->view_cells;
+    if (fused_cells) *fused_cells = plan->fused_cells;
+    if (scratch_bytes) {
+        const size_t keys = sizeof(unsigned long long) * static_cast<size_t>(plan->view_cells);
+        const size_t fuse = vs_fuse_dsms_workspace_size(1, plan->max_fuse_cells);
+        *scratch_bytes = std::max(keys, fuse) + 256;
+    }
+    return VS_OK;
+}
+
+extern "C" int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int bin_blocks_per_sm,
+                                void *scratch, size_t scratch_bytes, float *view_dsm, void *stream) {
+    VS_REQUIRE(plan && scratch && view_dsm, "vs_aoi_batch_run: null pointer");
+    VS_REQUIRE(0 <= view_begin && view_begin < view_end && view_end <= plan->n_views && bin_blocks_per_sm > 0 &&
+                   bin_blocks_per_sm <= 64,
+               "vs_aoi_batch_run: bad view range [%d, %d) or blocks per SM %d", view_begin, view_end, bin_blocks_per_sm);
+    size_t need = 0;
+    vs_aoi_batch_query(plan, nullptr, nullptr, &need);
+    if (scratch_bytes < need) {
+        set_error("vs_aoi_batch_run: scratch %zu < %zu bytes", scratch_bytes, need);
+        return VS_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream);
+    unsigned long long *keys = static_cast<unsigned long long *>(scratch);
+    const long long c0 = plan->view_off[view_begin], c1 = plan->view_off[view_end];
+    if (cudaMemsetAsync(keys + c0, 0, sizeof(unsigned long long) * (c1 - c0), st) != cudaSuccess ||
+        cudaMemsetAsync(plan->d_counter, 0, sizeof(unsigned long long), st) != cudaSuccess) {
+        set_error("vs_aoi_batch_run: cudaMemsetAsync failed");
+        return VS_ERR_CUDA;
+    }
+    const long long i0 = plan->item_start[view_begin], i1 = plan->item_start[view_end];
+    if (i1 > i0) {
+        const long long blocks = std::min<long long>(i1 - i0, 1LL * sm_count() * bin_blocks_per_sm);
+        map_bin_kernel<<<static_cast<unsigned>(blocks), kMapThreads, 0, st>>>(
+            plan->d_views, plan->d_aois, plan->d_item_start, view_begin, view_end - 1, i0, i1, plan->rows_per_item, keys,
+            plan->d_counter);
+        VS_LAUNCH_CHECK("map_bin_kernel");
+    }
+    const long long t0 = plan->tile_start[view_begin], t1 = plan->tile_start[view_end];
+    const long long eblocks = std::min<long long>(t1 - t0, 1LL * sm_count() * 8);
+    map_epilogue_kernel<<<static_cast<unsigned>(eblocks), dim3(TX, TY), 0, st>>>(
+        plan->d_views, plan->d_aois, plan->d_tile_start, view_begin, view_end - 1, t0, t1, keys, view_dsm);
+    VS_LAUNCH_CHECK("map_epilogue_kernel");
+    return VS_OK;
+}
+
+extern "C" int vs_aoi_batch_fuse(const VsAoiBatch *plan, int aoi_begin, int aoi_end, const float *view_dsm,
+                                 float *fused, int median_blur, void *scratch, size_t scratch_bytes, void *stream) {
+    VS_REQUIRE(plan && view_dsm && fused && scratch, "vs_aoi_batch_fuse: null pointer");
+    VS_REQUIRE(0 <= aoi_begin && aoi_begin < aoi_end && aoi_end <= plan->n_aois, "vs_aoi_batch_fuse: bad AOI range");
+    for (int a = aoi_begin; a < aoi_end; ++a) {
+        const VsAoi &A = plan->aois[a];
+        const int s = vs_fuse_dsms(view_dsm + plan->view_off[A.first_view], VS_LAYOUT_VHW, A.n_views, A.ysize, A.xsize,
+                                   fused + plan->fused_off[a], median_blur, scratch, scratch_bytes, stream);
+        if (s != VS_OK) return s;
+    }
+    return VS_OK;
+}
+
+extern "C" void vs_aoi_batch_destroy(VsAoiBatch *plan) { delete plan; }

@@ -286,3 +286,133 @@ def aoi50_raster_case(seed: int = BASE_SEED, n_views: int = 50, image: int = 409
     scene = make_scene(seed + 11, grid, 300, 3.0, 80.0)
     views = make_views(seed + 12, scene, n_views, image, image, 0.10, 0.20, 0.5)
     return scene, views
+
+
+# --------------------------------------------------------------------------------------
+# Many AOIs with per-view height maps (the batched and served forms)
+# --------------------------------------------------------------------------------------
+MAP_FRAC_BITS = 28
+
+
+def map_affine(ce: float, cn: float, gsd: float, theta: float) -> dict:
+    """Fixed-point (2^-28 m) pixel -> UTM map of a W x H view: pixel centres on a grid of
+    spacing ``gsd`` rotated by ``theta`` about the image centre (ce, cn), rows running
+    south.  Pixel (i, j) lands at e0 + ej(2j+1-W) + ei(2i+1-H) (and likewise north)."""
+    s = float(1 << MAP_FRAC_BITS)
+    c, sn = math.cos(theta), math.sin(theta)
+    return {'e0': int(round(ce * s)), 'n0': int(round(cn * s)), 'ej': int(round(gsd * c / 2 * s)),
+            'ei': int(round(-gsd * sn / 2 * s)), 'nj': int(round(-gsd * sn / 2 * s)),
+            'ni': int(round(-gsd * c / 2 * s))}
+
+
+@dataclass
+class AoiSpec:
+    """One AOI of the batched workload: its DSM grid, views and image size."""
+    index: int
+    xoff: float
+    yoff: float
+    res: float
+    xsize: int
+    ysize: int
+    n_views: int
+    image: int
+    seed: int
+
+    def grid(self) -> DsmGrid:
+        return DsmGrid(self.xoff, self.yoff, self.res, self.res, self.xsize, self.ysize)
+
+    @property
+    def cells(self) -> int:
+        return self.xsize * self.ysize
+
+
+def make_aoi_set(n_aois: int = 200, seed: int = BASE_SEED, area_km2=(0.2, 4.0), views=(8, 60),
+                 image=(1024, 8192), res=(0.3, 1.0)) -> list:
+    """AOIs with footprint U(area_km2) km^2 (aspect U(0.75, 1.33)), grid resolution U(res)
+    m, U{views} views and square images of U{image} px.  Origins lie in UTM-like ranges
+    (easting 270-515 km, northing 4.2-8.38 Mm) that keep each grid inside one binade of
+    its origin."""
+    rng = np.random.default_rng(seed + 300)
+    specs = []
+    for a in range(n_aois):
+        area = rng.uniform(*area_km2) * 1e6
+        aspect = rng.uniform(0.75, 1.33)
+        w_m = math.sqrt(area * aspect)
+        h_m = area / w_m
+        r = float(rng.uniform(*res))
+        xsize, ysize = int(w_m / r) + 1, int(h_m / r) + 1
+        xoff = float(rng.uniform(270000.0, 515000.0 - xsize * r))
+        yoff = float(rng.uniform(4200000.0 + ysize * r, 8380000.0))
+        n_views = int(rng.integers(views[0], views[1] + 1))
+        img = int(rng.integers(image[0], image[1] + 1))
+        specs.append(AoiSpec(a, xoff, yoff, r, xsize, ysize, n_views, img, seed + 7919 * (a + 1)))
+    return specs
+
+
+def aoi_view_affines(spec: AoiSpec, width: int = None, height: int = None, jitter: float = 0.5) -> list:
+    """Per-view fixed-point affine maps whose footprint covers the AOI grid (6% margin),
+    with a small rotation and a corner jitter, as ``make_views`` does for one AOI."""
+    rng = np.random.default_rng(spec.seed)
+    W = width or spec.image
+    H = height or spec.image
+    gsd = 1.06 * max(spec.xsize * spec.res / W, spec.ysize * spec.res / H)
+    ce0 = spec.xoff + spec.xsize * spec.res / 2.0
+    cn0 = spec.yoff - spec.ysize * spec.res / 2.0
+    out = []
+    for _ in range(spec.n_views):
+        theta = float(rng.uniform(-0.03, 0.03))
+        ce = ce0 + float(rng.uniform(-jitter, jitter))
+        cn = cn0 + float(rng.uniform(-jitter, jitter))
+        out.append(map_affine(ce, cn, gsd, theta))
+    return out
+
+
+def height_map_pool(n_maps: int, size: int, seed: int = BASE_SEED, device='cpu', n_boxes: int = 300,
+                    h_lo: float = 3.0, h_hi: float = 80.0, noise: float = 0.3, nan_lo: float = 0.10,
+                    nan_hi: float = 0.20):
+    """(n_maps, size, size) float32 height maps as in the single-AOI workload: ground 0 m,
+    ``n_boxes`` boxes (sides 1.5-15% of the map) of height U(h_lo, h_hi), N(0, noise)
+    noise, and NaN on a U(nan_lo, nan_hi) fraction of the pixels."""
+    import torch
+    rng = np.random.default_rng(seed + 500)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed + 501)
+    pool = torch.zeros((n_maps, size, size), dtype=torch.float32, device=device)
+    for m in range(n_maps):
+        lo, hi = max(2, int(0.015 * size)), max(3, int(0.15 * size))
+        sides = rng.integers(lo, hi, size=(n_boxes, 2))
+        corners = rng.integers(0, size, size=(n_boxes, 2))
+        heights = rng.uniform(h_lo, h_hi, n_boxes)
+        for b in range(n_boxes):
+            i0, j0 = int(corners[b, 0]), int(corners[b, 1])
+            pool[m, i0:i0 + int(sides[b, 0]), j0:j0 + int(sides[b, 1])].clamp_(min=float(heights[b]))
+        pool[m] += torch.randn((size, size), generator=gen, device=device) * noise
+        frac = float(rng.uniform(nan_lo, nan_hi))
+        pool[m].masked_fill_(torch.rand((size, size), generator=gen, device=device) < frac, float('nan'))
+    return pool
+
+
+def small_aoi_case(seed: int = BASE_SEED):
+    """Three small AOIs (2-4 views each) for parity tests: per-view (H, W) float32 maps with
+    NaN, signed zeros and odd widths, and their grids and affine maps."""
+    rng = np.random.default_rng(seed + 900)
+    specs = [AoiSpec(0, 354052.25, 6182702.5, 0.5, 41, 33, 3, 0, seed + 1),
+             AoiSpec(1, 300001.0, 4300123.75, 0.3, 64, 64, 3, 0, seed + 2),
+             AoiSpec(2, 512000.5, 8200000.0, 1.0, 27, 50, 4, 0, seed + 3)]
+    maps, affines = [], []
+    for s in specs:
+        ms, afs = [], []
+        sizes = [(int(rng.integers(30, 70)), int(rng.integers(30, 70))) for _ in range(s.n_views)]
+        for v in range(s.n_views):
+            H, W = sizes[v]
+            m = (rng.normal(0.0, 0.3, (H, W)) + rng.choice([0.0, 10.0, 25.0], (H, W), p=[0.6, 0.3, 0.1]))
+            m = m.astype(np.float32)
+            m[rng.random((H, W)) < 0.15] = np.nan
+            zeros = rng.random((H, W)) < 0.03
+            m[zeros] = np.where(rng.random(zeros.sum()) < 0.5, np.float32(0.0), np.float32(-0.0))
+            ms.append(m)
+            sub = AoiSpec(s.index, s.xoff, s.yoff, s.res, s.xsize, s.ysize, 1, 0, s.seed + 31 * v)
+            afs.append(aoi_view_affines(sub, width=W, height=H)[0])
+        maps.append(ms)
+        affines.append(afs)
+    return specs, maps, affines
