@@ -285,6 +285,8 @@ def run_ours(args):
         del grid_t, dsms
         torch.cuda.empty_cache()
         result['precision_form'] = precision_form(wl.metas)
+        # ---- batched form (config: 200 uneven AOIs, waves, graph, autotuned work shapes)
+        result['batched_form'] = batched_form(steps=2, warmup=1)
         # ---- CPU baseline (oracle, bounded sample)
         result['cpu_baseline'] = cpu_baseline(wl, gargs, pool=False)
     if world > 1:
@@ -351,6 +353,110 @@ def precision_form(metas, n_points=16 << 20, steps=10, warmup=3, sample_stride=1
     res['hbm_peak_gbs'] = hbm_peak
     del out, xyz, ref_col, ref_row
     torch.cuda.empty_cache()
+    return res
+
+
+def batched_form(n_aois=200, pool_maps=32, budget_gb=96, steps=2, warmup=1, plain_views=24, with_fits=True,
+                 seed=None):
+    """200 AOIs of uneven size (footprint U(0.2,4) km^2, 8-60 views, U(1024,8192)^2 FP32
+    height maps, grid 0.3-1.0 m): per-view DSMs and per-AOI fusion for all of them, as
+    (i) the batched form (one binning and one epilogue launch per wave of AOIs, waves sized
+    to an HBM budget; work shapes from the autotuner), (ii) the same captured in one CUDA
+    graph, (iii) the same kernels launched per view, and (iv) the plain per-view GPU form
+    (the reference's structure: FP64 point list, proj_to_grid, blur, per view) on a sample
+    of views scaled by pixels.  Plus the per-AOI camera fits of all views."""
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.engine import AoiCameraFits, AoiSetEngine
+    from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3, proj_to_grid
+    seed = synth.BASE_SEED if seed is None else seed
+    specs = synth.make_aoi_set(n_aois, seed)
+    size = max(s.image for s in specs)
+    t0 = time.perf_counter()
+    pool = synth.height_map_pool(pool_maps, size, seed, 'cuda')
+    affines = [synth.aoi_view_affines(s) for s in specs]
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    eng = AoiSetEngine(specs, pool, affines, budget_bytes=int(budget_gb) << 30)
+    plan_s = time.perf_counter() - t0
+    tune = eng.autotune()
+    res = {'workload': f'{n_aois} AOIs: footprint U(0.2,4) km^2, 8-60 views, U(1024,8192)^2 FP32 height maps, '
+                       f'grid U(0.3,1.0) m; per-view DSM + fusion',
+           'aois': n_aois, 'views': eng.n_views, 'pixels': eng.pixels, 'cell_views': eng.cell_views,
+           'fused_cells': eng.cells, 'waves': len(eng.waves), 'hbm_budget_gb': budget_gb,
+           'map_pool': f'{pool_maps} maps of {size}^2 (view k reads map k mod {pool_maps})',
+           'setup_s': {'generate': round(gen_s, 2), 'plan': round(plan_s, 2)},
+           'autotune_ms': tune, 'chosen': {'rows_per_item': eng.rows_per_item,
+                                           'bin_blocks_per_sm': eng.bin_blocks_per_sm}}
+    modes = {}
+    for mode in ('batched', 'graph', 'per_view'):
+        for _ in range(warmup):
+            eng.step(mode)
+        t = eng.time_step(mode, reps=steps if mode != 'per_view' else 1)
+        modes[mode] = {'s_per_step': round(t, 4), 'pixels_per_s': eng.pixels / t,
+                       'dsm_cell_views_per_s': eng.cell_views / t, 'fused_cells_per_s': eng.cells / t}
+    res['modes'] = modes
+    # DRAM-level roofline of the batched step: 4 B per pixel read, 8 B key clear + 8 B key
+    # read + 4 B DSM write per cell-view, 4 B DSM read per cell-view in fusion, 8 B per
+    # fused cell (fusion output and blur)
+    algo = eng.pixels * 4 + eng.cell_views * (8 + 8 + 4 + 4) + eng.cells * 12
+    res['algorithmic_bytes_per_step'] = algo
+    res['achieved_gbs_batched'] = round(algo / modes['batched']['s_per_step'] / 1e9, 1)
+    # plain per-view GPU form on a sample of views, scaled by pixels
+    pix = 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    plain_t = 0.0
+    n_plain_views = 0
+    k = 0
+    for a, s in enumerate(specs):
+        if n_plain_views >= plain_views:
+            break
+        dsms = []
+        e0.record()
+        for v in range(s.n_views):
+            aff = affines[a][v]
+            m = pool[(k + v) % pool_maps][:s.image, :s.image]
+            dj = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[None, :]
+            di = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[:, None]
+            east = (aff['e0'] + aff['ej'] * dj + aff['ei'] * di).double() * 2.0 ** -28
+            north = (aff['n0'] + aff['nj'] * dj + aff['ni'] * di).double() * 2.0 ** -28
+            pts = torch.stack([east.reshape(-1), north.reshape(-1), m.reshape(-1).double()], dim=1)
+            d = proj_to_grid(pts, s.xoff, s.yoff, s.res, s.res, s.xsize, s.ysize)
+            dsms.append(median_blur3x3(d))
+            del pts, east, north
+        fuse_dsms(torch.stack(dsms), median_blur=True, layout='vhw')
+        e1.record()
+        torch.cuda.synchronize()
+        plain_t += e0.elapsed_time(e1) / 1e3
+        pix += s.n_views * s.image * s.image
+        n_plain_views += s.n_views
+        k += s.n_views
+        del dsms
+    est = plain_t * eng.pixels / pix
+    res['plain_per_view'] = {'sample': f'first {n_plain_views} views (AOIs 0..), scaled by pixels',
+                             'est_s_per_step': round(est, 3), 'pixels_per_s': eng.pixels / est}
+    res['speedup_batched_vs_plain'] = round(est / modes['batched']['s_per_step'], 2)
+    res['speedup_graph_vs_per_view_launches'] = round(modes['per_view']['s_per_step'] / modes['graph']['s_per_step'], 3)
+    eng.close()
+    del eng, pool
+    torch.cuda.empty_cache()
+    if with_fits:
+        metas = [synth.aoi_rpc_metas(s) for s in specs]
+        fits = AoiCameraFits(specs, metas)
+        fits.step()
+        torch.cuda.synchronize()
+        e0.record()
+        fits.step()
+        e1.record()
+        torch.cuda.synchronize()
+        ft = e0.elapsed_time(e1) / 1e3
+        res['camera_fits'] = {'views': sum(s.n_views for s in specs), 'grid': '200x200x20 per AOI (shared by its views)',
+                              's_per_step': round(ft, 4), 'rpc_pts_per_s': fits.points / ft,
+                              'status_ok': fits.status_ok()}
+        del fits
+        torch.cuda.empty_cache()
     return res
 
 
@@ -528,7 +634,15 @@ def main():
     ap.add_argument('--skip-extra', action='store_true', help='only the device-timed value')
     ap.add_argument('--precision-only', type=int, default=0, metavar='N',
                     help='run only the precision form on N points (0: off)')
+    ap.add_argument('--batched-only', type=int, default=0, metavar='AOIS',
+                    help='run only the batched multi-AOI form over AOIS AOIs (0: off)')
     args = ap.parse_args()
+    if args.batched_only:
+        from vissatsatellitestereo_gb300.build import build
+        build()
+        print(json.dumps({'batched_form': batched_form(n_aois=args.batched_only, steps=args.steps,
+                                                       warmup=args.warmup)}))
+        return
     if args.precision_only:
         from vissatsatellitestereo_gb300 import synth
         from vissatsatellitestereo_gb300.build import build

@@ -416,3 +416,56 @@ def small_aoi_case(seed: int = BASE_SEED):
         maps.append(ms)
         affines.append(afs)
     return specs, maps, affines
+
+
+def rpc_sample_grid_torch(meta: dict, n_xy: int, n_z: int, device='cpu') -> dict:
+    """``rpc_sample_grid`` on a torch device: flat FP64 tensors lat, lon, alt, x, y, z (the
+    same grid order and the same ENU formulas, in torch operations)."""
+    import torch
+    f64 = torch.float64
+    r = meta['rpc']
+    lat_pts = r['latOff'] + r['latScale'] * torch.linspace(1.0, -1.0, n_xy, dtype=f64, device=device)
+    lon_pts = r['lonOff'] + r['lonScale'] * torch.linspace(-1.0, 1.0, n_xy, dtype=f64, device=device)
+    alt_pts = r['altOff'] + r['altScale'] * torch.linspace(-1.0, 1.0, n_z, dtype=f64, device=device)
+    lat = lat_pts.repeat_interleave(n_xy).repeat(n_z)
+    lon = lon_pts.repeat(n_xy).repeat(n_z)
+    alt = alt_pts.repeat_interleave(n_xy * n_xy)
+    lat0 = float((lat_pts.min() + lat_pts.max()) / 2.0)
+    lon0 = float((lon_pts.min() + lon_pts.max()) / 2.0)
+    alt0 = float(alt_pts.min())
+
+    def ecef(la, lo, al):
+        phi, lam = torch.deg2rad(torch.as_tensor(la, dtype=f64, device=device)), \
+            torch.deg2rad(torch.as_tensor(lo, dtype=f64, device=device))
+        sphi = torch.sin(phi)
+        n = 6378137.0 / torch.sqrt(1.0 - _E2 * sphi * sphi)
+        return ((n + al) * torch.cos(phi) * torch.cos(lam), (n + al) * torch.cos(phi) * torch.sin(lam),
+                (n * (1.0 - _E2) + al) * sphi)
+
+    x, y, z = ecef(lat, lon, alt)
+    x0, y0, z0 = ecef(lat0, lon0, alt0)
+    dx, dy, dz = x - x0, y - y0, z - z0
+    phi0, lam0 = math.radians(lat0), math.radians(lon0)
+    sp, cp, sl, cl = math.sin(phi0), math.cos(phi0), math.sin(lam0), math.cos(lam0)
+    east = -sl * dx + cl * dy
+    t = cl * dx + sl * dy
+    north = -sp * t + cp * dz
+    up = cp * t + sp * dz
+    return {'lat': lat, 'lon': lon, 'alt': alt, 'x': east, 'y': north, 'z': up}
+
+
+_E2 = (1.0 / 298.257223563) * (2.0 - 1.0 / 298.257223563)
+
+
+def aoi_rpc_metas(spec: AoiSpec) -> list:
+    """Per-view RPC cameras of one AOI: independent seeded coefficients (as
+    ``make_rpc_meta``) around one shared normalisation (the AOI's lat/lon/alt offsets), so
+    every view sees the AOI's sample grid."""
+    base = make_rpc_meta(spec.seed, spec.image, spec.image)
+    out = []
+    for v in range(spec.n_views):
+        m = make_rpc_meta(spec.seed + 1 + v, spec.image, spec.image)
+        for k in ('latOff', 'latScale', 'lonOff', 'lonScale', 'altOff', 'altScale'):
+            m['rpc'][k] = base['rpc'][k]
+        out.append(m)
+    return out
