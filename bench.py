@@ -287,6 +287,8 @@ def run_ours(args):
         result['precision_form'] = precision_form(wl.metas)
         # ---- batched form (config: 200 uneven AOIs, waves, graph, autotuned work shapes)
         result['batched_form'] = batched_form(steps=2, warmup=1)
+        # ---- serving form (config: Poisson AOI fusion requests, resident state, 150 GB budget)
+        result['serving_form'] = serving_form(n_requests=args.serve)
         # ---- CPU baseline (oracle, bounded sample)
         result['cpu_baseline'] = cpu_baseline(wl, gargs, pool=False)
     if world > 1:
@@ -356,6 +358,87 @@ def precision_form(metas, n_points=16 << 20, steps=10, warmup=3, sample_stride=1
     return res
 
 
+def plain_aoi_seconds(spec, maps, affines):
+    """GPU time of the plain per-view form of one AOI (the reference's structure on the GPU):
+    per view the FP64 point list of its height map, proj_to_grid and the blur, one call
+    each, then the fusion."""
+    import torch
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3, proj_to_grid
+    s = spec
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dsms = []
+    e0.record()
+    for m, aff in zip(maps, affines):
+        m = m[:s.image, :s.image]
+        dj = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[None, :]
+        di = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[:, None]
+        east = (aff['e0'] + aff['ej'] * dj + aff['ei'] * di).double() * 2.0 ** -28
+        north = (aff['n0'] + aff['nj'] * dj + aff['ni'] * di).double() * 2.0 ** -28
+        pts = torch.stack([east.reshape(-1), north.reshape(-1), m.reshape(-1).double()], dim=1)
+        d = proj_to_grid(pts, s.xoff, s.yoff, s.res, s.res, s.xsize, s.ysize)
+        dsms.append(median_blur3x3(d))
+        del pts, east, north
+    fuse_dsms(torch.stack(dsms), median_blur=True, layout='vhw')
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def serving_form(n_requests=400, rate=20.0, n_aois=400, budget_gb=150, pool_maps=32, seed=None, plain_aois=3):
+    """A stream of AOI fusion requests (Poisson arrivals at `rate`/s, Zipf popularity over a
+    catalog of `n_aois` AOIs with config-3 size ranges drawn log-uniformly) served in real
+    time with HBM-resident camera sets and per-view DSMs under a `budget_gb` admission
+    budget and continuous batching.  The plain per-view GPU path has no resident state:
+    its latencies come from a FIFO model fed with its measured per-pixel GPU time."""
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.serve import (FusionServer, Request, fifo_latencies, pool_view_source,
+                                                    poisson_stream)
+    seed = synth.BASE_SEED if seed is None else seed
+    specs = synth.make_aoi_catalog(n_aois, seed)
+    size = max(s.image for s in specs)
+    pool = synth.height_map_pool(pool_maps, size, seed, 'cuda')
+    affines = [synth.aoi_view_affines(s) for s in specs]
+    metas = [synth.aoi_rpc_metas(s) for s in specs]
+    source = pool_view_source(specs, pool, affines)
+    # warm-up on a throw-away server (library setup, allocator growth)
+    warm = FusionServer(specs, source, metas, budget_bytes=int(budget_gb) << 30)
+    warm.run_stream([Request(0, 0, 0.0), Request(1, 1, 0.0)], realtime=False)
+    del warm
+    torch.cuda.synchronize()
+    srv = FusionServer(specs, source, metas, budget_bytes=int(budget_gb) << 30)
+    stream = poisson_stream(n_requests, rate, n_aois, seed)
+    stats = srv.run_stream(stream, realtime=True)
+    # plain per-view path: measured on a few AOIs, per-request service = pixels / rate + fuse
+    first = [0]
+    for s in specs:
+        first.append(first[-1] + s.n_views)
+    plain_t, plain_pix = 0.0, 0
+    for a in range(plain_aois):
+        maps = [pool[(first[a] + v) % pool_maps] for v in range(specs[a].n_views)]
+        plain_aoi_seconds(specs[a], maps, affines[a])          # warm
+        plain_t += plain_aoi_seconds(specs[a], maps, affines[a])
+        plain_pix += specs[a].n_views * specs[a].image ** 2
+    per_pixel = plain_t / plain_pix
+    service = [specs[r.aoi].n_views * specs[r.aoi].image ** 2 * per_pixel for r in stream]
+    lat = fifo_latencies([r.arrival for r in stream], service)
+    res = {'workload': f'{n_requests} AOI fusion requests, Poisson {rate}/s, Zipf(1.0) over {n_aois} AOIs '
+                       f'(config-3 ranges, log-uniform), {budget_gb} GB resident budget',
+           'served': stats,
+           'plain_per_view_model': {
+               'per_request_service_ms_mean': round(float(np.mean(service)) * 1e3, 2),
+               'utilisation_at_rate': round(float(np.sum(service) / stream[-1].arrival), 3),
+               'p50_latency_ms': round(float(np.percentile(lat, 50)) * 1e3, 1),
+               'p99_latency_ms': round(float(np.percentile(lat, 99)) * 1e3, 1),
+               'pixels_per_s': 1.0 / per_pixel,
+               'basis': f'FIFO queue of the same arrivals; service = measured plain per-view GPU time per pixel '
+                        f'({plain_aois} AOIs) x the AOI pixels (no resident state)'}}
+    del srv, pool
+    torch.cuda.empty_cache()
+    return res
+
+
 def batched_form(n_aois=200, pool_maps=32, budget_gb=96, steps=2, warmup=1, plain_views=24, with_fits=True,
                  seed=None):
     """200 AOIs of uneven size (footprint U(0.2,4) km^2, 8-60 views, U(1024,8192)^2 FP32
@@ -367,9 +450,7 @@ def batched_form(n_aois=200, pool_maps=32, budget_gb=96, steps=2, warmup=1, plai
     of views scaled by pixels.  Plus the per-AOI camera fits of all views."""
     import torch
     from vissatsatellitestereo_gb300 import synth
-    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
     from vissatsatellitestereo_gb300.engine import AoiCameraFits, AoiSetEngine
-    from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3, proj_to_grid
     seed = synth.BASE_SEED if seed is None else seed
     specs = synth.make_aoi_set(n_aois, seed)
     size = max(s.image for s in specs)
@@ -405,35 +486,15 @@ def batched_form(n_aois=200, pool_maps=32, budget_gb=96, steps=2, warmup=1, plai
     res['algorithmic_bytes_per_step'] = algo
     res['achieved_gbs_batched'] = round(algo / modes['batched']['s_per_step'] / 1e9, 1)
     # plain per-view GPU form on a sample of views, scaled by pixels
-    pix = 0
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    plain_t = 0.0
-    n_plain_views = 0
-    k = 0
+    pix, plain_t, n_plain_views, k = 0, 0.0, 0, 0
     for a, s in enumerate(specs):
         if n_plain_views >= plain_views:
             break
-        dsms = []
-        e0.record()
-        for v in range(s.n_views):
-            aff = affines[a][v]
-            m = pool[(k + v) % pool_maps][:s.image, :s.image]
-            dj = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[None, :]
-            di = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[:, None]
-            east = (aff['e0'] + aff['ej'] * dj + aff['ei'] * di).double() * 2.0 ** -28
-            north = (aff['n0'] + aff['nj'] * dj + aff['ni'] * di).double() * 2.0 ** -28
-            pts = torch.stack([east.reshape(-1), north.reshape(-1), m.reshape(-1).double()], dim=1)
-            d = proj_to_grid(pts, s.xoff, s.yoff, s.res, s.res, s.xsize, s.ysize)
-            dsms.append(median_blur3x3(d))
-            del pts, east, north
-        fuse_dsms(torch.stack(dsms), median_blur=True, layout='vhw')
-        e1.record()
-        torch.cuda.synchronize()
-        plain_t += e0.elapsed_time(e1) / 1e3
+        maps = [pool[(k + v) % pool_maps] for v in range(s.n_views)]
+        plain_t += plain_aoi_seconds(s, maps, affines[a])
         pix += s.n_views * s.image * s.image
         n_plain_views += s.n_views
         k += s.n_views
-        del dsms
     est = plain_t * eng.pixels / pix
     res['plain_per_view'] = {'sample': f'first {n_plain_views} views (AOIs 0..), scaled by pixels',
                              'est_s_per_step': round(est, 3), 'pixels_per_s': eng.pixels / est}
@@ -447,6 +508,7 @@ def batched_form(n_aois=200, pool_maps=32, budget_gb=96, steps=2, warmup=1, plai
         fits = AoiCameraFits(specs, metas)
         fits.step()
         torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         fits.step()
         e1.record()
@@ -636,7 +698,15 @@ def main():
                     help='run only the precision form on N points (0: off)')
     ap.add_argument('--batched-only', type=int, default=0, metavar='AOIS',
                     help='run only the batched multi-AOI form over AOIS AOIs (0: off)')
+    ap.add_argument('--serve', type=int, default=400, metavar='REQUESTS',
+                    help='requests of the serving form (Poisson 20/s; 2000 is the full stream)')
+    ap.add_argument('--serve-only', action='store_true', help='run only the serving form')
     args = ap.parse_args()
+    if args.serve_only:
+        from vissatsatellitestereo_gb300.build import build
+        build()
+        print(json.dumps({'serving_form': serving_form(n_requests=args.serve)}))
+        return
     if args.batched_only:
         from vissatsatellitestereo_gb300.build import build
         build()

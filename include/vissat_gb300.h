@@ -189,6 +189,8 @@ typedef struct VsMapView {
     int32_t aoi, reserved;
     int64_t e0, n0;                  /* fixed-point origin terms (|.| < 2^53) */
     int32_t ej, ei, nj, ni;          /* fixed-point half-pixel steps */
+    float *dsm;                      /* device output of this view's DSM; NULL: the run's
+                                        view_dsm buffer at the view's offset */
 } VsMapView;
 /* Opaque host-side plan: validated descriptors and per-AOI binning tables uploaded into the
  * plan workspace.  Planning synchronises `stream`; running does not, and launches kernels
@@ -205,7 +207,8 @@ int vs_aoi_batch_query(const VsAoiBatch *plan, int64_t *view_cells, int64_t *fus
 /* Rasterises views [view_begin, view_end) into their float32 DSMs: one persistent binning
  * launch over all their pixels (work items of rows_per_item map rows, taken from a
  * device-side counter by bin_blocks_per_sm CTAs per SM) and one epilogue launch over all
- * their 32x32 tiles (nanmax decode, hole fill, blur).  A single view is the per-view form. */
+ * their 32x32 tiles (nanmax decode, hole fill, blur).  A single view is the per-view form.
+ * view_dsm may be NULL when every view of the plan has its own `dsm` output. */
 int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int bin_blocks_per_sm,
                      void *scratch, size_t scratch_bytes, float *view_dsm, void *stream);
 /* Fuses AOIs [aoi_begin, aoi_end) from their views' DSMs (vs_fuse_dsms per AOI). */

@@ -1,0 +1,64 @@
+"""Serving form on the GPU: a request's fused DSM is the same alone and in a batch, after
+evictions, and equal to the oracle's (bit-exact)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import same_bits
+from oracle import maps as omaps
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def catalog():
+    from vissatsatellitestereo_gb300 import synth
+    specs, maps, affines = synth.small_aoi_case()
+    dev = [[torch.from_numpy(m).cuda() for m in ms] for ms in maps]
+
+    def views_of(a):
+        return [(h, h.shape[1], h.shape[0], aff) for h, aff in zip(dev[a], affines[a])]
+    ref = []
+    for s, ms, afs in zip(specs, maps, affines):
+        g = {'xoff': s.xoff, 'yoff': s.yoff, 'xres': s.res, 'yres': s.res, 'xsize': s.xsize, 'ysize': s.ysize}
+        ref.append(omaps.fused_dsm([omaps.view_dsm(m, a, g) for m, a in zip(ms, afs)]))
+    return specs, views_of, ref
+
+
+def serve(specs, views_of, aois, batched, budget=1 << 30):
+    from vissatsatellitestereo_gb300.serve import FusionServer, Request
+    srv = FusionServer(specs, views_of, budget_bytes=budget)
+    reqs = [Request(i, a, 0.0) for i, a in enumerate(aois)]
+    stats, outs = srv.run_stream(reqs, realtime=False, keep_outputs=True) if batched else (None, {})
+    if not batched:
+        for r in reqs:
+            outs[r.rid] = srv.process([r])[0]
+        torch.cuda.synchronize()
+    return srv, reqs, {k: v.cpu().numpy() for k, v in outs.items()}
+
+
+def test_alone_and_in_the_mix_are_identical_and_match_the_oracle(catalog):
+    specs, views_of, ref = catalog
+    aois = [0, 1, 2, 0, 2, 1, 1]
+    _, reqs_a, alone = serve(specs, views_of, aois, batched=False)
+    srv, reqs_b, mixed = serve(specs, views_of, aois, batched=True)
+    assert srv.batches == 1                       # every request arrived: one batch
+    for r in reqs_b:
+        assert same_bits(alone[r.rid], mixed[r.rid])
+        assert same_bits(mixed[r.rid], ref[r.aoi])
+    assert [r.hit for r in reqs_a] == [False, False, False, True, True, True, True]
+
+
+def test_eviction_and_recompute_give_the_same_bits(catalog):
+    from vissatsatellitestereo_gb300.serve import state_bytes
+    specs, views_of, ref = catalog
+    budget = max(state_bytes(s) for s in specs)    # room for one AOI at a time
+    srv, reqs, outs = serve(specs, views_of, [0, 1, 0, 2, 0], batched=False, budget=budget)
+    assert srv.store.evictions >= 2
+    seen, recomputed = set(), False
+    for r in reqs:                                 # an AOI served before was rebuilt after eviction
+        recomputed |= r.aoi in seen and not r.hit
+        seen.add(r.aoi)
+    assert recomputed
+    for r in reqs:
+        assert same_bits(outs[r.rid], ref[r.aoi])

@@ -32,7 +32,7 @@ class VsMapView(ctypes.Structure):
     _fields_ = [('heights', ctypes.c_void_p), ('row_stride', ctypes.c_int64), ('width', ctypes.c_int32),
                 ('height', ctypes.c_int32), ('aoi', ctypes.c_int32), ('reserved', ctypes.c_int32),
                 ('e0', ctypes.c_int64), ('n0', ctypes.c_int64), ('ej', ctypes.c_int32), ('ei', ctypes.c_int32),
-                ('nj', ctypes.c_int32), ('ni', ctypes.c_int32)]
+                ('nj', ctypes.c_int32), ('ni', ctypes.c_int32), ('dsm', ctypes.c_void_p)]
 
 
 @dataclass
@@ -73,6 +73,7 @@ class MapView:
     width: int
     height: int
     affine: MapAffine
+    dsm: torch.Tensor = None   # optional CUDA float32 (ysize, xsize) output of this view's DSM
 
 
 class AoiBatch:
@@ -106,9 +107,17 @@ class AoiBatch:
             if h.shape[0] < v.height or h.shape[1] < v.width:
                 raise ValueError('heights smaller than the view')
             self._keep.append(h)
+            out = 0
+            if v.dsm is not None:
+                g = self.grids[a]
+                if not (v.dsm.is_cuda and v.dsm.dtype == torch.float32 and v.dsm.is_contiguous() and
+                        v.dsm.numel() == g.xsize * g.ysize):
+                    raise ValueError('dsm must be a contiguous CUDA float32 tensor of the AOI grid size')
+                self._keep.append(v.dsm)
+                out = v.dsm.data_ptr()
             m = v.affine
             self.view_arr[i] = VsMapView(h.data_ptr(), h.stride(0), v.width, v.height, a, 0, m.e0, m.n0, m.ej, m.ei,
-                                         m.nj, m.ni)
+                                         m.nj, m.ni, out or None)
         lib = _lib.lib()
         nbytes = lib.vs_aoi_batch_plan_workspace_size(self.aoi_arr, n_aois, self.n_views)
         self._plan_ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device='cuda')
@@ -149,10 +158,11 @@ class AoiBatch:
         return torch.empty(self.scratch_bytes, dtype=torch.uint8, device='cuda')
 
     def run(self, view_dsm, scratch, views=None, bin_blocks_per_sm=4):
-        """Rasterise views[0]..views[1]-1 (all by default) into ``view_dsm``."""
+        """Rasterise views[0]..views[1]-1 (all by default) into ``view_dsm`` (views with
+        their own ``dsm`` output write there; ``view_dsm`` may then be None)."""
         v0, v1 = (0, self.n_views) if views is None else views
         _lib.call('vs_aoi_batch_run', self._plan, v0, v1, int(bin_blocks_per_sm), scratch.data_ptr(),
-                  scratch.numel(), view_dsm.data_ptr(), stream_handle())
+                  scratch.numel(), None if view_dsm is None else view_dsm.data_ptr(), stream_handle())
         return view_dsm
 
     def fuse(self, view_dsm, fused, scratch, aois=None, median_blur=True):

@@ -712,7 +712,8 @@ struct MapViewDev {
     int W, H;
     int aoi;
     int vec;                  // rows are 16-byte aligned: float4 loads
-    long long off;            // cell offset of the view's key grid / DSM
+    long long off;            // cell offset of the view's key grid (and default DSM slot)
+    float *out;               // the view's DSM, or null: the run's buffer at `off`
 };
 
 struct AoiDev {
@@ -857,7 +858,8 @@ __global__ void __launch_bounds__(TX *TY) map_epilogue_kernel(
         const int tiles_x = (W + TX - 1) / TX;
         const long long local = t - __ldg(tile_start + v);
         const int ty = static_cast<int>(local / tiles_x), tx = static_cast<int>(local - static_cast<long long>(ty) * tiles_x);
-        epilogue_tile(keys + mv.off, MapZeroDecoder{}, dsm + mv.off, nullptr, H, W, ty * TILE_Y, tx * TX, sm);
+        float *out = mv.out ? mv.out : dsm + mv.off;
+        epilogue_tile(keys + mv.off, MapZeroDecoder{}, out, nullptr, H, W, ty * TILE_Y, tx * TX, sm);
         __syncthreads();
     }
 }
@@ -992,6 +994,7 @@ struct VsAoiBatch {
     std::vector<VsAoi> aois;
     std::vector<long long> view_off, fused_off, item_start, tile_start;
     long long view_cells = 0, fused_cells = 0, max_fuse_cells = 0;
+    bool all_direct = true;                // every view has its own DSM output
     vs::MapViewDev *d_views = nullptr;
     vs::AoiDev *d_aois = nullptr;
     long long *d_item_start = nullptr, *d_tile_start = nullptr;
@@ -1170,6 +1173,8 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
         d.aoi = V.aoi;
         d.vec = ((reinterpret_cast<uintptr_t>(V.heights) & 15) == 0) && (V.row_stride % 4 == 0);
         d.off = p->view_off[v];
+        d.out = V.dsm;
+        if (!V.dsm) p->all_direct = false;
         const VsAoi &A = aois[V.aoi];
         const long long cells = A.xsize * A.ysize;
         p->view_off[v + 1] = p->view_off[v] + cells;
@@ -1213,7 +1218,7 @@ extern "C" int vs_aoi_batch_query(const VsAoiBatch *plan, int64_t *view_cells, i
 
 extern "C" int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int bin_blocks_per_sm,
                                 void *scratch, size_t scratch_bytes, float *view_dsm, void *stream) {
-    VS_REQUIRE(plan && scratch && view_dsm, "vs_aoi_batch_run: null pointer");
+    VS_REQUIRE(plan && scratch && (view_dsm || plan->all_direct), "vs_aoi_batch_run: null pointer");
     VS_REQUIRE(0 <= view_begin && view_begin < view_end && view_end <= plan->n_views && bin_blocks_per_sm > 0 &&
                    bin_blocks_per_sm <= 64,
                "vs_aoi_batch_run: bad view range [%d, %d) or blocks per SM %d", view_begin, view_end, bin_blocks_per_sm);

@@ -1,0 +1,262 @@
+"""Serving form: a stream of AOI fusion requests over HBM-resident AOI state.
+
+A request asks for the fused DSM of one AOI of a catalog (aggregate_2p5d.py:65-81 over
+the AOI's per-view DSMs of produce_dsm.py:46-58).  The server keeps, per AOI, its camera
+set (the perspective fits of camera_approx.py:150-204) and its partial DSMs (one float32
+DSM per view) resident in HBM under an admission budget, evicting the least recently used
+AOIs that the current batch does not need.  A request for a resident AOI costs one fusion;
+a miss first rasterises all of the AOI's views (one persistent binning launch and one
+epilogue launch for all misses of the batch, straight into the resident stacks) and fits
+its cameras.  Requests are batched continuously: every iteration takes all requests that
+have arrived (up to ``max_batch``), so a burst shares the rasterisation launches.  The
+result of a request does not depend on what it is batched with (every kernel writes only
+its own AOI's buffers).
+"""
+import collections
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .aggregate_2p5d import fuse_dsms
+from .batch import AoiBatch, AoiGrid, MapAffine, MapView
+
+
+@dataclass
+class Request:
+    rid: int
+    aoi: int
+    arrival: float            # seconds after the stream starts
+    done: float = None
+    hit: bool = None
+    batch: int = None
+
+
+def poisson_stream(n_requests, rate, n_aois, seed, zipf_s=1.0):
+    """Requests with exponential inter-arrival gaps (Poisson arrivals at ``rate`` per second)
+    over AOIs drawn with Zipf(``zipf_s``) popularity (a seeded permutation of the catalog)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, n_requests)
+    arrivals = np.cumsum(gaps)
+    ranks = np.arange(1, n_aois + 1, dtype=np.float64)
+    p = ranks ** -zipf_s
+    p /= p.sum()
+    order = rng.permutation(n_aois)
+    picks = order[rng.choice(n_aois, size=n_requests, p=p)]
+    return [Request(i, int(a), float(t)) for i, (a, t) in enumerate(zip(picks, arrivals))]
+
+
+class ResidentStore:
+    """Least-recently-used map AOI -> resident state under a byte budget (host bookkeeping;
+    the states hold device tensors, freed when evicted)."""
+
+    def __init__(self, budget_bytes):
+        self.budget = int(budget_bytes)
+        self.used = 0
+        self.items = collections.OrderedDict()      # aoi -> (state, nbytes)
+        self.hits = self.misses = self.evictions = 0
+
+    def get(self, aoi):
+        item = self.items.get(aoi)
+        if item is None:
+            return None
+        self.items.move_to_end(aoi)
+        return item[0]
+
+    def admit(self, nbytes, pinned=()):
+        """Evict least recently used AOIs outside ``pinned`` until ``nbytes`` more fit.
+        Returns the evicted AOIs; raises MemoryError when they cannot be made to fit."""
+        nbytes = int(nbytes)
+        if nbytes > self.budget:
+            raise MemoryError(f'AOI state of {nbytes} bytes exceeds the budget of {self.budget}')
+        evicted = []
+        for aoi in list(self.items):
+            if self.used + nbytes <= self.budget:
+                break
+            if aoi in pinned:
+                continue
+            _, b = self.items.pop(aoi)
+            self.used -= b
+            self.evictions += 1
+            evicted.append(aoi)
+        if self.used + nbytes > self.budget:
+            raise MemoryError('the AOIs pinned by the batch leave no room')
+        return evicted
+
+    def put(self, aoi, state, nbytes):
+        if aoi in self.items:
+            self.used -= self.items.pop(aoi)[1]
+        self.items[aoi] = (state, int(nbytes))
+        self.used += int(nbytes)
+
+    def __contains__(self, aoi):
+        return aoi in self.items
+
+
+def state_bytes(spec):
+    """Resident bytes of one AOI: a float32 DSM per view plus its camera parameters."""
+    return 4 * spec.cells * spec.n_views + 8 * 14 * spec.n_views
+
+
+def pool_view_source(specs, pool, affines):
+    """View source over a resident height-map pool: view k of AOI a reads pool map
+    (first view index of a + k) mod P, window [:image, :image]."""
+    first = np.concatenate([[0], np.cumsum([s.n_views for s in specs])]).tolist()
+    P = pool.shape[0]
+
+    def views_of(a):
+        s = specs[a]
+        return [(pool[(first[a] + v) % P], s.image, s.image, aff) for v, aff in enumerate(affines[a])]
+    return views_of
+
+
+class FusionServer:
+    def __init__(self, specs, view_source, metas=None, budget_bytes=150 << 30, max_batch=64, rows_per_item=32,
+                 bin_blocks_per_sm=8, scratch_cap_bytes=32 << 30, fit_grid=(200, 20)):
+        """specs: the AOI catalog (``synth.AoiSpec``: grid and view count); view_source(a):
+        the AOI's views as (CUDA float32 heights, width, height, fixed-point affine dict);
+        metas: per AOI the views' RPC meta_dicts (None: no camera fits)."""
+        self.specs = list(specs)
+        self.view_source = view_source
+        self.metas = metas
+        self.store = ResidentStore(budget_bytes)
+        self.max_batch = int(max_batch)
+        self.rows_per_item = rows_per_item
+        self.bin_blocks_per_sm = bin_blocks_per_sm
+        self.scratch_cap = int(scratch_cap_bytes)
+        self.fit_grid = fit_grid
+        self.scratch = torch.empty(0, dtype=torch.uint8, device='cuda')
+        self.pixels = 0               # height-map pixels rasterised
+        self.cell_views = 0           # per-view DSM cells produced
+        self.fused_cell_views = 0     # cell-views read by fusions
+        self.fit_points = 0
+        self.batches = 0
+
+    # ---- misses -----------------------------------------------------------------------
+    def _views(self, a, stack):
+        return [MapView(h, w, hh, MapAffine(**aff), dsm=stack[v])
+                for v, (h, w, hh, aff) in enumerate(self.view_source(a))]
+
+    def _rasterise(self, aois, stacks):
+        grids = [AoiGrid(self.specs[a].xoff, self.specs[a].yoff, self.specs[a].res, self.specs[a].res,
+                         self.specs[a].xsize, self.specs[a].ysize) for a in aois]
+        plan = AoiBatch(grids, [self._views(a, stacks[a]) for a in aois], rows_per_item=self.rows_per_item)
+        if self.scratch.numel() < plan.scratch_bytes:
+            self.scratch = torch.empty(plan.scratch_bytes, dtype=torch.uint8, device='cuda')
+        plan.run(None, self.scratch, bin_blocks_per_sm=self.bin_blocks_per_sm)
+        self.pixels += plan.pixels
+        self.cell_views += plan.view_cells
+        return plan
+
+    def _fit(self, a):
+        from . import synth
+        from .camera_approx import approx_perspective_enu
+        ms = self.metas[a]
+        g = synth.rpc_sample_grid_torch(ms[0], self.fit_grid[0], self.fit_grid[1], 'cuda')
+        params, err, status = approx_perspective_enu(ms, g['lat'], g['lon'], g['alt'], g['x'], g['y'], g['z'])
+        self.fit_points += len(ms) * g['lat'].numel()
+        return params, err, status
+
+    def _materialise(self, misses, pinned):
+        """Admit, rasterise and fit the missing AOIs (rasterisation batched in groups whose
+        key-grid scratch stays under the cap)."""
+        stacks, group, group_bytes, plans = {}, [], 0, []
+        for a in misses:
+            s = self.specs[a]
+            self.store.admit(state_bytes(s), pinned)
+            stack = torch.empty((s.n_views, s.ysize, s.xsize), dtype=torch.float32, device='cuda')
+            stacks[a] = stack
+            need = 8 * s.cells * s.n_views
+            if group and group_bytes + need > self.scratch_cap:
+                plans.append(self._rasterise(group, stacks))
+                group, group_bytes = [], 0
+            group.append(a)
+            group_bytes += need
+            cams = self._fit(a) if self.metas is not None else None
+            self.store.put(a, {'stack': stack, 'cameras': cams}, state_bytes(s))
+        if group:
+            plans.append(self._rasterise(group, stacks))
+        return plans
+
+    # ---- requests ---------------------------------------------------------------------
+    def process(self, batch):
+        """Serve one batch of requests; returns their fused DSMs (device tensors)."""
+        self.batches += 1
+        pinned = {r.aoi for r in batch}
+        misses = []
+        for r in batch:
+            hit = r.aoi in self.store and r.aoi not in misses
+            r.hit = hit
+            if hit:
+                self.store.hits += 1
+            else:
+                self.store.misses += 1
+                if r.aoi not in misses:
+                    misses.append(r.aoi)
+        plans = self._materialise(misses, pinned) if misses else []
+        outs = []
+        for r in batch:
+            st = self.store.get(r.aoi)
+            stack = st['stack']
+            outs.append(fuse_dsms(stack, median_blur=True, layout='vhw'))
+            self.fused_cell_views += stack.numel()
+        for p in plans:
+            p.close()
+        return outs
+
+    def run_stream(self, requests, realtime=True, keep_outputs=False, on_batch=None):
+        """Serve ``requests`` (sorted by arrival).  In real time, a request cannot be taken
+        before its arrival time; every iteration takes all arrived requests (up to
+        max_batch).  Returns the latency statistics."""
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        outputs = {}
+        t0 = time.perf_counter()
+        busy = 0.0
+        while pending:
+            now = time.perf_counter() - t0
+            if realtime and pending[0].arrival > now:
+                time.sleep(min(pending[0].arrival - now, 0.05))
+                continue
+            batch = []
+            while pending and len(batch) < self.max_batch and (not realtime or pending[0].arrival <= now):
+                batch.append(pending.popleft())
+            b0 = time.perf_counter()
+            outs = self.process(batch)
+            torch.cuda.synchronize()
+            b1 = time.perf_counter()
+            busy += b1 - b0
+            for r, o in zip(batch, outs):
+                r.done = b1 - t0
+                r.batch = self.batches
+                if keep_outputs:
+                    outputs[r.rid] = o
+            if on_batch:
+                on_batch(batch, outs)
+        wall = time.perf_counter() - t0
+        lat = np.array([r.done - r.arrival for r in requests])
+        hits = np.array([bool(r.hit) for r in requests])
+        stats = {
+            'requests': len(requests), 'wall_s': round(wall, 3), 'gpu_busy_s': round(busy, 3),
+            'p50_latency_ms': round(float(np.percentile(lat, 50)) * 1e3, 3),
+            'p99_latency_ms': round(float(np.percentile(lat, 99)) * 1e3, 3),
+            'mean_latency_ms': round(float(lat.mean()) * 1e3, 3),
+            'p50_hit_latency_ms': round(float(np.percentile(lat[hits], 50)) * 1e3, 3) if hits.any() else None,
+            'p99_miss_latency_ms': round(float(np.percentile(lat[~hits], 99)) * 1e3, 3) if (~hits).any() else None,
+            'hit_rate': round(float(hits.mean()), 4), 'evictions': self.store.evictions, 'batches': self.batches,
+            'resident_gb_end': round(self.store.used / 2 ** 30, 2),
+            'pixels_per_s_busy': self.pixels / busy if busy else None,
+            'dsm_cells_per_s_busy': self.cell_views / busy if busy else None,
+            'fused_cell_views_per_s_busy': self.fused_cell_views / busy if busy else None,
+            'rpc_fit_pts_per_s_busy': self.fit_points / busy if busy else None,
+        }
+        return (stats, outputs) if keep_outputs else stats
+
+
+def fifo_latencies(arrivals, service):
+    """Latencies of a single FIFO server with the given arrival and service times."""
+    t, out = 0.0, []
+    for a, s in zip(arrivals, service):
+        t = max(t, a) + s
+        out.append(t - a)
+    return np.array(out)

@@ -469,3 +469,28 @@ def aoi_rpc_metas(spec: AoiSpec) -> list:
             m['rpc'][k] = base['rpc'][k]
         out.append(m)
     return out
+
+
+def _loguniform(rng, lo, hi):
+    return float(math.exp(rng.uniform(math.log(lo), math.log(hi))))
+
+
+def make_aoi_catalog(n_aois: int = 400, seed: int = BASE_SEED, area_km2=(0.2, 4.0), views=(8, 60),
+                     image=(1024, 8192), res=(0.3, 1.0)) -> list:
+    """AOIs of the serving workload: the ranges of ``make_aoi_set`` drawn log-uniformly
+    (footprint, resolution, view count and image size)."""
+    rng = np.random.default_rng(seed + 700)
+    specs = []
+    for a in range(n_aois):
+        area = _loguniform(rng, *area_km2) * 1e6
+        aspect = rng.uniform(0.75, 1.33)
+        w_m = math.sqrt(area * aspect)
+        h_m = area / w_m
+        r = _loguniform(rng, *res)
+        xsize, ysize = int(w_m / r) + 1, int(h_m / r) + 1
+        xoff = float(rng.uniform(270000.0, 515000.0 - xsize * r))
+        yoff = float(rng.uniform(4200000.0 + ysize * r, 8380000.0))
+        n_views = int(round(_loguniform(rng, views[0], views[1])))
+        img = int(round(_loguniform(rng, image[0], image[1])))
+        specs.append(AoiSpec(a, xoff, yoff, r, xsize, ysize, n_views, img, seed + 104729 * (a + 1)))
+    return specs
