@@ -237,6 +237,37 @@ def test_dsm_from_points_batch_matches_oracle():
         assert same_bits(out[v], ref), v
 
 
+def test_dsm_from_points_overlap_matches_serial_and_oracle():
+    """Epilogues on a second stream overlapped with the next view's binning (rotating key
+    grids, alternating first-zero arrays): identical to the serial call and the oracle,
+    with signed zeros in the same cells of consecutive views."""
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    grid = synth.DsmGrid(synth.EXPLORER_UL_EASTING, synth.EXPLORER_UL_NORTHING, 0.3, 0.3, 200, 170)
+    scene = synth.make_scene(79, grid, 30, 3.0, 80.0)
+    views = synth.make_views(80, scene, 7, 260, 300, 0.1, 0.3, 0.5)
+    clouds = [synth.view_points(scene, v) for v in views]
+    for v, c in enumerate(clouds):
+        # a region of non-positive heights whose cell maxima are zeros: the sign of a
+        # cell's first zero alternates view by view
+        c[:6000, 2] = -np.abs(c[:6000, 2]) - 1.0
+        c[:6000:2, 2] = -0.0 if v % 2 else 0.0
+        c[1:6000:4, 2] = 0.0 if v % 2 else -0.0
+    clouds[3] = clouds[3][:-13]
+    offsets = np.cumsum([0] + [len(c) for c in clouds])
+    pts = np.concatenate(clouds)
+    args = (grid.xoff, grid.yoff, grid.xres, grid.yres, grid.xsize, grid.ysize)
+    side = torch.cuda.Stream()
+    over = dsm_from_points(pts, offsets, *args, epilogue_stream=side).cpu().numpy()
+    serial = dsm_from_points(pts, offsets, *args).cpu().numpy()
+    assert same_bits(over, serial)
+    for v, c in enumerate(clouds):
+        ref = blur.median_blur3x3(raster.proj_to_grid(c, *args).astype(np.float32))
+        assert same_bits(over[v], ref), v
+        assert (over[v] == 0).any()
+
+
 def test_median_blur_matches_oracle():
     from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3
     rng = np.random.default_rng(3)

@@ -32,16 +32,18 @@ def ptr(t):
 
 
 class Workspace:
-    """Grow-only scratch buffer per device (the library never allocates)."""
+    """Grow-only scratch buffer per device and stream (the library never allocates; calls
+    on different streams may run concurrently, so they never share scratch)."""
     _bufs = {}
 
     @classmethod
     def get(cls, nbytes):
         dev = torch.cuda.current_device()
-        buf = cls._bufs.get(dev)
+        key = (dev, torch.cuda.current_stream().cuda_stream)
+        buf = cls._bufs.get(key)
         if buf is None or buf.numel() < nbytes:
             buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=f'cuda:{dev}')
-            cls._bufs[dev] = buf
+            cls._bufs[key] = buf
         return buf
 
 

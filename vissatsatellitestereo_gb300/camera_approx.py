@@ -16,9 +16,14 @@ def approx_perspective_enu(meta_dicts, lat, lon, alt, xx, yy, zz, mode='fast', w
     """Per-view camera parameters [w, h, fx, fy, cx, cy, s, qw, qx, qy, qz, tx, ty, tz]
     (V, 14), error statistics (V, 6) (or None) and status (V,) as device tensors.
 
-    lat/lon/alt/xx/yy/zz: (N,) shared by all views (the reference's grid) or (V, N)."""
+    lat/lon/alt/xx/yy/zz: (N,) shared by all views (the reference's grid) or (V, N).
+    ``meta_dicts`` may also be the (V, 92) float64 CUDA camera tensor of
+    ``_lib.camera_array`` (no host-to-device copy per call)."""
     require_cuda()
-    cams = torch.from_numpy(_lib.camera_array(meta_dicts)).cuda()
+    if isinstance(meta_dicts, torch.Tensor):
+        cams = meta_dicts.to(device='cuda', dtype=torch.float64).contiguous()
+    else:
+        cams = torch.from_numpy(_lib.camera_array(meta_dicts)).cuda()
     V = cams.shape[0]
     la, lo, al, x, y, z = (as_device(a, torch.float64) for a in (lat, lon, alt, xx, yy, zz))
     n = la.shape[-1]

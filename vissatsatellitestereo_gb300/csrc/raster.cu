@@ -966,6 +966,118 @@ extern "C" int vs_dsm_from_points(const double *points, const int64_t *offsets, 
     return VS_OK;
 }
 
+// Overlapped form: view v's epilogue (issue-bound, L2-resident keys) runs on a second
+// stream while view v+1's points are binned (HBM-bound).  Three key grids rotate: bin(v)
+// fills K[v%3]; epilogue(v) reads K[v%3] and clears K[(v+2)%3] for bin(v+2), which waits
+// for it.  The "first zero" words alternate between two arrays (bin(v+1) posts to the one
+// epilogue(v) does not read); their epoch tags make stale words lose without clearing.
+namespace vs {
+namespace {
+struct OverlapWs {
+    unsigned long long *keys[3];
+    unsigned long long *first[2];
+    long long *row_thr, *col_thr;
+    size_t bytes;
+};
+
+OverlapWs carve_overlap(void *ws, long long xsize, long long ysize) {
+    Carver cv(ws);
+    OverlapWs r;
+    const size_t cells = static_cast<size_t>(xsize) * ysize;
+    for (auto &k : r.keys) k = cv.take<unsigned long long>(cells);
+    for (auto &f : r.first) f = cv.take<unsigned long long>(cells);
+    r.row_thr = cv.take<long long>(ysize + 1);
+    r.col_thr = cv.take<long long>(xsize + 1);
+    r.bytes = cv.used;
+    return r;
+}
+
+// Per-thread, per-device ring of ordering events (created once; no device memory).
+struct EventRing {
+    int device = -1;
+    cudaEvent_t bin[3] = {}, epi[3] = {};
+};
+
+int event_ring(EventRing *&out) {
+    static thread_local EventRing ring;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        set_error("cudaGetDevice failed");
+        return VS_ERR_CUDA;
+    }
+    if (ring.device != dev) {
+        for (int i = 0; i < 3; ++i) {
+            if (cudaEventCreateWithFlags(&ring.bin[i], cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&ring.epi[i], cudaEventDisableTiming) != cudaSuccess) {
+                set_error("cudaEventCreateWithFlags failed");
+                return VS_ERR_CUDA;
+            }
+        }
+        ring.device = dev;
+    }
+    out = &ring;
+    return VS_OK;
+}
+}  // namespace
+}  // namespace vs
+
+extern "C" size_t vs_dsm_from_points_overlap_workspace_size(int n_views, int64_t xsize, int64_t ysize) {
+    if (n_views <= 0 || xsize <= 0 || ysize <= 0) return 0;
+    return carve_overlap(nullptr, xsize, ysize).bytes + 256;
+}
+
+extern "C" int vs_dsm_from_points_overlap(const double *points, const int64_t *offsets, int n_views, double xoff,
+                                          double yoff, double xresolution, double yresolution, int64_t xsize,
+                                          int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
+                                          void *stream, void *epilogue_stream) {
+    VS_REQUIRE(n_views > 0 && n_views < (1 << 23) && grid_ok(xsize, ysize),
+               "vs_dsm_from_points_overlap: bad sizes views=%d grid=%lldx%lld", n_views, (long long)xsize,
+               (long long)ysize);
+    VS_REQUIRE(points && offsets && dsm && workspace, "vs_dsm_from_points_overlap: null pointer");
+    const size_t need = vs_dsm_from_points_overlap_workspace_size(n_views, xsize, ysize);
+    if (workspace_bytes < need) {
+        set_error("vs_dsm_from_points_overlap: workspace %zu < %zu bytes", workspace_bytes, need);
+        return VS_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream), es = as_stream(epilogue_stream);
+    EventRing *ev = nullptr;
+    int s = event_ring(ev);
+    if (s != VS_OK) return s;
+    OverlapWs w = carve_overlap(workspace, xsize, ysize);
+    RasterWs tw;                       // threshold tables only
+    tw.row_thr = w.row_thr;
+    tw.col_thr = w.col_thr;
+    Tables tb;
+    const long long cells = xsize * ysize;
+    s = make_tables(xoff, yoff, xresolution, yresolution, xsize, ysize, tw, tb, st);
+    for (int i = 0; i < 2 && s == VS_OK; ++i) s = clear(w.keys[i], sizeof(unsigned long long) * cells, st);
+    for (int i = 0; i < 2 && s == VS_OK; ++i) s = clear(w.first[i], sizeof(unsigned long long) * cells, st);
+    if (s != VS_OK) return s;
+    const long long launch_points = static_cast<long long>(sm_count()) * 8 * 256 * kPts;
+    const dim3 egrid(static_cast<unsigned>(ceil_div(xsize, TX)), static_cast<unsigned>(ceil_div(ysize, TILE_Y)));
+    auto cuda_ok = [](cudaError_t e) {
+        if (e == cudaSuccess) return true;
+        set_error("stream ordering failed: %s", cudaGetErrorString(e));
+        return false;
+    };
+    for (int v = 0; v < n_views; ++v) {
+        if (v >= 2 && !cuda_ok(cudaStreamWaitEvent(st, ev->epi[(v - 2) % 3], 0))) return VS_ERR_CUDA;
+        s = bin_launch(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, w.keys[v % 3],
+                       w.first[v & 1], st);
+        if (s != VS_OK) return s;
+        if (!cuda_ok(cudaEventRecord(ev->bin[v % 3], st)) || !cuda_ok(cudaStreamWaitEvent(es, ev->bin[v % 3], 0)))
+            return VS_ERR_CUDA;
+        unsigned long long *nxt = (v + 2 < n_views) ? w.keys[(v + 2) % 3] : nullptr;
+        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, es>>>(w.keys[v % 3], w.first[v & 1], points, dsm + v * cells, nxt,
+                                                            static_cast<int>(ysize), static_cast<int>(xsize));
+        VS_LAUNCH_CHECK("dsm_epilogue_kernel");
+        if (!cuda_ok(cudaEventRecord(ev->epi[v % 3], es))) return VS_ERR_CUDA;
+    }
+    // the caller's stream covers the last epilogues
+    if (!cuda_ok(cudaStreamWaitEvent(st, ev->epi[(n_views - 1) % 3], 0))) return VS_ERR_CUDA;
+    return VS_OK;
+}
+
 extern "C" int vs_median_blur3x3_f32(const float *in, float *out, int64_t h, int64_t w, int64_t n_img,
                                      void *stream) {
     VS_REQUIRE(h > 0 && w > 0 && n_img > 0 && in && out && in != out, "vs_median_blur3x3_f32: bad arguments");

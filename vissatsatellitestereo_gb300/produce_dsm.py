@@ -14,9 +14,14 @@ def grid_size(aoi_width, aoi_height, e_resolution=E_RESOLUTION, n_resolution=N_R
     return int(aoi_width / e_resolution) + 1, int(aoi_height / n_resolution) + 1
 
 
-def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize, ysize, out=None):
+def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize, ysize, out=None,
+                    epilogue_stream=None):
     """points: (total, 3) float64 (device tensor or array); offsets: (V+1,) int64 view
-    boundaries.  Returns (V, ysize, xsize) float32 device tensor."""
+    boundaries.  Returns (V, ysize, xsize) float32 device tensor.
+
+    ``epilogue_stream`` (a torch.cuda.Stream): run each view's decode / hole fill / blur
+    there, overlapped with the binning of the next view on the current stream (the
+    current stream still covers all the work when the call returns)."""
     require_cuda()
     pts = as_device(points, torch.float64)
     offs = as_device(offsets, torch.int64)
@@ -24,7 +29,12 @@ def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize
     xsize, ysize = int(xsize), int(ysize)
     if out is None:
         out = torch.empty((V, ysize, xsize), dtype=torch.float32, device='cuda')
-    wp, wb = workspace(_lib.lib().vs_dsm_from_points_workspace_size(V, xsize, ysize))
-    _lib.call('vs_dsm_from_points', ptr(pts), ptr(offs), V, float(xoff), float(yoff), float(xresolution),
-              float(yresolution), xsize, ysize, ptr(out), wp, wb, stream_handle())
+    args = (ptr(pts), ptr(offs), V, float(xoff), float(yoff), float(xresolution), float(yresolution), xsize, ysize,
+            ptr(out))
+    if epilogue_stream is None:
+        wp, wb = workspace(_lib.lib().vs_dsm_from_points_workspace_size(V, xsize, ysize))
+        _lib.call('vs_dsm_from_points', *args, wp, wb, stream_handle())
+    else:
+        wp, wb = workspace(_lib.lib().vs_dsm_from_points_overlap_workspace_size(V, xsize, ysize))
+        _lib.call('vs_dsm_from_points_overlap', *args, wp, wb, stream_handle(), epilogue_stream.cuda_stream)
     return out
