@@ -306,5 +306,11 @@ def test_fusion_matches_numpy(V):
         a[1, 1, :3] = np.inf
         a[2, 2, :] = np.float32(3e38)
         a[3, 3, :] = np.where(np.arange(V) % 2 == 0, np.float32(1e7), np.float32(-1e7 + 0.37))
-    ref = fuse.fuse_numpy(a)
+        a[4, 4, :] = np.inf                                   # infinite median
+        a[5, 5, :V // 2] = -np.inf                            # -inf below a finite median
+        a[6, 6, :] = np.float32(5.0) + np.float32(0.25) * (np.arange(V) % 5 - 2)   # tied deviations
+        a[7, 7, :] = np.where(np.arange(V) < (2 * V) // 3, np.inf, np.float32(1.5))  # +inf majority
+        a[8, 8, :] = np.where(np.arange(V) % 3 == 0, np.float32(-2.5), np.float32(7.25))
+    with np.errstate(invalid='ignore'):
+        ref = fuse.fuse_numpy(a)
     assert same_bits(fuse_dsms(a, median_blur=False), ref)

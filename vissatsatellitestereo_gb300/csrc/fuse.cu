@@ -12,8 +12,9 @@
 //
 // One thread owns one cell; the V values live in registers (V padded to a power of two,
 // template parameter) and are sorted with a bitonic network on order-preserving integer
-// keys (NaN -> all ones, so missing values sort last).  Views beyond 64 use a
-// local-memory path with the same arithmetic.
+// keys (NaN -> all ones, so missing values sort last); the MAD's deviations, taken in
+// sorted order, form a bitonic sequence and need only the merge half of the network.
+// Views beyond 64 use a local-memory path with the same arithmetic.
 #include <algorithm>
 #include <math.h>
 #include <mutex>
@@ -44,6 +45,23 @@ __device__ __forceinline__ void bitonic_sort(unsigned (&a)[N]) {
                     else { a[i] = hi; a[l] = lo; }
                 }
             }
+}
+
+// Sorts a bitonic sequence (a cyclic shift of non-decreasing then non-increasing, e.g.
+// non-increasing then non-decreasing) ascending: the merge half of the bitonic network.
+template <int N>
+__device__ __forceinline__ void bitonic_merge(unsigned (&a)[N]) {
+#pragma unroll
+    for (int j = N >> 1; j > 0; j >>= 1)
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const int l = i ^ j;
+            if (l > i) {
+                const unsigned lo = min(a[i], a[l]), hi = max(a[i], a[l]);
+                a[i] = lo;
+                a[l] = hi;
+            }
+        }
 }
 
 // select sorted[idx] with compile-time indexing (keeps the array in registers)
@@ -100,19 +118,33 @@ __device__ float fuse_cell(const float (&x)[N], int V) {
     if (n <= 2) return __int_as_float(0x7fffffff);
     bitonic_sort(k);
     const float med = median_of_sorted(pick(k, (n - 1) >> 1), pick(k, n >> 1));
-    // deviations |x - med| of the valid values; NaN deviations (inf - inf) are missing
+    // deviations |x - med| of the valid values; NaN deviations (inf - inf) are missing.
+    // With a finite median, the deviations of the sorted values are non-increasing up to
+    // the median and non-decreasing after it (fl(x - med) is monotone in x), and the missing
+    // slots sort last: a bitonic sequence, so one merge sorts it.
     unsigned dk[N];
     int nd = 0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        float d = (i < V && !isnan(x[i])) ? fabsf(__fsub_rn(x[i], med)) : __int_as_float(0x7fffffff);
-        dk[i] = fkey(d);
-        nd += (dk[i] != kMissing);
-    }
     float mad = __int_as_float(0x7fffffff);
-    if (nd > 0) {
-        bitonic_sort(dk);
+    if (isfinite(med)) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const float d = fabsf(__fsub_rn(float_from_key(k[i]), med));
+            dk[i] = (k[i] != kMissing) ? fkey(d) : kMissing;
+        }
+        nd = n;
+        bitonic_merge(dk);
         mad = median_of_sorted(pick(dk, (nd - 1) >> 1), pick(dk, nd >> 1));
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            float d = (i < V && !isnan(x[i])) ? fabsf(__fsub_rn(x[i], med)) : __int_as_float(0x7fffffff);
+            dk[i] = fkey(d);
+            nd += (dk[i] != kMissing);
+        }
+        if (nd > 0) {
+            bitonic_sort(dk);
+            mad = median_of_sorted(pick(dk, (nd - 1) >> 1), pick(dk, nd >> 1));
+        }
     }
     float kept[N];
     int cnt = 0;
