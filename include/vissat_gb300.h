@@ -95,6 +95,23 @@ size_t vs_rpc_project_cube_workspace_size(int n_cams);
 int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const float *xyz, int64_t n, float *colrow,
                         int variant, void *workspace, size_t workspace_bytes, void *stream);
 
+/* Replaces RPCModel.inverse_projection (lib/rpc_model.py:170-249) for n_cams cameras:
+ * (lon, lat) of image points (col, row) at altitudes alt, by the reference's iteration
+ * (start lon = lat = -1 in the normalised frame, finite-difference steps 2 then 0.1),
+ * repeated for all of a camera's points until every one reprojects within sqrt(1e-18)
+ * normalised units -- the same global iteration count, so bit-identical results.
+ * col/row/alt: device FP64; camera c reads its n points at col + c*point_stride.
+ * lon/lat: device FP64 [n_cams][n] (normalised when `normalized` != 0, as
+ * return_normalized=True); alt_out (nullable): the input altitudes, or the normalised ones.
+ * iterations (nullable, HOST int32 [n_cams]): the iteration counts.  The reference loops
+ * without a bound; here a camera exceeding max_iter fails with VS_ERR_DEGENERATE.  The
+ * call synchronises `stream` once per iteration (the host runs the global loop). */
+size_t vs_rpc_inverse_project_workspace_size(int n_cams, int64_t n);
+int vs_rpc_inverse_project(const VsRpcCamera *cams, int n_cams, const double *col, const double *row,
+                           const double *alt, int64_t n, int64_t point_stride, int normalized, double *lon,
+                           double *lat, double *alt_out, int max_iter, int32_t *iterations, void *workspace,
+                           size_t workspace_bytes, void *stream);
+
 /* ---- (b) perspective fit ------------------------------------------------------------ */
 
 /* Replaces solve_perspective (lib/solve_perspective.py:82-126) and its factorize

@@ -5,7 +5,8 @@ Run once in a container where the reference checkout is present:
     python tests/golden/make_golden.py [--ref /root/reference]
 
 It imports the reference modules that import cleanly (``lib/rpc_model.py``,
-``lib/solve_perspective.py``, ``lib/check_error.py``, ``lib/gen_grid.py``) and executes
+``lib/solve_perspective.py``, ``lib/check_error.py``, ``lib/gen_grid.py``,
+``lib/solve_affine.py``) and executes
 the reference's source for the two routines whose modules do not import:
 
 * ``lib/proj_to_grid.py`` -- needs ``numpy_groupies`` (absent) and ``np.int`` (removed
@@ -75,9 +76,43 @@ def fusion_block(ref):
     return compile(body, os.path.join(ref, 'aggregate_2p5d.py'), 'exec')
 
 
+def inverse_and_affine(ref, seed):
+    """(e) RPCModel.inverse_projection on 1-D inputs (the shape its np.vstack(...).T
+    expects) and (f) solve_affine on lat/lon/alt grids, as approx_affine_latlonalt calls it."""
+    from lib.rpc_model import RPCModel
+    from lib.solve_affine import solve_affine
+    inv = {}
+    for i, size in enumerate((2048, 4096, 8192)):
+        meta = synth.make_rpc_meta(seed + 600 + i, size, size)
+        r = meta['rpc']
+        rng = np.random.default_rng(seed + 610 + i)
+        n = 400
+        col = rng.uniform(0, size, n)
+        row = rng.uniform(0, size, n)
+        alt = r['altOff'] + r['altScale'] * rng.uniform(-1, 1, n)
+        lon, lat, _ = RPCModel(meta).inverse_projection(col, row, alt)
+        lon_n, lat_n, alt_n = RPCModel(meta).inverse_projection(col, row, alt, return_normalized=True)
+        inv[f'cam{i}'] = dict(meta=np.array(repr(meta)), col=col, row=row, alt=alt, lon=lon, lat=lat,
+                              lon_n=lon_n, lat_n=lat_n, alt_n=alt_n)
+    np.savez_compressed(os.path.join(HERE, 'rpc_inverse.npz'),
+                        **{f'{k}_{f}': v[f] for k, v in inv.items() for f in v})
+    aff = {}
+    for i, size in enumerate((2048, 4096)):
+        meta = synth.make_rpc_meta(seed + 700 + i, size, size)
+        g = synth.rpc_sample_grid(meta, 25, 6)
+        col, row = RPCModel(meta).projection(g.lat, g.lon, g.alt)
+        keep = (col >= 0) & (row >= 0) & (col < size) & (row < size)
+        P = solve_affine(g.lat, g.lon, g.alt, col, row, keep)
+        aff[f'cam{i}'] = dict(meta=np.array(repr(meta)), lat=g.lat, lon=g.lon, alt=g.alt, col=col, row=row,
+                              keep=keep, P=P)
+    np.savez_compressed(os.path.join(HERE, 'affine_fit.npz'),
+                        **{f'{k}_{f}': v[f] for k, v in aff.items() for f in v})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--sections', default='all', help="'all' or a comma list of: base, inverse")
     args = ap.parse_args()
     ref = os.path.abspath(args.ref)
     sys.path.insert(0, ref)
@@ -87,6 +122,12 @@ def main():
     from lib.gen_grid import gen_grid
 
     seed = synth.BASE_SEED
+    sections = {'base', 'inverse'} if args.sections == 'all' else set(args.sections.split(','))
+    if 'inverse' in sections:
+        inverse_and_affine(ref, seed)
+    if 'base' not in sections:
+        print('golden vectors written to', HERE)
+        return
 
     # (a) RPC projection: three cameras, grid points plus ragged extras (NaN, far away)
     rpc_cases = {}

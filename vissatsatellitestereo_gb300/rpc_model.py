@@ -8,6 +8,8 @@ are copied to the GPU and back; CUDA tensors stay on the device (results are ten
 ``mode='exact'`` (default) evaluates in FP64 in the reference's operation order and is
 bit-identical to it; ``mode='fast'`` uses the compensated FP32 form (< 1e-4 px).
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -65,6 +67,34 @@ class RPCModel(object):
             return col, row
         return col.cpu().numpy(), row.cpu().numpy()
 
+    def inverse_projection(self, col, row, alt, return_normalized=False):
+        """(lon, lat, alt) of image points at the given altitudes (lib/rpc_model.py:170-249),
+        bit-identical to the reference on 1-D inputs.  Arrays of one shape (the reference
+        needs 1-D; any shape works here, point by point).  With return_normalized the
+        normalised (lon, lat, alt) come back."""
+        require_cuda()
+        on_device = any(is_cuda_tensor(a) for a in (col, row, alt))
+        shape = tuple(torch.as_tensor(col).shape) if not isinstance(col, torch.Tensor) else tuple(col.shape)
+        c, r, a = (as_device(v, torch.float64).reshape(-1) for v in (col, row, alt))
+        n = c.numel()
+        lon = torch.empty(n, dtype=torch.float64, device='cuda')
+        lat = torch.empty(n, dtype=torch.float64, device='cuda')
+        alt_out = torch.empty(n, dtype=torch.float64, device='cuda')
+        its = (ctypes.c_int32 * 1)()
+        if n:
+            wp, wb = workspace(_lib.lib().vs_rpc_inverse_project_workspace_size(1, n))
+            _lib.call('vs_rpc_inverse_project', ptr(self._camera()), 1, ptr(c), ptr(r), ptr(a), n, 0,
+                      int(bool(return_normalized)), ptr(lon), ptr(lat), ptr(alt_out), 1000, its, wp, wb,
+                      stream_handle())
+        self.last_iterations = int(its[0])
+        outs = [t.reshape(shape) for t in (lon, lat, alt_out)]
+        if not return_normalized and not on_device:
+            outs[2] = alt
+        if on_device:
+            return tuple(outs)
+        return tuple(o if isinstance(o, np.ndarray) or not isinstance(o, torch.Tensor) else o.cpu().numpy()
+                     for o in outs)
+
 
 def project_cameras(meta_dicts, lat, lon, alt, mode='fast', shared=True, keep=False):
     """Batched projection: C cameras over one shared point set (shared=True, arrays of N)
@@ -118,3 +148,24 @@ def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
     _lib.call('vs_rpc_project_cube', ptr(cams), C, ptr(pts), n, ptr(out), CUBE_VARIANTS[variant], ws_ptr, ws_len,
               stream_handle())
     return out
+
+
+def inverse_project_cameras(meta_dicts, col, row, alt, shared=True, normalized=False, max_iter=1000):
+    """Batched inverse projection: C cameras over one point set (shared, arrays of N) or one
+    set per camera ((C, N) arrays).  Returns device tensors (lon, lat, alt) of shape (C, N)
+    and the per-camera iteration counts."""
+    require_cuda()
+    cams = meta_dicts if isinstance(meta_dicts, torch.Tensor) else torch.from_numpy(_lib.camera_array(meta_dicts))
+    cams = cams.to(device='cuda', dtype=torch.float64).contiguous()
+    C = cams.shape[0]
+    c, r, a = (as_device(v, torch.float64) for v in (col, row, alt))
+    n = c.shape[-1]
+    lon = torch.empty((C, n), dtype=torch.float64, device='cuda')
+    lat = torch.empty((C, n), dtype=torch.float64, device='cuda')
+    alt_out = torch.empty((C, n), dtype=torch.float64, device='cuda')
+    its = (ctypes.c_int32 * C)()
+    if n:
+        wp, wb = workspace(_lib.lib().vs_rpc_inverse_project_workspace_size(C, n))
+        _lib.call('vs_rpc_inverse_project', ptr(cams), C, ptr(c), ptr(r), ptr(a), n, 0 if shared else n,
+                  int(bool(normalized)), ptr(lon), ptr(lat), ptr(alt_out), int(max_iter), its, wp, wb, stream_handle())
+    return lon, lat, alt_out, [int(v) for v in its]
