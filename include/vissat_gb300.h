@@ -126,6 +126,27 @@ int vs_dlt_fit(const double *x, const double *y, const double *z, int64_t xyz_st
                double *K, double *R, double *t, int32_t *status, void *workspace,
                size_t workspace_bytes, void *stream);
 
+/* Replaces solve_affine (lib/solve_affine.py:37-72) for n_views independent problems: the
+ * least-squares affine camera [col; row] = P [x y z 1]^T over the kept points.  x/y/z:
+ * device FP64, view v at x + v*xyz_stride; col/row: device FP64 [n_views][n]; keep
+ * (nullable): device uint8 [n_views][n].  P: device FP64 [n_views][2][4] (row-major, the
+ * reference's reshape((2, 4))); status (nullable): VS_OK or VS_ERR_DEGENERATE (fewer than
+ * 4 kept points or a singular system; P is NaN).  FP64 normal equations in per-axis
+ * normalised coordinates: predictions agree with LAPACK's solution to well below 1e-6 px. */
+size_t vs_affine_fit_workspace_size(int n_views, int64_t n);
+int vs_affine_fit(const double *x, const double *y, const double *z, int64_t xyz_stride, const double *col,
+                  const double *row, const uint8_t *keep, int n_views, int64_t n, double *P, int32_t *status,
+                  void *workspace, size_t workspace_bytes, void *stream);
+
+/* Replaces the per-view loop of CameraApprox.approx_affine_latlonalt
+ * (camera_approx.py:112-137): FP64 projection of the lat/lon/alt grid through each RPC
+ * camera (as RPCModel.projection), in-image mask, affine fit with (x, y, z) = (lat, lon,
+ * alt).  params: device FP64 [n_views][10] = [width, height, P (8)]. */
+size_t vs_camera_approx_affine_workspace_size(int n_views, int64_t n);
+int vs_camera_approx_affine(const VsRpcCamera *cams, int n_views, const double *lat, const double *lon,
+                            const double *alt, int64_t n, int64_t point_stride, double *params, int32_t *status,
+                            void *workspace, size_t workspace_bytes, void *stream);
+
 /* Replaces check_perspective_error (lib/check_error.py:37-121): per view the
  * mean/median/max pixel reprojection error and mean/median/max inverse-projection error
  * of camera K[R|t] over the kept points.  err: device FP64 [n_views][6]. */

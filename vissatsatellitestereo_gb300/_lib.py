@@ -50,6 +50,10 @@ SIGNATURES = {
     'vs_rpc_inverse_project_workspace_size': (_sz, [_int, _i64]),
     'vs_rpc_inverse_project': (_int, [_vp, _int, _vp, _vp, _vp, _i64, _i64, _int, _vp, _vp, _vp, _int, _vp, _vp, _sz,
                                       _vp]),
+    'vs_affine_fit_workspace_size': (_sz, [_int, _i64]),
+    'vs_affine_fit': (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _int, _i64, _vp, _vp, _vp, _sz, _vp]),
+    'vs_camera_approx_affine_workspace_size': (_sz, [_int, _i64]),
+    'vs_camera_approx_affine': (_int, [_vp, _int, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _sz, _vp]),
     'vs_dlt_fit_workspace_size': (_sz, [_int, _i64]),
     'vs_dlt_fit': (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _int, _i64, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     'vs_perspective_error_workspace_size': (_sz, [_int, _i64]),
