@@ -109,10 +109,23 @@ def inverse_and_affine(ref, seed):
                         **{f'{k}_{f}': v[f] for k, v in aff.items() for f in v})
 
 
+def ply_files(ref, seed):
+    """(g) lib/ply_np_converter.np2ply binary outputs (its text mode raises with the vendored
+    plyfile): float32 without colour, float32 with colour and comments, float64."""
+    from lib.ply_np_converter import np2ply
+    rng = np.random.default_rng(seed + 800)
+    v = rng.normal(0.0, 100.0, (37, 3)) + np.array([354052.0, 6182702.0, 50.0])
+    c = rng.integers(0, 256, (37, 3)).astype(np.uint8)
+    np.savez_compressed(os.path.join(HERE, 'ply_inputs.npz'), vertex=v, color=c)
+    np2ply(v, os.path.join(HERE, 'ply_f32.ply'))
+    np2ply(v, os.path.join(HERE, 'ply_f32_color.ply'), color=c, comments=['VisSat point cloud', 'utm 17N'])
+    np2ply(v, os.path.join(HERE, 'ply_f64.ply'), use_double=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
-    ap.add_argument('--sections', default='all', help="'all' or a comma list of: base, inverse")
+    ap.add_argument('--sections', default='all', help="'all' or a comma list of: base, inverse, formats")
     args = ap.parse_args()
     ref = os.path.abspath(args.ref)
     sys.path.insert(0, ref)
@@ -122,9 +135,11 @@ def main():
     from lib.gen_grid import gen_grid
 
     seed = synth.BASE_SEED
-    sections = {'base', 'inverse'} if args.sections == 'all' else set(args.sections.split(','))
+    sections = {'base', 'inverse', 'formats'} if args.sections == 'all' else set(args.sections.split(','))
     if 'inverse' in sections:
         inverse_and_affine(ref, seed)
+    if 'formats' in sections:
+        ply_files(ref, seed)
     if 'base' not in sections:
         print('golden vectors written to', HERE)
         return
