@@ -123,9 +123,11 @@ class ClockSampler:
 # our arm
 # ------------------------------------------------------------------------------------
 def launches_per_step(views):
-    camera = 1 + 1 + 1 + 1 + 1 + 1 + 1 + 1 + 4 * 2 + 1      # bbox init/bbox/norm/project+moments/solve/wh/err/sel-init/4x(hist,step)/final
-    raster = 2 + views * 4                                   # thresholds x2, per view: bin, zero init, zero first, epilogue
-    fusion = 2                                               # fuse + blur
+    # kernels only (memsets are not kernels); checked against the ncu launch list
+    camera = 15        # bbox init, bbox, norm, prepare, project, moments, solve, error points, error count,
+    #                    select step x3, select histogram x2, error final
+    raster = 2 + views * 2   # thresholds x2; per view: bin, epilogue
+    fusion = 2               # fuse + blur
     return camera + raster + fusion
 
 

@@ -256,50 +256,79 @@ __global__ void __launch_bounds__(kMomThreads) moments_kernel(
     for (int k = 0; k < kMom; ++k) m[k] = 0.0f;
     float count = 0.0f;
     const long long base = static_cast<long long>(blockIdx.x) * kMomThreads * kChunk + threadIdx.x;
+    // groups of kAhead points: all loads of a group are issued before its arithmetic
+    constexpr int kAhead = 4;
 #pragma unroll 1
-    for (int j = 0; j < kChunk; ++j) {
-        const long long i = base + static_cast<long long>(j) * kMomThreads;
-        if (i >= n) break;
-        df c, r;
-        if (colrow) {
-            const float4 cr = colrow[static_cast<long long>(v) * n + i];
-            c = {cr.x, cr.y};
-            r = {cr.z, cr.w};
-            if (!(df_ge0(c) && df_ge0(r) && df_lt(c, w) && df_lt(r, h))) continue;
-        } else {
-            if (keep && !keep[v * n + i]) continue;
-            c = split_double(col[v * n + i]);
-            r = split_double(row[v * n + i]);
+    for (int j0 = 0; j0 < kChunk; j0 += kAhead) {
+        double X[kAhead], Y[kAhead], Z[kAhead];
+        df c[kAhead], r[kAhead];
+        bool ok[kAhead];
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            const long long i = base + static_cast<long long>(j0 + u) * kMomThreads;
+            ok[u] = i < n;
+            X[u] = Y[u] = Z[u] = 0.0;
+            c[u] = r[u] = df{0.0f, 0.0f};
+            if (ok[u]) {
+                X[u] = xv[i];
+                Y[u] = yv[i];
+                Z[u] = zv[i];
+                if (colrow) {
+                    const float4 cr = colrow[static_cast<long long>(v) * n + i];
+                    c[u] = {cr.x, cr.y};
+                    r[u] = {cr.z, cr.w};
+                    ok[u] = df_ge0(c[u]) && df_ge0(r[u]) && df_lt(c[u], w) && df_lt(r[u], h);
+                } else {
+                    ok[u] = !keep || keep[v * n + i];
+                    c[u] = split_double(col[v * n + i]);
+                    r[u] = split_double(row[v * n + i]);
+                }
+            }
         }
-        float px, py, pz, pc, pr;
-        normalised_point(nf, xv[i], yv[i], zv[i], c, r, px, py, pz, pc, pr);
-        add_moments(m, px, py, pz, pc, pr);
-        count += 1.0f;
+#pragma unroll
+        for (int u = 0; u < kAhead; ++u) {
+            if (!ok[u]) continue;
+            float px, py, pz, pc, pr;
+            normalised_point(nf, X[u], Y[u], Z[u], c[u], r[u], px, py, pz, pc, pr);
+            add_moments(m, px, py, pz, pc, pr);
+            count += 1.0f;
+        }
     }
     store_block_moments(m, count, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kSlots, red);
+}
+
+// Double-float form of every view's camera, prepared once per call (one thread per view)
+// rather than by the first thread of every projection block.
+__global__ void prepare_views_kernel(const VsRpcCamera *__restrict__ cams, int n_views, RpcFast *__restrict__ fast,
+                                     float *__restrict__ wh) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_views) return;
+    RpcFast f;
+    prepare_fast(cams[v], f);
+    fast[v] = f;
+    wh[2 * v] = f.width;
+    wh[2 * v + 1] = f.height;
 }
 
 // Projection pass of the fused camera path: (col, row) of every grid point through view
 // v's RPC camera as double-floats.
 template <int MODE>
 __global__ void __launch_bounds__(256) project_view_kernel(const VsRpcCamera *__restrict__ cams,
+                                                           const RpcFast *__restrict__ fasts,
                                                            const double *__restrict__ lat,
                                                            const double *__restrict__ lon,
                                                            const double *__restrict__ alt, long long n,
-                                                           long long stride, float4 *__restrict__ colrow,
-                                                           float *__restrict__ wh) {
+                                                           long long stride, float4 *__restrict__ colrow) {
     __shared__ VsRpcCamera cam;
     __shared__ RpcFast fast;
     const int v = blockIdx.y;
     {
-        const double *src = reinterpret_cast<const double *>(cams + v);
-        double *dst = reinterpret_cast<double *>(&cam);
-        for (int i = threadIdx.x; i < static_cast<int>(sizeof(VsRpcCamera) / 8); i += blockDim.x) dst[i] = src[i];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        prepare_fast(cam, fast);
-        if (blockIdx.x == 0) wh[2 * v] = fast.width, wh[2 * v + 1] = fast.height;
+        const unsigned *src = MODE == VS_PROJ_EXACT ? reinterpret_cast<const unsigned *>(cams + v)
+                                                    : reinterpret_cast<const unsigned *>(fasts + v);
+        unsigned *dst = MODE == VS_PROJ_EXACT ? reinterpret_cast<unsigned *>(&cam) : reinterpret_cast<unsigned *>(&fast);
+        const int words = MODE == VS_PROJ_EXACT ? static_cast<int>(sizeof(VsRpcCamera) / 4)
+                                                : static_cast<int>(sizeof(RpcFast) / 4);
+        for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
     const long long off = v * stride;
@@ -656,7 +685,7 @@ __device__ __forceinline__ df dot2(const df *q, float x, float y, float z) {
 //    its own projection, cam = h2 K^-1 [c^ r^ 1], so the distance is
 //    |h2| |delta x d| / |d| with delta = K^-1 [c^ - c, r^ - r, 0]: the pixel residual
 //    enters directly and nothing of the camera's ~1e5-1e6 m depth cancels.
-__global__ void __launch_bounds__(kErrThreads) error_points_kernel(
+__global__ void __launch_bounds__(kErrThreads, 3) error_points_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
     const double *__restrict__ col, const double *__restrict__ row, const float4 *__restrict__ colrow,
     const uint8_t *__restrict__ keep, long long n, const ErrCam *__restrict__ cams, ErrWs w) {
@@ -939,6 +968,7 @@ struct FitWs {
     ErrCam *errcam;
     float4 *colrow;
     float *wh;
+    RpcFast *fast;
 };
 
 FitWs carve_fit(Carver &cv, int V, long long n, bool fused) {
@@ -949,6 +979,7 @@ FitWs carve_fit(Carver &cv, int V, long long n, bool fused) {
     f.errcam = cv.take<ErrCam>(V);
     f.colrow = fused ? cv.take<float4>(static_cast<size_t>(V) * n) : nullptr;
     f.wh = cv.take<float>(2 * static_cast<size_t>(V));
+    f.fast = fused ? cv.take<RpcFast>(V) : nullptr;
     return f;
 }
 
@@ -1089,14 +1120,16 @@ extern "C" int vs_camera_approx_perspective(const VsRpcCamera *cams, int n_views
     int s = launch_norm(x, y, z, point_stride, nullptr, nullptr, nullptr, cams, n_views, n, f, st);
     if (s != VS_OK) return s;
     const int blocks = mom_blocks(n);
+    prepare_views_kernel<<<static_cast<unsigned>(ceil_div(n_views, 64)), 64, 0, st>>>(cams, n_views, f.fast, f.wh);
+    VS_LAUNCH_CHECK("prepare_views_kernel");
     if (n > 0) {
         const unsigned pg = static_cast<unsigned>(std::min<long long>(ceil_div(n, 256), sm_count() * 8LL / n_views + 8));
         if (proj_mode == VS_PROJ_EXACT)
-            project_view_kernel<VS_PROJ_EXACT><<<dim3(pg, n_views), 256, 0, st>>>(cams, lat, lon, alt, n,
-                                                                                  point_stride, f.colrow, f.wh);
+            project_view_kernel<VS_PROJ_EXACT><<<dim3(pg, n_views), 256, 0, st>>>(cams, f.fast, lat, lon, alt, n,
+                                                                                  point_stride, f.colrow);
         else
-            project_view_kernel<VS_PROJ_FAST><<<dim3(pg, n_views), 256, 0, st>>>(cams, lat, lon, alt, n,
-                                                                                 point_stride, f.colrow, f.wh);
+            project_view_kernel<VS_PROJ_FAST><<<dim3(pg, n_views), 256, 0, st>>>(cams, f.fast, lat, lon, alt, n,
+                                                                                 point_stride, f.colrow);
         VS_LAUNCH_CHECK("project_view_kernel");
     }
     moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, point_stride, nullptr, nullptr, f.colrow,
