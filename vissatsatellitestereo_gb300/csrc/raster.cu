@@ -841,17 +841,21 @@ __global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
     }
 }
 
-// Persistent epilogue over the 32x32 tiles of many views: tiles [tile_begin, tile_end).
+// Persistent epilogue over the 32x32 tiles of many views: tiles [tile_begin, tile_end),
+// grid-strided so that the blocks sweep the key grids in order (L2 locality of the
+// halos).  Tile indices only grow, so every thread follows the view index with a forward
+// walk (one search at the start) and needs no barrier for it.
 __global__ void __launch_bounds__(TX *TY) map_epilogue_kernel(
     const MapViewDev *__restrict__ views, const AoiDev *__restrict__ aois, const long long *__restrict__ tile_start,
     int v_lo, int v_hi, long long tile_begin, long long tile_end, const unsigned long long *__restrict__ keys,
     float *__restrict__ dsm) {
     __shared__ EpilogueSmem sm;
-    __shared__ int s_view;
-    for (long long t = tile_begin + blockIdx.x; t < tile_end; t += gridDim.x) {
-        if (threadIdx.x == 0 && threadIdx.y == 0) s_view = find_range(tile_start, v_lo, v_hi, t);
-        __syncthreads();
-        const int v = s_view;
+    const long long t0 = tile_begin + blockIdx.x;
+    if (t0 >= tile_end) return;
+    int v = find_range(tile_start, v_lo, v_hi, t0);
+    long long next = __ldg(tile_start + v + 1);
+    for (long long t = t0; t < tile_end; t += gridDim.x) {
+        while (t >= next) next = __ldg(tile_start + (++v) + 1);
         const MapViewDev &mv = views[v];
         const AoiDev &ad = aois[mv.aoi];
         const int W = ad.xsize, H = ad.ysize;
