@@ -232,6 +232,21 @@ __device__ __forceinline__ bool axis_fast(const FastAxis &a, long long bv, int &
     return ok;
 }
 
+// axis_fast from the difference d itself.  For a contained grid the origin-binade test is
+// implied: d is monotone in the coordinate, and every coordinate outside the origin's
+// binade lies at least two cells outside [0, tmax).
+__device__ __forceinline__ bool axis_from_d(const FastAxis &a, long long d, int &r, bool &sure) {
+    const bool ok = (d >= 0) & (d < a.tmax);
+    const unsigned u = static_cast<unsigned>(static_cast<unsigned long long>(d) >> a.shift);
+    const float q = __fmul_rn(__uint2float_rn(u), a.scale);
+    const float big = __fadd_rn(q, 12582912.0f);
+    const float fr = __fsub_rn(q, __fsub_rn(big, 12582912.0f));
+    const int rn = static_cast<int>(static_cast<unsigned>(__float_as_int(big)) - 0x4b400000u);
+    r = min(max(rn - (fr < 0.0f ? 1 : 0), 0), a.nm1);
+    sure = fabsf(fr) > __fmaf_rn(a.err_rel, q, a.err_abs);
+    return ok;
+}
+
 __device__ __noinline__ int axis_correct(const long long *thr, int r, long long d) {
     for (int it = 0; it < 8 && __ldg(thr + r) > d; ++it) --r;
     for (int it = 0; it < 8 && __ldg(thr + r + 1) <= d; ++it) ++r;
@@ -714,6 +729,10 @@ struct MapViewDev {
     int vec;                  // rows are 16-byte aligned: float4 loads
     long long off;            // cell offset of the view's key grid (and default DSM slot)
     float *out;               // the view's DSM, or null: the run's buffer at `off`
+    // the axes' differences from the grid origin (in ulps of the origin's binade) are
+    // affine in the pixel indices: d = d0 + d_di * (2i+1-H) + d_dj * (2j+1-W)
+    long long dc0, dc_di, dc_dj;   // columns: bits(x) - bits(xoff)
+    long long dr0, dr_di, dr_dj;   // rows:    bits(yoff) - bits(y)
 };
 
 struct AoiDev {
@@ -782,8 +801,6 @@ __global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
         const MapViewDev mv = views[v];
         const AoiDev &ad = aois[mv.aoi];
         const FastAxis R = ad.row, C = ad.col;
-        const long long bx = ad.bx, by = ad.by;
-        const int shx = ad.shx, shy = ad.shy;
         const unsigned long long ncols = static_cast<unsigned>(ad.xsize);
         unsigned long long *vk = keys + mv.off;
         const int i0 = static_cast<int>(it - __ldg(item_start + v)) * rows_per_item;
@@ -803,24 +820,21 @@ __global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
 #pragma unroll
                 for (int k = 0; k < 4; ++k) hb[k] = j0 + k < mv.W ? __float_as_uint(__ldcs(row + j0 + k)) : 0x7fc00000u;
             }
-            const int di2 = 2 * i + 1 - mv.H;
-            const long long rx = mv.e0 + static_cast<long long>(mv.ei) * di2;
-            const long long ry = mv.n0 + static_cast<long long>(mv.ni) * di2;
+            const int di2 = 2 * i + 1 - mv.H, dj0 = 2 * j0 + 1 - mv.W;
+            long long dcol = mv.dc0 + mv.dc_di * di2 + mv.dc_dj * dj0;
+            long long drow = mv.dr0 + mv.dr_di * di2 + mv.dr_dj * dj0;
+            const long long scol = 2 * mv.dc_dj, srow = 2 * mv.dr_dj;   // per pixel along the row
             long long cell[4];
             unsigned long long key[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int dj2 = 2 * (j0 + k) + 1 - mv.W;
-                const long long xf = rx + static_cast<long long>(mv.ej) * dj2;
-                const long long yf = ry + static_cast<long long>(mv.nj) * dj2;
+            for (int k = 0; k < 4; ++k, dcol += scol, drow += srow) {
                 int r, c;
-                long long dr, dc;
                 bool sr, sc;
-                bool ok = axis_fast<true>(R, by + (yf << shy), r, dr, sr);
-                ok &= axis_fast<false>(C, bx + (xf << shx), c, dc, sc);
+                bool ok = axis_from_d(R, drow, r, sr);
+                ok &= axis_from_d(C, dcol, c, sc);
                 ok &= (hb[k] & 0x7fffffffu) <= 0x7f800000u;     // not NaN
-                if (ok && !sr) r = axis_correct(R.thr, r, dr);
-                if (ok && !sc) c = axis_correct(C.thr, c, dc);
+                if (ok && !sr) r = axis_correct(R.thr, r, drow);
+                if (ok && !sc) c = axis_correct(C.thr, c, dcol);
                 const long long cl = static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(r)) * ncols) + c;
                 const unsigned long long idx = static_cast<unsigned long long>(i) * static_cast<unsigned>(mv.W) + (j0 + k);
                 key[k] = ok ? map_key(hb[k], idx) : kEmptyKey;
@@ -1290,6 +1304,17 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
         d.vec = ((reinterpret_cast<uintptr_t>(V.heights) & 15) == 0) && (V.row_stride % 4 == 0);
         d.off = p->view_off[v];
         d.out = V.dsm;
+        // d = bits(x) - bits(xoff) = (bx - bits(xoff)) + (x_fx << shx), x_fx affine in the
+        // pixel indices (the shifts are exact: the plan checked |x_fx| << sh < 2^62)
+        {
+            const long long cb = ad.bx - ad.col.off_bits, rb = ad.row.off_bits - ad.by;
+            d.dc0 = cb + (V.e0 << ad.shx);
+            d.dc_di = static_cast<long long>(V.ei) << ad.shx;
+            d.dc_dj = static_cast<long long>(V.ej) << ad.shx;
+            d.dr0 = rb - (V.n0 << ad.shy);
+            d.dr_di = -(static_cast<long long>(V.ni) << ad.shy);
+            d.dr_dj = -(static_cast<long long>(V.nj) << ad.shy);
+        }
         if (!V.dsm) p->all_direct = false;
         const VsAoi &A = aois[V.aoi];
         const long long cells = A.xsize * A.ysize;
