@@ -104,3 +104,29 @@ def test_cube_empty_and_errors(cameras50):
     too_many = cameras50 * 3          # 150 > VS_CUBE_MAX_CAMERAS
     with pytest.raises(_lib.VsError):
         project_cube(too_many, np.zeros((3, 5), np.float32))
+
+
+@pytest.mark.parametrize('n_cams,n', [(50, 20000), (3, 37), (1, 1), (7, 300), (64, 1000)])
+def test_cube_tcgen05_variant(n_cams, n):
+    """BF16X3 on tcgen05 (TMEM accumulators): within the BF16X3 bound of the oracle and
+    within 2e-3 px of the mma.sync BF16X3 kernel (same split, other accumulation order)."""
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.rpc_model import project_cube
+    metas = [synth.make_rpc_meta(3000 + v, 4096, 4096) for v in range(n_cams)]
+    pts = cube_points(n, 17 + n_cams)[:, :n]
+    size = n_cams * 2 * n
+    buf = torch.full((size + 4096,), 12345.0, dtype=torch.float32, device='cuda')
+    tc = buf[:size].view(n_cams, 2, n)
+    project_cube(metas, pts, variant='bf16x3_tc', out=tc)
+    assert (buf[size:] == 12345.0).all()
+    ref = project_cube(metas, pts, variant='bf16x3').cpu().numpy()
+    got = tc.cpu().numpy()
+    assert np.abs(got - oracle_colrow(metas, pts)).max() <= TOL['bf16x3']
+    assert np.abs(got - ref).max() <= 2e-3
+
+
+def test_cube_tcgen05_rejects_too_many_cameras(cameras50):
+    from vissatsatellitestereo_gb300 import _lib
+    from vissatsatellitestereo_gb300.rpc_model import project_cube
+    with pytest.raises(_lib.VsError):
+        project_cube(cameras50 + cameras50[:20], np.zeros((3, 5), np.float32), variant='bf16x3_tc')

@@ -29,6 +29,7 @@ VS_CUBE_FP32 = 0
 VS_CUBE_BF16X3 = 1
 VS_CUBE_TF32X3 = 2
 VS_CUBE_BF16X6 = 3
+VS_CUBE_BF16X3_TC = 4
 VS_CUBE_MAX_CAMERAS = 128
 
 # VsRpcCamera: 92 doubles in declaration order

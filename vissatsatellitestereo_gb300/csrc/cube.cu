@@ -443,6 +443,11 @@ int launch_mma(const VsRpcCamera *cams, int n_cams, const float *xyz, long long 
 }
 
 }  // namespace
+
+size_t cube_tc_workspace_bytes(int n_cams);
+int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
+                   cudaStream_t st);
+
 }  // namespace vs
 
 using namespace vs;
@@ -451,7 +456,7 @@ extern "C" size_t vs_rpc_project_cube_workspace_size(int n_cams) {
     if (n_cams <= 0) return 0;
     Carver cv(nullptr);
     carve_cube(cv, n_cams);
-    return cv.used + 256;
+    return std::max(cv.used + 256, cube_tc_workspace_bytes(n_cams));
 }
 
 extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const float *xyz, int64_t n, float *colrow,
@@ -459,7 +464,7 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
     VS_REQUIRE(n_cams > 0 && n_cams <= VS_CUBE_MAX_CAMERAS && n >= 0,
                "vs_rpc_project_cube: bad sizes (cameras %d, max %d; n %lld)", n_cams, VS_CUBE_MAX_CAMERAS, (long long)n);
     VS_REQUIRE(variant == VS_CUBE_FP32 || variant == VS_CUBE_BF16X3 || variant == VS_CUBE_TF32X3 ||
-                   variant == VS_CUBE_BF16X6,
+                   variant == VS_CUBE_BF16X6 || variant == VS_CUBE_BF16X3_TC,
                "vs_rpc_project_cube: bad variant %d", variant);
     VS_REQUIRE(cams && workspace && (n == 0 || (xyz && colrow)), "vs_rpc_project_cube: null pointer");
     const size_t need = vs_rpc_project_cube_workspace_size(n_cams);
@@ -475,6 +480,7 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
         case VS_CUBE_BF16X3: return launch_mma<VS_CUBE_BF16X3>(cams, n_cams, xyz, n, colrow, w, st);
         case VS_CUBE_TF32X3: return launch_mma<VS_CUBE_TF32X3>(cams, n_cams, xyz, n, colrow, w, st);
         case VS_CUBE_BF16X6: return launch_mma<VS_CUBE_BF16X6>(cams, n_cams, xyz, n, colrow, w, st);
+        case VS_CUBE_BF16X3_TC: return launch_cube_tc(cams, n_cams, xyz, n, colrow, workspace, st);
         default: break;
     }
     cube_prepare_fp32_kernel<<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(kTerms) * 4 * n_cams, 256)), 256, 0,

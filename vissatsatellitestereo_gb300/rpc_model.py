@@ -116,7 +116,7 @@ def project_cameras(meta_dicts, lat, lon, alt, mode='fast', shared=True, keep=Fa
 
 
 CUBE_VARIANTS = {'fp32': _lib.VS_CUBE_FP32, 'bf16x3': _lib.VS_CUBE_BF16X3, 'tf32x3': _lib.VS_CUBE_TF32X3,
-                 'bf16x6': _lib.VS_CUBE_BF16X6}
+                 'bf16x6': _lib.VS_CUBE_BF16X6, 'bf16x3_tc': _lib.VS_CUBE_BF16X3_TC}
 
 
 def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
