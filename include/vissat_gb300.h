@@ -204,12 +204,14 @@ int vs_dsm_from_points(const double *points, const int64_t *offsets, int n_views
 /* vs_dsm_from_points with each view's decode / hole fill / blur on `epilogue_stream`,
  * overlapped with the binning of the next view on `stream` (three rotating key grids, two
  * alternating "first zero" arrays, ordering events).  `stream` covers all of the work when
- * the call's operations complete.  Same results as vs_dsm_from_points. */
+ * the call's operations complete.  Same results as vs_dsm_from_points.  bin_events
+ * (nullable): 2 * n_views cudaEvent_t created by the caller; events 2v and 2v+1 are
+ * recorded on `stream` just before and after view v's binning launch (kernel timing). */
 size_t vs_dsm_from_points_overlap_workspace_size(int n_views, int64_t xsize, int64_t ysize);
 int vs_dsm_from_points_overlap(const double *points, const int64_t *offsets, int n_views, double xoff,
                                double yoff, double xresolution, double yresolution, int64_t xsize,
                                int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
-                               void *stream, void *epilogue_stream);
+                               void *stream, void *epilogue_stream, void *const *bin_events);
 
 /* ---- (c') batched form: many AOIs, per-view FP32 height maps ----------------------------
  * The per-view point lists of aggregate_2p5d_util.py:75-98 (pixel -> UTM of a height map)

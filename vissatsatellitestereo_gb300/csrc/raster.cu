@@ -1047,7 +1047,7 @@ extern "C" size_t vs_dsm_from_points_overlap_workspace_size(int n_views, int64_t
 extern "C" int vs_dsm_from_points_overlap(const double *points, const int64_t *offsets, int n_views, double xoff,
                                           double yoff, double xresolution, double yresolution, int64_t xsize,
                                           int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
-                                          void *stream, void *epilogue_stream) {
+                                          void *stream, void *epilogue_stream, void *const *bin_events) {
     VS_REQUIRE(n_views > 0 && n_views < (1 << 23) && grid_ok(xsize, ysize),
                "vs_dsm_from_points_overlap: bad sizes views=%d grid=%lldx%lld", n_views, (long long)xsize,
                (long long)ysize);
@@ -1080,9 +1080,12 @@ extern "C" int vs_dsm_from_points_overlap(const double *points, const int64_t *o
     };
     for (int v = 0; v < n_views; ++v) {
         if (v >= 2 && !cuda_ok(cudaStreamWaitEvent(st, ev->epi[(v - 2) % 3], 0))) return VS_ERR_CUDA;
+        if (bin_events && !cuda_ok(cudaEventRecord(static_cast<cudaEvent_t>(bin_events[2 * v]), st))) return VS_ERR_CUDA;
         s = bin_launch(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, w.keys[v % 3],
                        w.first[v & 1], st);
         if (s != VS_OK) return s;
+        if (bin_events && !cuda_ok(cudaEventRecord(static_cast<cudaEvent_t>(bin_events[2 * v + 1]), st)))
+            return VS_ERR_CUDA;
         if (!cuda_ok(cudaEventRecord(ev->bin[v % 3], st)) || !cuda_ok(cudaStreamWaitEvent(es, ev->bin[v % 3], 0)))
             return VS_ERR_CUDA;
         unsigned long long *nxt = (v + 2 < n_views) ? w.keys[(v + 2) % 3] : nullptr;

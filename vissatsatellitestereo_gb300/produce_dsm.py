@@ -1,5 +1,7 @@
 """Batched ``produce_dsm_from_points`` (produce_dsm.py:46-58): every view's point cloud
 rasterised onto one DSM grid (proj_to_grid) and median-blurred in float32, in one call."""
+import ctypes
+
 import torch
 
 from . import _lib
@@ -15,13 +17,15 @@ def grid_size(aoi_width, aoi_height, e_resolution=E_RESOLUTION, n_resolution=N_R
 
 
 def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize, ysize, out=None,
-                    epilogue_stream=None):
+                    epilogue_stream=None, bin_events=None):
     """points: (total, 3) float64 (device tensor or array); offsets: (V+1,) int64 view
     boundaries.  Returns (V, ysize, xsize) float32 device tensor.
 
     ``epilogue_stream`` (a torch.cuda.Stream): run each view's decode / hole fill / blur
     there, overlapped with the binning of the next view on the current stream (the
-    current stream still covers all the work when the call returns)."""
+    current stream still covers all the work when the call returns).  ``bin_events`` (with
+    ``epilogue_stream``): a list of 2V timing-enabled torch.cuda.Events recorded around
+    each view's binning launch on the current stream."""
     require_cuda()
     pts = as_device(points, torch.float64)
     offs = as_device(offsets, torch.int64)
@@ -36,5 +40,13 @@ def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize
         _lib.call('vs_dsm_from_points', *args, wp, wb, stream_handle())
     else:
         wp, wb = workspace(_lib.lib().vs_dsm_from_points_overlap_workspace_size(V, xsize, ysize))
-        _lib.call('vs_dsm_from_points_overlap', *args, wp, wb, stream_handle(), epilogue_stream.cuda_stream)
+        evs = None
+        if bin_events is not None:
+            if len(bin_events) != 2 * V:
+                raise ValueError('bin_events needs 2 events per view')
+            for e in bin_events:        # the event handle exists once the event was recorded
+                if not e.cuda_event:
+                    e.record()
+            evs = (ctypes.c_void_p * (2 * V))(*[e.cuda_event for e in bin_events])
+        _lib.call('vs_dsm_from_points_overlap', *args, wp, wb, stream_handle(), epilogue_stream.cuda_stream, evs)
     return out
