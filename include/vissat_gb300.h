@@ -292,6 +292,73 @@ int vs_fuse_dsms(const float *dsm, int layout, int64_t n_views, int64_t h, int64
 int vs_fuse_dsms_static(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
                         int median_blur, void *stream);
 
+/* ---- (f1) depth maps -> UTM points -> DSM ---------------------------------------------------
+ * The chain of aggregate_2p5d_util.py:75-98 (convert_depth_map_worker): depth <= 0 becomes
+ * NaN; pixel (col, row) with depth d maps to inv_proj @ [col, row, 1, d] with a homogeneous
+ * divide (ENU metres about the AOI origin); pixels whose z is NaN are dropped, pixel order
+ * kept; ENU -> lat/lon/alt (coordinate_system.py:41-50, pymap3d.enu2geodetic) and lat/lon ->
+ * UTM easting/northing (lib/latlon_utm_converter.py:38-52, utm + pyproj) in the zone of the
+ * first point.  The geodesy restates the published algorithms (You 2000 for ECEF ->
+ * geodetic, Krueger's series to n^6 for transverse Mercator); pymap3d and pyproj are not
+ * bit-reproduced (their results agree to ~1e-8 m).
+ *
+ * A plan fixes the frame (ENU origin = the AOI centre and lowest altitude,
+ * coordinate_system.py:44-47; UTM zone and hemisphere) and an ENU box.  Inside the box the
+ * VS_GEO_FAST arithmetic evaluates the geodesy as a validated degree-4 polynomial (the plan
+ * checks it against the FP64 chain; enabled only within VS_GEO_FAST_TOL_M metres); outside
+ * it, and in VS_GEO_EXACT mode, every point takes the FP64 chain.  Creating a plan runs
+ * three small kernels and synchronises `stream`; the device buffer (vs_geo_plan_device_bytes)
+ * must stay allocated while the plan is used. */
+#define VS_GEO_EXACT 0
+#define VS_GEO_FAST 1
+#define VS_GEO_FAST_TOL_M 2.5e-7
+#define VS_GEO_FLAG_HEMISPHERE 1   /* a point lies in the other hemisphere (the reference asserts) */
+
+typedef struct VsGeoFrame {
+    double lat0, lon0, alt0;        /* ENU origin: degrees, degrees, metres */
+    int32_t utm_zone;               /* 1..60 */
+    int32_t south;                  /* 1: false northing 10,000 km */
+    double box_lo[3], box_hi[3];    /* ENU box of the fast path (m); box_hi <= box_lo: none */
+} VsGeoFrame;
+
+typedef struct VsGeoPlan VsGeoPlan;
+
+size_t vs_geo_plan_device_bytes(void);
+int vs_geo_plan_create(const VsGeoFrame *frame, void *device_buffer, size_t device_bytes, VsGeoPlan **plan,
+                       void *stream);
+/* Largest |fast - exact| (m) seen by the validation, and whether the fast path is on. */
+int vs_geo_plan_query(const VsGeoPlan *plan, double *max_err_m, int32_t *fast_enabled);
+void vs_geo_plan_destroy(VsGeoPlan *plan);
+
+/* coordinate_system.local_to_global: ENU points (point_stride doubles apart, xyz first) ->
+ * lat, lon (degrees), alt (m), FP64 chain. */
+int vs_enu_to_geodetic(const VsGeoPlan *plan, const double *enu, int64_t n, int64_t point_stride, double *lat,
+                       double *lon, double *alt, void *stream);
+/* lib/latlon_utm_converter.latlon_to_eastnorh in the plan's zone and hemisphere: lat, lon
+ * (degrees) -> easting, northing (m).  flags (device int32, nullable): VS_GEO_FLAG_* or-ed. */
+int vs_geodetic_to_utm(const VsGeoPlan *plan, const double *lat, const double *lon, int64_t n, double *east,
+                       double *north, int32_t *flags, void *stream);
+
+/* One depth map (height x width float32, row-major) -> points[n][3] = (easting, northing,
+ * altitude) of its valid pixels in pixel order; *n_points (device) receives n.  points
+ * must hold height * width rows.  inv_proj: host, 16 doubles, row-major. */
+size_t vs_depth_to_points_workspace_size(int64_t height, int64_t width);
+int vs_depth_to_points(const float *depth, int64_t height, int64_t width, const double *inv_proj,
+                       const VsGeoPlan *plan, int32_t mode, double *points, int64_t *n_points, int32_t *flags,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/* Depth maps -> per-view DSMs without materialising the points: the points of
+ * vs_depth_to_points (the same bits) binned as vs_dsm_from_points does (nanmax, hole fill,
+ * float32, 3x3 median blur) into dsm[n_views][ysize][xsize].  depths: host array of
+ * n_views device pointers; heights, widths: host arrays; inv_projs: host, n_views x 16.
+ * The grid must be positive and lie inside its origins' binades (the fast binning's
+ * precondition; VS_ERR_ARG otherwise -- use vs_depth_to_points + vs_dsm_from_points). */
+size_t vs_dsm_from_depth_maps_workspace_size(int64_t xsize, int64_t ysize);
+int vs_dsm_from_depth_maps(const float *const *depths, const int64_t *heights, const int64_t *widths, int n_views,
+                           const double *inv_projs, const VsGeoPlan *plan, int32_t mode, double xoff, double yoff,
+                           double xresolution, double yresolution, int64_t xsize, int64_t ysize, float *dsm,
+                           int32_t *flags, void *workspace, size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

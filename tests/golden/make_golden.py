@@ -14,6 +14,9 @@ the reference's source for the two routines whose modules do not import:
   and a stand-in ``numpy_groupies`` module whose ``aggregate(func='nanmax')`` restates
   numpy_groupies 0.9.9's numba implementation (see ``oracle/raster.py``).  Binning and
   the hole-fill loop are therefore the reference's own lines.
+* ``aggregate_2p5d_util.py`` -- imports cv2 through produce_dsm.  The depth map -> ENU
+  block of ``convert_depth_map_worker`` is cut out and executed as is (its geodesy calls
+  pymap3d/pyproj, absent, and stays with the oracle's restatement).
 * ``aggregate_2p5d.py`` -- needs cv2/GDAL/imageio.  The fusion block (from
   ``cnt = len(all_dsm)`` to the ``np.nanmean`` line) is cut out of ``run_fuse`` and
   executed as is.
@@ -122,10 +125,70 @@ def ply_files(ref, seed):
     np2ply(v, os.path.join(HERE, 'ply_f64.ply'), use_double=True)
 
 
+def depth_block(ref):
+    """The depth map -> ENU lines of aggregate_2p5d_util.convert_depth_map_worker (from the
+    depth <= 0 replacement to ``points = tmp[:, valid_mask].T``), cut out of the function
+    (its module imports cv2 through produce_dsm) and compiled as they are."""
+    lines = open(os.path.join(ref, 'aggregate_2p5d_util.py')).read().splitlines()
+    start = next(i for i, l in enumerate(lines) if 'depth_map[depth_map <= 0.0] = np.nan' in l)
+    end = next(i for i, l in enumerate(lines) if l.strip().startswith('points = tmp[:, valid_mask].T'))
+    body = '\n'.join(l[4:] for l in lines[start:end + 1])
+    return compile(body, os.path.join(ref, 'aggregate_2p5d_util.py'), 'exec')
+
+
+def _colmap_bytes(arr):
+    """A COLMAP dense array file: "width&height&channels&" then float32 column-major
+    (width, height, channels), written here from the format's description."""
+    a = arr if arr.ndim == 3 else arr[:, :, None]
+    h, w, c = a.shape
+    body = np.asfortranarray(np.transpose(a, (1, 0, 2)).astype('<f4')).tobytes(order='F')
+    return f'{w}&{h}&{c}&'.encode() + body
+
+
+def depth_files(ref, seed):
+    """(h) colmap/read_dense.read_array on a depth map (1 channel) and a normal map (3
+    channels); the depth -> ENU block of convert_depth_map_worker on two synthetic views."""
+    from colmap.read_dense import read_array
+    sys.path.insert(0, REPO)
+    from oracle import geo
+    rng = np.random.default_rng(seed + 900)
+    depth = rng.uniform(-1.0, 2.0, (23, 37)).astype(np.float32)
+    normal = rng.normal(0.0, 1.0, (23, 37, 3)).astype(np.float32)
+    out = {}
+    for name, arr in (('depth', depth), ('normal', normal)):
+        path = os.path.join(HERE, f'colmap_{name}.bin')
+        with open(path, 'wb') as f:
+            f.write(_colmap_bytes(arr))
+        out[f'{name}_written'] = arr
+        out[f'{name}_read'] = read_array(path)
+    np.savez_compressed(os.path.join(HERE, 'colmap_arrays.npz'), **out)
+
+    def utm(la, lo, z, s):
+        e, n = geo.geodetic_to_utm(np.array([la]), np.array([lo]), z, s)
+        return float(e[0]), float(n[0])
+
+    case = synth.make_depth_case(seed + 950, 2, 40, 56, utm, aoi_m=60.0, n_boxes=8)
+    block = depth_block(ref)
+    res = {'aoi': np.array(repr(case.aoi))}
+    for v in range(2):
+        depth_map = synth.depth_map_torch(case, v).numpy()
+        depth_map[3, 5] = np.nan
+        depth_map[4, 7] = np.inf
+        ns = {'np': np, 'depth_map': depth_map.copy(), 'inv_proj_mats': {'img': case.inv_proj[v]},
+              'img_name': 'img'}
+        exec(block, ns)
+        res[f'v{v}_depth'] = depth_map
+        res[f'v{v}_inv_proj'] = case.inv_proj[v]
+        res[f'v{v}_points4'] = ns['points']
+        res[f'v{v}_valid'] = ns['valid_mask']
+        res[f'v{v}_height_map'] = ns['height_map']
+    np.savez_compressed(os.path.join(HERE, 'depth_enu.npz'), **res)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
-    ap.add_argument('--sections', default='all', help="'all' or a comma list of: base, inverse, formats")
+    ap.add_argument('--sections', default='all', help="'all' or a comma list of: base, inverse, formats, depth")
     args = ap.parse_args()
     ref = os.path.abspath(args.ref)
     sys.path.insert(0, ref)
@@ -135,7 +198,9 @@ def main():
     from lib.gen_grid import gen_grid
 
     seed = synth.BASE_SEED
-    sections = {'base', 'inverse', 'formats'} if args.sections == 'all' else set(args.sections.split(','))
+    sections = {'base', 'inverse', 'formats', 'depth'} if args.sections == 'all' else set(args.sections.split(','))
+    if 'depth' in sections:
+        depth_files(ref, seed)
     if 'inverse' in sections:
         inverse_and_affine(ref, seed)
     if 'formats' in sections:

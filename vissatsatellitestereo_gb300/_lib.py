@@ -31,6 +31,10 @@ VS_CUBE_TF32X3 = 2
 VS_CUBE_BF16X6 = 3
 VS_CUBE_BF16X3_TC = 4
 VS_CUBE_MAX_CAMERAS = 128
+VS_GEO_EXACT = 0
+VS_GEO_FAST = 1
+VS_GEO_FAST_TOL_M = 2.5e-7
+VS_GEO_FLAG_HEMISPHERE = 1
 
 # VsRpcCamera: 92 doubles in declaration order
 CAMERA_DOUBLES = 92
@@ -81,7 +85,23 @@ SIGNATURES = {
     'vs_fuse_dsms_workspace_size': (_sz, [_i64, _i64]),
     'vs_fuse_dsms': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp, _sz, _vp]),
     'vs_fuse_dsms_static': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp]),
+    'vs_geo_plan_device_bytes': (_sz, []),
+    'vs_geo_plan_create': (_int, [_vp, _vp, _sz, _vp, _vp]),
+    'vs_geo_plan_query': (_int, [_vp, _vp, _vp]),
+    'vs_geo_plan_destroy': (None, [_vp]),
+    'vs_enu_to_geodetic': (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp]),
+    'vs_geodetic_to_utm': (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    'vs_depth_to_points_workspace_size': (_sz, [_i64, _i64]),
+    'vs_depth_to_points': (_int, [_vp, _i64, _i64, _vp, _vp, _int, _vp, _vp, _vp, _vp, _sz, _vp]),
+    'vs_dsm_from_depth_maps_workspace_size': (_sz, [_i64, _i64]),
+    'vs_dsm_from_depth_maps': (_int, [_vp, _vp, _vp, _int, _vp, _vp, _int, _dbl, _dbl, _dbl, _dbl, _i64, _i64, _vp,
+                                      _vp, _vp, _sz, _vp]),
 }
+
+
+class VsGeoFrame(ctypes.Structure):
+    _fields_ = [('lat0', _dbl), ('lon0', _dbl), ('alt0', _dbl), ('utm_zone', ctypes.c_int32),
+                ('south', ctypes.c_int32), ('box_lo', _dbl * 3), ('box_hi', _dbl * 3)]
 
 
 class VsError(RuntimeError):

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "geo.cuh"
 
 namespace vs {
 namespace {
@@ -1410,3 +1411,167 @@ extern "C" int vs_aoi_batch_fuse(const VsAoiBatch *plan, int aoi_begin, int aoi_
 }
 
 extern "C" void vs_aoi_batch_destroy(VsAoiBatch *plan) { delete plan; }
+
+// ---- (f1) depth maps -> DSM, without materialising the points ------------------------------
+// Each pixel's (easting, northing, altitude) is computed as vs_depth_to_points does (the same
+// shared device code, so the same bits) and binned at once with the fast binning.  Zeros of
+// the nanmax keep the first-of-equal rule through the "first zero" words, which here carry
+// the pixel index (monotone in the point index) and the zero's sign in bit 0.
+namespace vs {
+namespace {
+
+constexpr unsigned long long kDepthIdxLimit = 1ull << 39;
+
+struct SignZeroDecoder {
+    const unsigned long long *first;
+    __device__ __forceinline__ unsigned long long operator()(unsigned long long k, long long cell) const {
+        if (k != kZeroKey) return k;
+        return (first[cell] & 1ull) ? 0x7fffffffffffffffull : kZeroKey;
+    }
+};
+
+template <bool FLIP_ROW, bool FLIP_COL>
+__global__ void __launch_bounds__(256) depth_bin_kernel(const float *__restrict__ depth, long long H, long long W,
+                                                        DepthView v, GeoFast f, const GeoFrame *g, int mode,
+                                                        int south, FastAxis ra, FastAxis ca, int view,
+                                                        unsigned long long *__restrict__ vk,
+                                                        unsigned long long *__restrict__ first, int *flags) {
+    const long long total = H * W;
+    const unsigned long long tag = epoch_tag(view);
+    const unsigned long long ncols = static_cast<unsigned>(ca.nm1 + 1);
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * kDepthPix;
+    for (long long p = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kDepthPix; p < total;
+         p += stride) {
+        float d[kDepthPix];
+        load_depths(depth, p, total, d);
+        long long r = p / W, c = p - r * W;
+        long long run_cell = -1;
+        unsigned long long run_key = kEmptyKey;
+#pragma unroll 1
+        for (int k = 0; k < kDepthPix; ++k) {
+            const float cf = static_cast<float>(c), rf = static_cast<float>(r);
+            const int cls = pixel_class(v, cf, rf, d[k]);
+            unsigned long long bits[3];
+            if (cls != 0 && pixel_point(v, f, g, mode, cls, cf, rf, d[k], south, bits, flags)) {
+                int rr, cc;
+                long long dr, dc;
+                bool sr, sc;
+                bool ok = axis_fast<FLIP_ROW>(ra, static_cast<long long>(bits[1]), rr, dr, sr);
+                ok &= axis_fast<FLIP_COL>(ca, static_cast<long long>(bits[0]), cc, dc, sc);
+                ok &= !is_nan_bits(bits[2]);
+                if (ok) {
+                    if (!sr) rr = axis_correct(ra.thr, rr, dr);
+                    if (!sc) cc = axis_correct(ca.thr, cc, dc);
+                    const long long cell =
+                        static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(rr)) * ncols) + cc;
+                    const unsigned long long zb = bits[2];
+                    unsigned long long key;
+                    if ((zb << 1) == 0) {
+                        key = kZeroKey;
+                        const unsigned long long idx = static_cast<unsigned long long>(p + k);
+                        atomicMax(first + cell, tag | ((kDepthIdxLimit - 1ull - idx) << 1) | (zb >> 63));
+                    } else {
+                        key = (zb >> 63) ? ~zb : (zb | 0x8000000000000000ull);
+                    }
+                    if (cell == run_cell) {
+                        run_key = max(run_key, key);
+                    } else {
+                        if (run_key != kEmptyKey) atomicMax(vk + run_cell, run_key);
+                        run_cell = cell;
+                        run_key = key;
+                    }
+                }
+            }
+            if (++c == W) {
+                c = 0;
+                ++r;
+            }
+        }
+        if (run_key != kEmptyKey) atomicMax(vk + run_cell, run_key);
+    }
+}
+
+__global__ void __launch_bounds__(TX *TY) depth_epilogue_kernel(const unsigned long long *__restrict__ vk,
+                                                               const unsigned long long *__restrict__ first,
+                                                               float *__restrict__ out,
+                                                               unsigned long long *__restrict__ next_keys, int H,
+                                                               int W) {
+    __shared__ EpilogueSmem sm;
+    epilogue_tile(vk, SignZeroDecoder{first}, out, next_keys, H, W, blockIdx.y * TILE_Y, blockIdx.x * TX, sm);
+}
+
+FastAxis fast_axis_of(const Axis &ax) {
+    FastAxis fa;
+    memcpy(&fa.off_bits, &ax.off, sizeof(long long));
+    fa.tmax = ax.tmax;
+    fa.thr = ax.thr;
+    fa.top12 = ax.top12;
+    fa.shift = ax.shift;
+    fa.nm1 = static_cast<int>(ax.n - 1);
+    fa.scale = ax.scale;
+    fa.err_abs = ax.err_abs;
+    fa.err_rel = ax.err_rel;
+    return fa;
+}
+
+}  // namespace
+}  // namespace vs
+
+extern "C" size_t vs_dsm_from_depth_maps_workspace_size(int64_t xsize, int64_t ysize) {
+    if (xsize <= 0 || ysize <= 0) return 0;
+    return carve_raster(nullptr, xsize, ysize, true).bytes + 256;
+}
+
+extern "C" int vs_dsm_from_depth_maps(const float *const *depths, const int64_t *heights, const int64_t *widths,
+                                      int n_views, const double *inv_projs, const VsGeoPlan *plan, int32_t mode,
+                                      double xoff, double yoff, double xresolution, double yresolution, int64_t xsize,
+                                      int64_t ysize, float *dsm, int32_t *flags, void *workspace,
+                                      size_t workspace_bytes, void *stream) {
+    VS_REQUIRE(n_views > 0 && n_views < (1 << 23) && grid_ok(xsize, ysize),
+               "vs_dsm_from_depth_maps: bad sizes views=%d grid=%lldx%lld", n_views, (long long)xsize,
+               (long long)ysize);
+    VS_REQUIRE(depths && heights && widths && inv_projs && plan && dsm && workspace,
+               "vs_dsm_from_depth_maps: null pointer");
+    VS_REQUIRE(mode == VS_GEO_EXACT || mode == VS_GEO_FAST, "vs_dsm_from_depth_maps: bad mode %d", mode);
+    for (int v = 0; v < n_views; ++v)
+        VS_REQUIRE(depths[v] && heights[v] > 0 && widths[v] > 0 && heights[v] * widths[v] < (1LL << 39) &&
+                       heights[v] < (1 << 24) && widths[v] < (1 << 24),
+                   "vs_dsm_from_depth_maps: bad view %d", v);
+    const size_t need = vs_dsm_from_depth_maps_workspace_size(xsize, ysize);
+    if (workspace_bytes < need) {
+        set_error("vs_dsm_from_depth_maps: workspace %zu < %zu bytes", workspace_bytes, need);
+        return VS_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream);
+    RasterWs w = carve_raster(workspace, xsize, ysize, true);
+    Tables tb;
+    const long long cells = xsize * ysize;
+    int s = make_tables(xoff, yoff, xresolution, yresolution, xsize, ysize, w, tb, st);
+    if (s != VS_OK) return s;
+    VS_REQUIRE(tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained && xoff > 0 && yoff > 0,
+               "vs_dsm_from_depth_maps: the grid must be positive and inside its origins' binades");
+    if ((s = clear(w.keys[0], sizeof(unsigned long long) * cells, st)) != VS_OK) return s;
+    if ((s = clear(w.first, sizeof(unsigned long long) * cells, st)) != VS_OK) return s;
+    const FastAxis fr = fast_axis_of(tb.row), fc = fast_axis_of(tb.col);
+    const GeoFast &gf = geo_plan_fast(plan);
+    const GeoFrame *gfr = geo_plan_frame(plan);
+    const int south = geo_plan_south(plan);
+    const dim3 egrid(static_cast<unsigned>(ceil_div(xsize, TX)), static_cast<unsigned>(ceil_div(ysize, TILE_Y)));
+    int *fl = reinterpret_cast<int *>(flags);
+    for (int v = 0; v < n_views; ++v) {
+        DepthView dv;
+        VS_REQUIRE(make_depth_view(inv_projs + 16 * v, dv), "vs_dsm_from_depth_maps: non-finite matrix of view %d", v);
+        unsigned long long *cur = w.keys[v & 1], *nxt = (v + 1 < n_views) ? w.keys[(v + 1) & 1] : nullptr;
+        const long long total = heights[v] * widths[v];
+        const unsigned gx = static_cast<unsigned>(
+            std::max<long long>(1, std::min<long long>(ceil_div(ceil_div(total, kDepthPix), 256), sm_count() * 8LL)));
+        // rows: a = off - v for the positive origin; columns: a = v - off
+        depth_bin_kernel<true, false><<<gx, 256, 0, st>>>(depths[v], heights[v], widths[v], dv, gf, gfr, mode, south,
+                                                          fr, fc, v, cur, w.first, fl);
+        VS_LAUNCH_CHECK("depth_bin_kernel");
+        depth_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(cur, w.first, dsm + v * cells, nxt,
+                                                              static_cast<int>(ysize), static_cast<int>(xsize));
+        VS_LAUNCH_CHECK("depth_epilogue_kernel");
+    }
+    return VS_OK;
+}

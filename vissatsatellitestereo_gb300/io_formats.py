@@ -212,3 +212,52 @@ def read_dsm_tif(path):
         meta['alt_min'] = float(np.nanmin(image)) if np.isfinite(image).any() else float('nan')
         meta['alt_max'] = float(np.nanmax(image)) if np.isfinite(image).any() else float('nan')
     return image, meta
+
+
+# ---- COLMAP dense arrays and inverse projection matrices ---------------------------------
+def read_array(path):
+    """``colmap/read_dense.py:36-51``: an ASCII header "width&height&channels&" followed by
+    float32 values in column-major (width, height, channels) order; returns (height, width)
+    for one channel, (height, width, channels) otherwise, as the reference's squeeze does."""
+    with open(path, 'rb') as f:
+        raw = f.read()
+    pos, fields = 0, []
+    while len(fields) < 3:
+        amp = raw.index(b'&', pos)
+        fields.append(int(raw[pos:amp].decode().strip()))
+        pos = amp + 1
+    width, height, channels = fields
+    arr = np.frombuffer(raw, dtype='<f4', offset=pos, count=width * height * channels)
+    arr = arr.reshape((width, height, channels), order='F')
+    return np.transpose(arr, (1, 0, 2)).squeeze()
+
+
+def write_array(array, path):
+    """Inverse of ``read_array`` (COLMAP's writer): (height, width[, channels]) float32."""
+    a = _host(array).astype(np.float32)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    height, width, channels = a.shape
+    with open(path, 'wb') as f:
+        f.write(f'{width}&{height}&{channels}&'.encode())
+        f.write(np.transpose(a, (1, 0, 2)).astype('<f4').tobytes(order='F'))
+
+
+def read_inv_proj_mats(path):
+    """``aggregate_2p5d_util.py:55-61``: one line per image, "name m00 m01 ... m33"
+    (space-separated, row-major) -> {name: (4, 4) float64}."""
+    mats = {}
+    with open(path) as fp:
+        for line in fp.readlines():
+            tmp = line.split(' ')
+            mats[tmp[0]] = np.array([float(tmp[i]) for i in range(1, 17)]).reshape((4, 4))
+    return mats
+
+
+def write_inv_proj_mats(mats, path):
+    """Writes {name: (4, 4)} in the layout ``read_inv_proj_mats`` reads (repr of each float,
+    so the values round-trip exactly)."""
+    with open(path, 'w') as fp:
+        for name, m in mats.items():
+            vals = ' '.join(repr(float(x)) for x in np.asarray(m, dtype=np.float64).reshape(-1))
+            fp.write(f'{name} {vals}\n')

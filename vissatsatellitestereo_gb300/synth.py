@@ -494,3 +494,100 @@ def make_aoi_catalog(n_aois: int = 400, seed: int = BASE_SEED, area_km2=(0.2, 4.
         img = int(round(_loguniform(rng, image[0], image[1])))
         specs.append(AoiSpec(a, xoff, yoff, r, xsize, ysize, n_views, img, seed + 104729 * (a + 1)))
     return specs
+
+
+# --------------------------------------------------------------------------------------
+# Depth maps of satellite-like perspective views (the depth map -> UTM points chain)
+# --------------------------------------------------------------------------------------
+@dataclass
+class DepthCase:
+    """An AOI (the reference's aoi.json fields), a box-city scene in ENU metres about the
+    AOI origin, and per-view 4x4 inverse projection matrices as COLMAP's inv_proj_mats.txt
+    holds them (``aggregate_2p5d_util.py:55-61``)."""
+    aoi: dict
+    scene: Scene
+    inv_proj: np.ndarray     # (V, 4, 4) float64
+    height: int
+    width: int
+    nan_frac: list
+    seeds: list
+
+
+def make_depth_case(seed: int, n_views: int, height: int, width: int, utm_fn, aoi_m: float = 600.0,
+                    lat0: float = 39.77, lon0: float = -84.05, n_boxes: int = 300) -> DepthCase:
+    """Views of a square AOI of side ``aoi_m`` from cameras 550-650 km away, 5-30 degrees off
+    nadir: P = K [R | -R C] in ENU, extended with a [0 0 0 1] row and inverted (so the
+    "depth" of a pixel is the reciprocal of its projective scale).  ``utm_fn(lat, lon, zone,
+    south) -> (east, north)`` places the AOI's upper-left UTM corner (ul_easting,
+    ul_northing) from its centre."""
+    from .coordinate_system import utm_zone
+    rng = np.random.default_rng(seed)
+    dlat = aoi_m / 2.0 / 111132.954
+    dlon = aoi_m / 2.0 / (111319.49 * math.cos(math.radians(lat0)))
+    zone = utm_zone(lat0, lon0)
+    south = lat0 < 0
+    ec, nc = utm_fn(lat0, lon0, zone, south)
+    aoi = {'lat_min': lat0 - dlat, 'lat_max': lat0 + dlat, 'lon_min': lon0 - dlon, 'lon_max': lon0 + dlon,
+           'alt_min': -30.0, 'alt_max': 120.0, 'width': aoi_m, 'height': aoi_m,
+           'ul_easting': float(np.floor(float(ec) - aoi_m / 2.0)),
+           'ul_northing': float(np.floor(float(nc) + aoi_m / 2.0)),
+           'zone_number': zone, 'hemisphere': 'S' if south else 'N'}
+    grid = DsmGrid(-aoi_m / 2.0, aoi_m / 2.0, 0.5, 0.5, int(aoi_m / 0.5), int(aoi_m / 0.5))
+    scene = make_scene(seed + 1, grid, n_boxes, 3.0, 80.0, noise=0.2)
+    mats, fracs, seeds = [], [], []
+    for v in range(n_views):
+        off = math.radians(rng.uniform(5.0, 30.0))
+        az = rng.uniform(0.0, 2.0 * math.pi)
+        dist = rng.uniform(550e3, 650e3)
+        target = np.array([rng.uniform(-20, 20), rng.uniform(-20, 20), 30.0])
+        C = target + dist * np.array([math.sin(off) * math.sin(az), math.sin(off) * math.cos(az), math.cos(off)])
+        z = (target - C) / np.linalg.norm(target - C)
+        x = np.cross(z, [0.0, 1.0, 0.0])
+        x /= np.linalg.norm(x)
+        y = np.cross(z, x)
+        roll = rng.uniform(-0.1, 0.1)
+        x, y = math.cos(roll) * x + math.sin(roll) * y, -math.sin(roll) * x + math.cos(roll) * y
+        R = np.stack([x, y, z])
+        f = width * dist / (1.15 * aoi_m)
+        K = np.array([[f, rng.normal(0.0, 1.0), width / 2.0], [0.0, f * rng.uniform(0.999, 1.001), height / 2.0],
+                      [0.0, 0.0, 1.0]])
+        P4 = np.eye(4)
+        P4[:3, :3] = K @ R
+        P4[:3, 3] = -K @ R @ C
+        mats.append(np.linalg.inv(P4))
+        fracs.append(float(rng.uniform(0.10, 0.20)))
+        seeds.append(int(seed * 1000 + v))
+    return DepthCase(aoi, scene, np.stack(mats), height, width, fracs, seeds)
+
+
+def depth_map_torch(case: DepthCase, v: int, device='cpu'):
+    """(H, W) float32 depth map of view v: each pixel's depth puts its point on the scene
+    surface (the ray meets up = 0, the scene height there plus N(0, noise) is looked up, and
+    the depth solving up = height is taken), rounded to float32; ``nan_frac`` of the pixels
+    are invalid (COLMAP's -1e20, a few exact zeros)."""
+    import torch
+    f64 = torch.float64
+    H, W = case.height, case.width
+    M = torch.tensor(case.inv_proj[v], dtype=f64, device=device)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(case.seeds[v])
+    cc = torch.arange(W, device=device, dtype=f64)[None, :]
+    rr = torch.arange(H, device=device, dtype=f64)[:, None]
+    a = [M[i, 0] * cc + M[i, 1] * rr + M[i, 2] for i in range(4)]
+    b = [M[i, 3] for i in range(4)]
+    d0 = -a[2] / b[2]                                        # up = 0 (w = a3 + b3 d)
+    w0 = a[3] + b[3] * d0
+    e = (a[0] + b[0] * d0) / w0
+    n = (a[1] + b[1] * d0) / w0
+    ras, e0, n0, step = scene_raster_torch(case.scene, device)
+    ci = ((e - e0) / step).floor().long()
+    ri = ((n0 - n) / step).floor().long()
+    inside = (ci >= 0) & (ci < ras.shape[1]) & (ri >= 0) & (ri < ras.shape[0])
+    h = ras[ri.clamp(0, ras.shape[0] - 1), ci.clamp(0, ras.shape[1] - 1)].to(f64)
+    h = torch.where(inside, h, torch.zeros_like(h))
+    h = h + torch.randn((H, W), generator=gen, device=device, dtype=f64) * case.scene.noise
+    d = ((h * a[3] - a[2]) / (b[2] - h * b[3])).to(torch.float32)
+    u = torch.rand((H, W), generator=gen, device=device)
+    d = torch.where(u < case.nan_frac[v], torch.full_like(d, -1e20), d)
+    d = torch.where(u < 0.01 * case.nan_frac[v], torch.zeros_like(d), d)
+    return d.contiguous()
