@@ -368,6 +368,8 @@ def run_ours(args):
         result['batched_form'] = batched_form(steps=2, warmup=1)
         # ---- serving form (config: Poisson AOI fusion requests, resident state, 150 GB budget)
         result['serving_form'] = serving_form(n_requests=args.serve)
+        # ---- depth maps -> UTM points -> DSMs (the step before the rasterisation, fused into it)
+        result['depth_form'] = depth_form()
         # ---- CPU baseline (oracle, bounded sample)
         result['cpu_baseline'] = cpu_baseline(wl, gargs, pool=False)
     replicas.finish()
@@ -434,6 +436,96 @@ def precision_form(metas, n_points=16 << 20, steps=10, warmup=3, sample_stride=1
     del out, xyz, ref_col, ref_row
     torch.cuda.empty_cache()
     return res
+
+
+def depth_form(n_views=50, image=4096, cells=2000, res=0.3, steps=3, warmup=1, exact_views=2, cpu_crop=768,
+               seed=None):
+    """Depth maps -> UTM points -> per-view DSMs (aggregate_2p5d_util.py:75-98 feeding
+    produce_dsm_from_points): `n_views` synthetic image x image float32 depth maps of a
+    600 m AOI seen from 550-650 km, rasterised onto cells x cells at `res` m.
+
+    * fused: ``dsm_from_depth_maps`` (fast geodesy, points never materialised);
+    * points path: ``depth_map_to_points`` per view + ``dsm_from_points``;
+    * exact: the fused path with the FP64 geodesy chain per pixel, on `exact_views` views;
+    * CPU: the oracle's numpy chain (depth -> ENU -> geodetic -> UTM) on a crop.
+    Device time by CUDA events; inputs resident in HBM (3.4 GB of depth maps > L2)."""
+    import numpy as np
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.aggregate_2p5d_util import depth_map_to_points, dsm_from_depth_maps
+    from vissatsatellitestereo_gb300.coordinate_system import aoi_enu_box, aoi_origin, latlon_to_eastnorh, plan_for
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+
+    def utm(la, lo, z, s):
+        e, n = latlon_to_eastnorh(np.array([la]), np.array([lo]))
+        return float(e[0]), float(n[0])
+
+    seed = synth.BASE_SEED + 3000 if seed is None else seed
+    case = synth.make_depth_case(seed, n_views, image, image, utm, aoi_m=cells * res, n_boxes=300)
+    aoi = case.aoi
+    zones = [(aoi['zone_number'], aoi['hemisphere'] == 'S')] * n_views
+    grid = (aoi['ul_easting'], aoi['ul_northing'], res, res, cells, cells)
+    depths = [synth.depth_map_torch(case, v, 'cuda') for v in range(n_views)]
+    mats = list(case.inv_proj)
+    plan = plan_for(*aoi_origin(aoi), aoi['zone_number'], aoi['hemisphere'] == 'S', aoi_enu_box(aoi))
+    out = torch.empty((n_views, cells, cells), dtype=torch.float32, device='cuda')
+    pixels = n_views * image * image
+
+    def timed(fn, reps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    t_fused = timed(lambda: dsm_from_depth_maps(depths, mats, aoi, grid, 'fast', zones, out=out), steps, warmup)
+    fused = out.clone()
+
+    def points_path():
+        pts = [depth_map_to_points(d, mats[v], aoi, 'fast', *zones[v]) for v, d in enumerate(depths)]
+        offs = torch.tensor(np.cumsum([0] + [p.shape[0] for p in pts]), dtype=torch.int64, device='cuda')
+        dsm_from_points(torch.cat(pts), offs, *grid, out=out)
+        return sum(p.shape[0] for p in pts)
+
+    n_points = points_path()
+    t_points = timed(points_path, 1, 0)
+    same = bool(torch.equal(fused.view(torch.int32), out.view(torch.int32)))
+    ev = exact_views
+    t_exact = timed(lambda: dsm_from_depth_maps(depths[:ev], mats[:ev], aoi, grid, 'exact', zones[:ev],
+                                                out=out[:ev]), 1, 1)
+    diff = (fused[:ev] != out[:ev]) & ~(torch.isnan(fused[:ev]) & torch.isnan(out[:ev]))
+    exact_cells = {'differing_cells_frac': float(diff.float().mean()),
+                   'max_abs_diff_m': float((fused[:ev] - out[:ev]).abs().nan_to_num(0.0).max())}
+    res_ = {'workload': f'{n_views} depth maps of {image}x{image} float32 -> {cells}x{cells} DSMs at {res} m '
+                        f'(600 m AOI, cameras 550-650 km away, 10-20% invalid pixels)',
+            'unit': 'depth pixels/s', 'pixels': pixels, 'points': int(n_points),
+            'fast_plan_max_err_m': plan.max_err_m, 'fast_plan_enabled': plan.fast_enabled,
+            'fused': {'ms_per_view': round(t_fused / n_views * 1e3, 4), 'pixels_per_s': pixels / t_fused},
+            'points_path': {'ms_per_view': round(t_points / n_views * 1e3, 4), 'pixels_per_s': pixels / t_points,
+                            'same_dsm_bits_as_fused': same},
+            'exact_fp64': {'ms_per_view': round(t_exact / ev * 1e3, 4), 'pixels_per_s': ev * image * image / t_exact,
+                           'views': ev, 'dsm_vs_fast': exact_cells}}
+    del depths, out, fused
+    torch.cuda.empty_cache()
+    # CPU: the oracle's numpy chain on a crop of view 0 (one core)
+    import time
+    from oracle import geo
+    d0 = synth.depth_map_torch(case, 0, 'cpu').numpy()
+    r0 = (image - cpu_crop) // 2
+    crop = np.ascontiguousarray(d0[r0:r0 + cpu_crop, r0:r0 + cpu_crop])
+    M = case.inv_proj[0].copy()
+    M[:, 2] += M[:, 0] * r0 + M[:, 1] * r0          # the crop's pixel (c, r) is (c + r0, r + r0)
+    t0 = time.perf_counter()
+    geo.depth_to_points(crop, M, *aoi_origin(aoi))
+    t_cpu = time.perf_counter() - t0
+    res_['cpu_oracle_points'] = {'pixels_per_s': crop.size / t_cpu, 'cores': 1, 'kind': 'port',
+                                 'sample': f'{cpu_crop}x{cpu_crop} crop of one view, depth -> UTM points (numpy)'}
+    return res_
 
 
 def plain_aoi_seconds(spec, maps, affines):
@@ -779,7 +871,15 @@ def main():
     ap.add_argument('--serve', type=int, default=400, metavar='REQUESTS',
                     help='requests of the serving form (Poisson 20/s; 2000 is the full stream)')
     ap.add_argument('--serve-only', action='store_true', help='run only the serving form')
+    ap.add_argument('--depth-only', type=int, default=0, metavar='VIEWS',
+                    help='run only the depth map -> DSM form over VIEWS views (0: off)')
     args = ap.parse_args()
+    if args.depth_only:
+        from vissatsatellitestereo_gb300.build import build
+        build()
+        print(json.dumps({'depth_form': depth_form(n_views=args.depth_only, image=args.image,
+                                                   steps=args.steps, warmup=args.warmup)}))
+        return
     if args.serve_only:
         from vissatsatellitestereo_gb300.build import build
         build()

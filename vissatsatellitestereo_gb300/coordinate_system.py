@@ -39,10 +39,12 @@ def aoi_origin(aoi):
     return lat0, lon0, aoi['alt_min']
 
 
-def aoi_enu_box(aoi, margin=0.25, pad_m=50.0):
+def aoi_enu_box(aoi, margin=1.0, pad_m=500.0, pad_up_m=200.0):
     """ENU box of the fast path for an AOI: its latitude/longitude extent at the origin's
-    scale, enlarged by `margin` and `pad_m`, altitudes alt_min .. alt_max plus the same pad
-    and the Earth-curvature drop across the box.  Points outside take the FP64 chain."""
+    scale, doubled (`margin`) and padded by `pad_m` -- satellite views cropped to an AOI
+    reach well beyond it, and the polynomial stays within its validated bound over a few
+    km -- with altitudes alt_min .. alt_max padded by `pad_up_m` and the Earth-curvature
+    drop across the box.  Points outside take the FP64 chain."""
     aoi = load_aoi(aoi)
     lat0, lon0, alt0 = aoi_origin(aoi)
     rad = math.pi / 180.0
@@ -51,8 +53,8 @@ def aoi_enu_box(aoi, margin=0.25, pad_m=50.0):
     he = he * (1.0 + margin) + pad_m
     hn = hn * (1.0 + margin) + pad_m
     drop = (he * he + hn * hn) / (2.0 * EARTH_RADIUS_M)
-    lo = (-he, -hn, -pad_m - drop)
-    hi = (he, hn, aoi['alt_max'] - alt0 + pad_m)
+    lo = (-he, -hn, -pad_up_m - drop)
+    hi = (he, hn, aoi['alt_max'] - alt0 + pad_up_m)
     return lo, hi
 
 

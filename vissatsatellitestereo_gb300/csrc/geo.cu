@@ -212,18 +212,16 @@ __global__ void geodetic_to_utm_kernel(const GeoFrame *g, const double *__restri
 
 // ---- depth map -> points ------------------------------------------------------------------
 // Valid-pixel mask of a thread's 8 pixels (bit k: pixel p + k).
-__device__ __forceinline__ unsigned valid_mask(const DepthView &v, const float (&d)[kPixPerThread], long long p,
-                                               long long W) {
+__device__ __forceinline__ unsigned valid_mask(const DepthView &v, const double *smd, const float (&d)[kPixPerThread],
+                                               long long p, long long W) {
     long long r = p / W, c = p - r * W;
     unsigned mask = 0;
 #pragma unroll
     for (int k = 0; k < kPixPerThread; ++k) {
-        const int cls = pixel_class(v, static_cast<float>(c), static_cast<float>(r), d[k]);
+        const float cf = static_cast<float>(c), rf = static_cast<float>(r);
+        const int cls = pixel_class(v, cf, rf, d[k]);
         bool ok = cls == 1;
-        if (cls == 2) {
-            double enu[3];
-            ok = pixel_enu_exact(v, static_cast<float>(c), static_cast<float>(r), d[k], enu);
-        }
+        if (cls == 2) ok = pixel_valid_exact(smd, cf, rf, d[k]);
         mask |= ok ? (1u << k) : 0u;
         if (++c == W) {
             c = 0;
@@ -236,11 +234,13 @@ __device__ __forceinline__ unsigned valid_mask(const DepthView &v, const float (
 __global__ void __launch_bounds__(kPixThreads) depth_count_kernel(const float *__restrict__ depth, long long H,
                                                                   long long W, DepthView v, int *__restrict__ counts) {
     __shared__ int warp_sum[kPixThreads / 32];
+    __shared__ double smd[16];
+    stage_matrix(v, smd);
     const long long total = H * W;
     const long long p = static_cast<long long>(blockIdx.x) * kPixPerBlock + threadIdx.x * kPixPerThread;
     float d[kPixPerThread];
     load_depths(depth, p, total, d);
-    int n = __popc(valid_mask(v, d, p, W));
+    int n = __popc(valid_mask(v, smd, d, p, W));
 #pragma unroll
     for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
     if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = n;
@@ -280,11 +280,13 @@ __global__ void __launch_bounds__(kPixThreads) depth_points_kernel(
     const float *__restrict__ depth, long long H, long long W, DepthView v, GeoFast f, const GeoFrame *g, int mode,
     int south, const long long *__restrict__ offsets, unsigned long long *__restrict__ out, int *flags) {
     __shared__ int warp_sum[kPixThreads / 32];
+    __shared__ double smd[16];
+    stage_matrix(v, smd);
     const long long total = H * W;
     const long long p = static_cast<long long>(blockIdx.x) * kPixPerBlock + threadIdx.x * kPixPerThread;
     float d[kPixPerThread];
     load_depths(depth, p, total, d);
-    const unsigned mask = valid_mask(v, d, p, W);
+    const unsigned mask = valid_mask(v, smd, d, p, W);
     // block-exclusive prefix of the per-thread counts
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int n = __popc(mask);
@@ -305,7 +307,10 @@ __global__ void __launch_bounds__(kPixThreads) depth_points_kernel(
         if (mask & (1u << k)) {
             unsigned long long bits[3];
             const float cf = static_cast<float>(c), rf = static_cast<float>(r);
-            pixel_point(v, f, g, mode, pixel_class(v, cf, rf, d[k]), cf, rf, d[k], south, bits, flags);
+            const float dk = depth[p + k];
+            df w;
+            const int cls = pixel_class(v, cf, rf, dk, w);
+            pixel_point(v, smd, f, g, mode, cls, w, cf, rf, dk, south, bits, flags);
             unsigned long long *dst = out + 3 * slot;
             dst[0] = bits[0];
             dst[1] = bits[1];

@@ -208,13 +208,15 @@ __device__ __forceinline__ bool geo_fast(const GeoFast &f, const df (&enu)[3], u
         p[i][3] = __fmul_rn(p[i][2], s[i].hi);
         p[i][4] = __fmul_rn(p[i][2], p[i][2]);
     }
+    // monomials of degree 2..4 in the order of geo_monomial (compile-time exponents)
     float m[kGeoNl];
+    int j = 0;
 #pragma unroll
-    for (int j = 0; j < kGeoNl; ++j) {
-        int a, b, c;
-        geo_monomial(j, a, b, c);
-        m[j] = __fmul_rn(__fmul_rn(p[0][a], p[1][b]), p[2][c]);
-    }
+    for (int deg = 2; deg <= 4; ++deg)
+#pragma unroll
+        for (int x = deg; x >= 0; --x)
+#pragma unroll
+            for (int y = deg - x; y >= 0; --y) m[j++] = __fmul_rn(__fmul_rn(p[0][x], p[1][y]), p[2][deg - x - y]);
 #pragma unroll
     for (int o = 0; o < 3; ++o) {
         float nl = 0.0f;
@@ -224,6 +226,16 @@ __device__ __forceinline__ bool geo_fast(const GeoFast &f, const df (&enu)[3], u
         bits[o] = fx30_to_bits(f.c0[o] + fx30(v.hi) + fx30(v.lo));
     }
     return true;
+}
+
+// 1 / w in double-float: an approximate reciprocal refined by one Newton step whose residual
+// 1 - w q is formed exactly (two_prod; 1 - p.hi is exact for p.hi near 1): relative error
+// about the square of the first estimate's, below 2^-43.
+__device__ __forceinline__ df df_recip(df w) {
+    const float q = __fdividef(1.0f, w.hi);
+    const df p = two_prod(w.hi, q);
+    const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p.hi), p.lo), __fmul_rn(w.lo, q));
+    return fast_two_sum(q, __fmul_rn(q, e));
 }
 
 // ---- projective stage ---------------------------------------------------------------------
@@ -241,31 +253,66 @@ __device__ __forceinline__ df proj_row(const DepthView &v, int i, float col, flo
     return df_add(acc, df_mul_f(v.m[i][3], d));
 }
 
-// Row i of M [col, row, 1, d] in FP64 (rare path: volatile operations stay in their branch).
-__device__ __forceinline__ double proj_row_exact(const DepthView &v, int i, double col, double row, double d) {
-    return rare_dadd(rare_dadd(rare_dadd(rare_dmul(v.md[i][0], col), rare_dmul(v.md[i][1], row)), v.md[i][2]),
-                     rare_dmul(v.md[i][3], d));
-}
-
-// Pixel classes: 0 no point (depth <= 0 or NaN, or the homogeneous z is NaN); 1 fast
-// candidate (finite positive depth, non-zero homogeneous w: z is finite); 2 decided by FP64.
-__device__ __forceinline__ int pixel_class(const DepthView &v, float col, float row, float d) {
+// Pixel classes: 0 no point (depth <= 0 or NaN); 1 fast candidate (finite positive depth,
+// non-zero homogeneous w: z is finite, the pixel has a point); 2 decided by FP64 (infinite
+// depth or zero w).  w: the homogeneous w in double-float.
+__device__ __forceinline__ int pixel_class(const DepthView &v, float col, float row, float d, df &w) {
+    w = {0.0f, 0.0f};
     if (!(d > 0.0f)) return 0;
     if (d == __int_as_float(0x7f800000)) return 2;
-    const df w = proj_row(v, 3, col, row, d);
+    w = proj_row(v, 3, col, row, d);
     return w.hi != 0.0f ? 1 : 2;
 }
+__device__ __forceinline__ int pixel_class(const DepthView &v, float col, float row, float d) {
+    df w;
+    return pixel_class(v, col, row, d, w);
+}
 
-// FP64 ENU of a pixel; false when its homogeneous z is NaN (the reference drops it).
-__device__ __forceinline__ bool pixel_enu_exact(const DepthView &v, float col, float row, float d, double (&enu)[3]) {
-    const double c = rare_f2d(col), r = rare_f2d(row), dd = rare_f2d(d);
-    const double w = proj_row_exact(v, 3, c, r, dd);
-    const double z = rare_ddiv(proj_row_exact(v, 2, c, r, dd), w);
+// FP64 ENU of a pixel from the row-major matrix md; false when its homogeneous z is NaN
+// (the reference drops it).
+__device__ __forceinline__ double proj_row_exact(const double *md, int i, double col, double row, double d) {
+    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(md[4 * i], col), __dmul_rn(md[4 * i + 1], row)), md[4 * i + 2]),
+                     __dmul_rn(md[4 * i + 3], d));
+}
+
+__device__ __forceinline__ bool pixel_enu_exact(const double *md, float col, float row, float d, double (&enu)[3]) {
+    const double c = static_cast<double>(col), r = static_cast<double>(row), dd = static_cast<double>(d);
+    const double w = proj_row_exact(md, 3, c, r, dd);
+    const double z = __ddiv_rn(proj_row_exact(md, 2, c, r, dd), w);
     if (z != z) return false;
-    enu[0] = rare_ddiv(proj_row_exact(v, 0, c, r, dd), w);
-    enu[1] = rare_ddiv(proj_row_exact(v, 1, c, r, dd), w);
+    enu[0] = __ddiv_rn(proj_row_exact(md, 0, c, r, dd), w);
+    enu[1] = __ddiv_rn(proj_row_exact(md, 1, c, r, dd), w);
     enu[2] = z;
     return true;
+}
+
+// The FP64 path of one pixel (rare: outside the fast box, exact mode, class 2), kept out of
+// line so the fast path keeps its registers.  md: the view's FP64 matrix (shared memory).
+struct PixelBits {
+    unsigned long long e, n, a;
+    int ok;
+};
+static __device__ __noinline__ PixelBits pixel_point_exact(const double *md, const GeoFrame *g, float col, float row,
+                                                          float d, int cls, int south, int *flags) {
+    PixelBits out{0x7ff8000000000000ull, 0x7ff8000000000000ull, 0x7ff8000000000000ull, 1};
+    double enu[3];
+    if (!pixel_enu_exact(md, col, row, d, enu)) {
+        out.ok = cls == 2 ? 0 : 1;           // a class-1 pixel keeps its point (NaN coordinates)
+        return out;
+    }
+    double east, north, alt, lat;
+    geo_exact(g, enu[0], enu[1], enu[2], east, north, alt, lat);
+    if (flags && ((lat < 0.0) != (south != 0))) atomicOr(flags, VS_GEO_FLAG_HEMISPHERE);
+    out.e = static_cast<unsigned long long>(__double_as_longlong(east));
+    out.n = static_cast<unsigned long long>(__double_as_longlong(north));
+    out.a = static_cast<unsigned long long>(__double_as_longlong(alt));
+    return out;
+}
+
+// FP64 validity of a class-2 pixel.
+static __device__ __noinline__ bool pixel_valid_exact(const double *md, float col, float row, float d) {
+    double enu[3];
+    return pixel_enu_exact(md, col, row, d, enu);
 }
 
 // ---- per-pixel drivers shared by the points and the fused rasterisation kernels ------------
@@ -285,34 +332,32 @@ __device__ __forceinline__ void load_depths(const float *__restrict__ depth, lon
     }
 }
 
-// (easting, northing, altitude) bits of a pixel of class cls (1 or 2): the fast path when the
-// mode and plan allow it and the point lies in the plan's box, else the FP64 chain.  Returns
-// false when the pixel has no point (class 2 with a NaN homogeneous z).  A class-1 pixel
-// always has one (NaN coordinates in the degenerate case of a zero FP64 w).
-__device__ __forceinline__ bool pixel_point(const DepthView &v, const GeoFast &f, const GeoFrame *g, int mode, int cls,
-                                            float col, float row, float d, int south, unsigned long long (&bits)[3],
-                                            int *flags) {
+// (easting, northing, altitude) bits of a pixel of class cls (1 or 2) with homogeneous w:
+// the fast path when the mode and plan allow it and the point lies in the plan's box, else
+// the FP64 chain.  Returns false when the pixel has no point (class 2 with a NaN
+// homogeneous z).  A class-1 pixel always has one (NaN coordinates in the degenerate case of
+// a zero FP64 w).
+__device__ __forceinline__ bool pixel_point(const DepthView &v, const double *md, const GeoFast &f,
+                                            const GeoFrame *g, int mode, int cls, df w, float col, float row,
+                                            float d, int south, unsigned long long (&bits)[3], int *flags) {
     if (cls == 1 && mode == VS_GEO_FAST && f.enabled) {
-        const df w = proj_row(v, 3, col, row, d);
-        const df rw = df_div({1.0f, 0.0f}, w);
+        const df rw = df_recip(w);
         df enu[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) enu[i] = df_mul(proj_row(v, i, col, row, d), rw);
         if (geo_fast(f, enu, bits)) return true;
     }
-    double enu[3];
-    if (!pixel_enu_exact(v, col, row, d, enu)) {
-        if (cls == 2) return false;
-        bits[0] = bits[1] = bits[2] = 0x7ff8000000000000ull;
-        return true;
-    }
-    double east, north, alt, lat;
-    geo_exact(g, enu[0], enu[1], enu[2], east, north, alt, lat);
-    if (flags && ((lat < 0.0) != (south != 0))) atomicOr(flags, VS_GEO_FLAG_HEMISPHERE);
-    bits[0] = static_cast<unsigned long long>(__double_as_longlong(east));
-    bits[1] = static_cast<unsigned long long>(__double_as_longlong(north));
-    bits[2] = static_cast<unsigned long long>(__double_as_longlong(alt));
-    return true;
+    const PixelBits pb = pixel_point_exact(md, g, col, row, d, cls, south, flags);
+    bits[0] = pb.e;
+    bits[1] = pb.n;
+    bits[2] = pb.a;
+    return pb.ok != 0;
+}
+
+// The view's FP64 matrix in shared memory for the out-of-line FP64 path.
+__device__ __forceinline__ void stage_matrix(const DepthView &v, double *smd) {
+    if (threadIdx.x < 16) smd[threadIdx.x] = v.md[threadIdx.x >> 2][threadIdx.x & 3];
+    __syncthreads();
 }
 
 // Host side (geo.cu): frame constants, per-view matrices, plan accessors.

@@ -1436,23 +1436,25 @@ __global__ void __launch_bounds__(256) depth_bin_kernel(const float *__restrict_
                                                         int south, FastAxis ra, FastAxis ca, int view,
                                                         unsigned long long *__restrict__ vk,
                                                         unsigned long long *__restrict__ first, int *flags) {
+    __shared__ double smd[16];
+    stage_matrix(v, smd);
     const long long total = H * W;
     const unsigned long long tag = epoch_tag(view);
     const unsigned long long ncols = static_cast<unsigned>(ca.nm1 + 1);
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * kDepthPix;
     for (long long p = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kDepthPix; p < total;
          p += stride) {
-        float d[kDepthPix];
-        load_depths(depth, p, total, d);
         long long r = p / W, c = p - r * W;
         long long run_cell = -1;
         unsigned long long run_key = kEmptyKey;
 #pragma unroll 1
         for (int k = 0; k < kDepthPix; ++k) {
             const float cf = static_cast<float>(c), rf = static_cast<float>(r);
-            const int cls = pixel_class(v, cf, rf, d[k]);
+            const float dk = p + k < total ? __ldcs(depth + p + k) : -1.0f;
+            df w;
+            const int cls = pixel_class(v, cf, rf, dk, w);
             unsigned long long bits[3];
-            if (cls != 0 && pixel_point(v, f, g, mode, cls, cf, rf, d[k], south, bits, flags)) {
+            if (cls != 0 && pixel_point(v, smd, f, g, mode, cls, w, cf, rf, dk, south, bits, flags)) {
                 int rr, cc;
                 long long dr, dc;
                 bool sr, sc;
