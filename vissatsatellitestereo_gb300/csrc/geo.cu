@@ -214,16 +214,17 @@ __global__ void geodetic_to_utm_kernel(const GeoFrame *g, const double *__restri
 // Valid-pixel mask of a thread's 8 pixels (bit k: pixel p + k).
 __device__ __forceinline__ unsigned valid_mask(const DepthView &v, const double *smd, const float (&d)[kPixPerThread],
                                                long long p, long long W) {
-    long long r = p / W, c = p - r * W;
+    int r = static_cast<int>(p / W), c = static_cast<int>(p - (p / W) * W);
+    const int Wi = static_cast<int>(W);
     unsigned mask = 0;
 #pragma unroll
     for (int k = 0; k < kPixPerThread; ++k) {
-        const float cf = static_cast<float>(c), rf = static_cast<float>(r);
+        const float cf = __int2float_rn(c), rf = __int2float_rn(r);
         const int cls = pixel_class(v, cf, rf, d[k]);
         bool ok = cls == 1;
         if (cls == 2) ok = pixel_valid_exact(smd, cf, rf, d[k]);
         mask |= ok ? (1u << k) : 0u;
-        if (++c == W) {
+        if (++c == Wi) {
             c = 0;
             ++r;
         }
@@ -301,12 +302,13 @@ __global__ void __launch_bounds__(kPixThreads) depth_points_kernel(
     int before = 0;
     for (int w = 0; w < wid; ++w) before += warp_sum[w];
     long long slot = offsets[blockIdx.x] + before + incl - n;
-    long long r = p / W, c = p - r * W;
+    int r = static_cast<int>(p / W), c = static_cast<int>(p - (p / W) * W);
+    const int Wi = static_cast<int>(W);
 #pragma unroll 1
     for (int k = 0; k < kPixPerThread; ++k) {
         if (mask & (1u << k)) {
             unsigned long long bits[3];
-            const float cf = static_cast<float>(c), rf = static_cast<float>(r);
+            const float cf = __int2float_rn(c), rf = __int2float_rn(r);
             const float dk = depth[p + k];
             df w;
             const int cls = pixel_class(v, cf, rf, dk, w);
@@ -317,7 +319,7 @@ __global__ void __launch_bounds__(kPixThreads) depth_points_kernel(
             dst[2] = bits[2];
             ++slot;
         }
-        if (++c == W) {
+        if (++c == Wi) {
             c = 0;
             ++r;
         }

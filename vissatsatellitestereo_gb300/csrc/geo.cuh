@@ -180,11 +180,19 @@ __device__ __forceinline__ unsigned long long fx30_to_bits(long long S) {
     return sign | ((static_cast<unsigned long long>(p - kGeoFxBits + 1022) << 52) + mant);
 }
 
-// Sum of a double-float product list, lightly renormalised (three terms).
+// Double-float sum whose error is ~2^-48 of the operands' magnitudes (not of the result):
+// one TwoSum of the high parts, the low parts added plainly.  Here every sum's operands
+// are at most ~1e6 m, so the absolute error stays below ~1e-8 m.
+__device__ __forceinline__ df df_add_ops(df a, df b) {
+    const df s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+// Sum of three double-float products.
 __device__ __forceinline__ df df_dot3(const df (&c)[3], const df (&s)[3]) {
     df acc = df_mul(c[0], s[0]);
-    acc = df_add(acc, df_mul(c[1], s[1]));
-    return df_add(acc, df_mul(c[2], s[2]));
+    acc = df_add_ops(acc, df_mul(c[1], s[1]));
+    return df_add_ops(acc, df_mul(c[2], s[2]));
 }
 
 // (easting, northing, altitude) FP64 bits of an ENU point given in double-float.  Returns
@@ -245,12 +253,14 @@ struct DepthView {
     double md[4][4];
 };
 
-// Row i of M [col, row, 1, d] in double-float; col and row are exact floats.
+// Row i of M [col, row, 1, d] in double-float; col and row are exact floats.  The terms
+// reach ~1e6 (a camera centre hundreds of km away cancelling along the ray), so the sums'
+// operand-relative error of ~2^-48 is ~1e-9 m absolute.
 __device__ __forceinline__ df proj_row(const DepthView &v, int i, float col, float row, float d) {
     df acc = df_mul_f(v.m[i][0], col);
-    acc = df_add(acc, df_mul_f(v.m[i][1], row));
-    acc = df_add(acc, v.m[i][2]);
-    return df_add(acc, df_mul_f(v.m[i][3], d));
+    acc = df_add_ops(acc, df_mul_f(v.m[i][1], row));
+    acc = df_add_ops(acc, v.m[i][2]);
+    return df_add_ops(acc, df_mul_f(v.m[i][3], d));
 }
 
 // Pixel classes: 0 no point (depth <= 0 or NaN); 1 fast candidate (finite positive depth,

@@ -1442,14 +1442,25 @@ __global__ void __launch_bounds__(256) depth_bin_kernel(const float *__restrict_
     const unsigned long long tag = epoch_tag(view);
     const unsigned long long ncols = static_cast<unsigned>(ca.nm1 + 1);
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * kDepthPix;
-    for (long long p = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kDepthPix; p < total;
-         p += stride) {
-        long long r = p / W, c = p - r * W;
+    // pixel (row, col) of p kept incrementally in 32 bits (H, W < 2^24): no 64-bit division
+    // or 64-bit int -> float conversion per pixel
+    const long long p0 = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kDepthPix;
+    const int Wi = static_cast<int>(W);
+    const int stride_r = static_cast<int>(stride / W), stride_c = static_cast<int>(stride - (stride / W) * W);
+    int r0 = static_cast<int>(p0 / W), c0 = static_cast<int>(p0 - (p0 / W) * W);
+    for (long long p = p0; p < total; p += stride) {
+        int r = r0, c = c0;
+        float rf = __int2float_rn(r), cf = __int2float_rn(c);
+        r0 += stride_r;
+        c0 += stride_c;
+        if (c0 >= Wi) {
+            c0 -= Wi;
+            ++r0;
+        }
         long long run_cell = -1;
         unsigned long long run_key = kEmptyKey;
 #pragma unroll 1
         for (int k = 0; k < kDepthPix; ++k) {
-            const float cf = static_cast<float>(c), rf = static_cast<float>(r);
             const float dk = p + k < total ? __ldcs(depth + p + k) : -1.0f;
             df w;
             const int cls = pixel_class(v, cf, rf, dk, w);
@@ -1484,9 +1495,12 @@ __global__ void __launch_bounds__(256) depth_bin_kernel(const float *__restrict_
                     }
                 }
             }
-            if (++c == W) {
+            cf = __fadd_rn(cf, 1.0f);
+            if (++c == Wi) {
                 c = 0;
+                cf = 0.0f;
                 ++r;
+                rf = __fadd_rn(rf, 1.0f);
             }
         }
         if (run_key != kEmptyKey) atomicMax(vk + run_cell, run_key);
