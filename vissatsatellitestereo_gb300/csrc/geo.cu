@@ -84,8 +84,11 @@ __global__ void geo_nodes_kernel(GeoPlanDev *p) {
 __global__ void geo_fit_kernel(GeoPlanDev *p) {
     __shared__ double cheb[3][kCheb];
     __shared__ double mono[3][kCheb];
+    __shared__ double tj[kNodes][kNodes];        // T_a(x_j) = cos(a theta_j)
     const int centre = (2 * kNodes + 2) * kNodes + 2;
     const int t = threadIdx.x;
+    if (t < kNodes * kNodes) tj[t / kNodes][t % kNodes] = cos((t / kNodes) * kPi * ((t % kNodes) + 0.5) / kNodes);
+    __syncthreads();
     if (t < 3 * kCheb) {
         const int o = t / kCheb, k = t % kCheb;
         int a, b, c;
@@ -94,8 +97,7 @@ __global__ void geo_fit_kernel(GeoPlanDev *p) {
         double s = 0.0;
         for (int q = 0; q < kNodeCount; ++q) {
             const int j0 = q / (kNodes * kNodes), j1 = (q / kNodes) % kNodes, j2 = q % kNodes;
-            const double th0 = kPi * (j0 + 0.5) / kNodes, th1 = kPi * (j1 + 0.5) / kNodes, th2 = kPi * (j2 + 0.5) / kNodes;
-            s += (p->nodes[o][q] - ref) * cos(a * th0) * cos(b * th1) * cos(c * th2);
+            s += (p->nodes[o][q] - ref) * tj[a][j0] * tj[b][j1] * tj[c][j2];
         }
         const double w = (a ? 2.0 : 1.0) * (b ? 2.0 : 1.0) * (c ? 2.0 : 1.0) / kNodeCount;
         cheb[o][k] = s * w;
