@@ -166,32 +166,55 @@ def run_ours(args):
     from vissatsatellitestereo_gb300 import _lib
     main = torch.cuda.current_stream()
     s_fit, s_epi = torch.cuda.Stream(), torch.cuda.Stream()
-    sched = [s_epi]           # epilogue stream of the rasterisation (the main stream: serial)
+    s_hi, s_epi_hi = torch.cuda.Stream(priority=-1), torch.cuda.Stream(priority=-1)   # high priority
+    # schedules: the rasterisation's stream, its epilogue stream (None: the same, serial), and
+    # whether the fit starts with the rasterisation or after it (then overlapping the fusion)
+    SCHEDULES = {
+        'fit_concurrent': dict(ras=main, epi=s_epi, late=False),
+        'fit_concurrent_raster_high_priority': dict(ras=s_hi, epi=s_epi_hi, late=False),
+        'fit_concurrent_raster_high_priority_serial_epilogues': dict(ras=s_hi, epi=None, late=False),
+        'fit_after_raster_with_fusion': dict(ras=main, epi=s_epi, late=True),
+    }
+    sched = [SCHEDULES['fit_concurrent']]
     cams_t = torch.from_numpy(_lib.camera_array(wl.metas)).to(dev)
 
     def fit():
         return approx_perspective_enu(cams_t, grid_t['lat'], grid_t['lon'], grid_t['alt'], grid_t['x'],
                                       grid_t['y'], grid_t['z'], mode='fast', shared_points=False)
 
-    def step(ev=None):
-        if ev: ev['t0'].record()
-        s_fit.wait_stream(main)
+    def run_fit(ev):
         with torch.cuda.stream(s_fit):
             if ev: ev['f0'].record()
             out = fit()
             if ev: ev['f1'].record()
-        dsm_from_points(points, offsets, *gargs, out=dsms, epilogue_stream=sched[0],
-                        bin_events=ev['bins'] if ev else None)
-        if ev: ev['r1'].record()
-        fuse_dsms(dsms, median_blur=True, layout='vhw', out=fused)
-        if ev: ev['u1'].record()
+        return out
+
+    def step(ev=None):
+        cfg = sched[0]
+        ras = cfg['ras']
+        if ev: ev['t0'].record()
+        s_fit.wait_stream(main)
+        if ras is not main:
+            ras.wait_stream(main)
+        out = None if cfg['late'] else run_fit(ev)
+        with torch.cuda.stream(ras):
+            dsm_from_points(points, offsets, *gargs, out=dsms, epilogue_stream=cfg['epi'] or ras,
+                            bin_events=ev['bins'] if ev else None)
+            if ev: ev['r1'].record()
+            if cfg['late']:
+                s_fit.wait_stream(ras)
+                out = run_fit(ev)
+            fuse_dsms(dsms, median_blur=True, layout='vhw', out=fused)
+            if ev: ev['u1'].record()
+        if ras is not main:
+            main.wait_stream(ras)
         main.wait_stream(s_fit)
         if ev: ev['t1'].record()
         return out
 
-    def raster_schedule_ms(epi, reps=3):
+    def raster_schedule_ms(cfg, reps=3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        sched[0] = epi
+        sched[0] = cfg
         step()
         torch.cuda.synchronize()
         e0.record()
@@ -209,9 +232,10 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         step()
-    # epilogues overlapped on their own stream, or serial after each binning: keep the faster
-    sched_ms = {'overlapped': raster_schedule_ms(s_epi), 'serial': raster_schedule_ms(main)}
-    sched[0] = s_epi if sched_ms['overlapped'] <= sched_ms['serial'] else main
+    # the schedules above, each timed over a few steps: keep the fastest
+    sched_ms = {name: raster_schedule_ms(cfg) for name, cfg in SCHEDULES.items()}
+    best = min(sched_ms, key=sched_ms.get)
+    sched[0] = SCHEDULES[best]
     torch.cuda.synchronize()
     replicas.barrier()
     clocks = ClockSampler(local)
@@ -311,10 +335,8 @@ def run_ours(args):
         'rpc_pts_per_s': wl.rpc_points_per_step * args.steps * world / elapsed,
         'raster_pts_per_s': wl.views * n_pts * args.steps * world / elapsed,
         'stages_ms': stages, 'fit_status_ok': bool(np.all(status_np == 0)),
-        'schedule': 'camera fit on a second stream concurrent with the rasterisation; per-view epilogues '
-                    + ('on a third stream overlapped with the next binning' if sched[0] is s_epi
-                       else 'after each binning on the same stream') + ' (the faster of the two, measured at start)',
-        'raster_schedule_ms': {k: round(v, 3) for k, v in sched_ms.items()},
+        'schedule': best + ' (the fastest of the schedules timed before the timed steps)',
+        'schedule_ms': {k: round(v, 3) for k, v in sched_ms.items()},
         'serial_ms_per_step': serial_ms,
         'roofline': roofline, 'clocks': clock_info, 'gpu_launches': launches_per_step(wl.views) * args.steps,
     }
