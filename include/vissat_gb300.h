@@ -213,6 +213,18 @@ int vs_dsm_from_points_overlap(const double *points, const int64_t *offsets, int
                                int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
                                void *stream, void *epilogue_stream, void *const *bin_events);
 
+/* vs_dsm_from_points with the points in HOST memory (the reference's numpy arrays; pinned
+ * memory lets the copies overlap the binning): view v's points are copied into staging
+ * buffer v % ring (ring 1..8, device buffers in the workspace) on `copy_stream` while the
+ * earlier views are binned on `stream`.  host_offsets: host int64 [n_views + 1].  Same
+ * results as vs_dsm_from_points; when the call's work on `stream` completes, so have the
+ * copies.  The host buffers must stay unchanged until then. */
+size_t vs_dsm_from_points_host_workspace_size(int64_t max_view_points, int ring, int64_t xsize, int64_t ysize);
+int vs_dsm_from_points_host(const double *host_points, const int64_t *host_offsets, int n_views, double xoff,
+                            double yoff, double xresolution, double yresolution, int64_t xsize, int64_t ysize,
+                            float *dsm, int ring, void *workspace, size_t workspace_bytes, void *stream,
+                            void *copy_stream);
+
 /* ---- (c') batched form: many AOIs, per-view FP32 height maps ----------------------------
  * The per-view point lists of aggregate_2p5d_util.py:75-98 (pixel -> UTM of a height map)
  * feeding produce_dsm_from_points (produce_dsm.py:46-58) and the per-AOI fusion of

@@ -268,6 +268,31 @@ def test_dsm_from_points_overlap_matches_serial_and_oracle():
         assert (over[v] == 0).any()
 
 
+def test_dsm_from_points_host_pipeline_equals_device_path():
+    """Host points copied view by view into a 3-buffer device ring on a second stream
+    (vs_dsm_from_points_host): bit-identical to the device-input call, with an empty view, a
+    one-point view, odd view offsets and more views than ring buffers."""
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    grid = synth.DsmGrid(synth.EXPLORER_UL_EASTING, synth.EXPLORER_UL_NORTHING, 0.3, 0.3, 180, 150)
+    scene = synth.make_scene(81, grid, 25, 3.0, 80.0)
+    views = synth.make_views(82, scene, 6, 200, 230, 0.1, 0.3, 0.5)
+    clouds = [synth.view_points(scene, v) for v in views]
+    clouds[1] = clouds[1][:0]
+    clouds[2] = clouds[2][:1]
+    clouds[4] = clouds[4][:-3]
+    offsets = np.cumsum([0] + [len(c) for c in clouds])
+    pts = np.concatenate(clouds)
+    args = (grid.xoff, grid.yoff, grid.xres, grid.yres, grid.xsize, grid.ysize)
+    dev = dsm_from_points(torch.from_numpy(pts).cuda(), torch.from_numpy(offsets).cuda(), *args)
+    pinned = torch.from_numpy(pts).pin_memory()
+    host = dsm_from_points(pinned, torch.from_numpy(offsets), *args)
+    torch.cuda.synchronize()
+    assert same_bits(host.cpu().numpy(), dev.cpu().numpy())
+    assert np.isnan(host[1].cpu().numpy()).all()
+
+
 def test_median_blur_matches_oracle():
     from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3
     rng = np.random.default_rng(3)

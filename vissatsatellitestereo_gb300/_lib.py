@@ -85,6 +85,9 @@ SIGNATURES = {
     'vs_fuse_dsms_workspace_size': (_sz, [_i64, _i64]),
     'vs_fuse_dsms': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp, _sz, _vp]),
     'vs_fuse_dsms_static': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp]),
+    'vs_dsm_from_points_host_workspace_size': (_sz, [_i64, _int, _i64, _i64]),
+    'vs_dsm_from_points_host': (_int, [_vp, _vp, _int, _dbl, _dbl, _dbl, _dbl, _i64, _i64, _vp, _int, _vp, _sz, _vp,
+                                       _vp]),
     'vs_geo_plan_device_bytes': (_sz, []),
     'vs_geo_plan_create': (_int, [_vp, _vp, _sz, _vp, _vp]),
     'vs_geo_plan_query': (_int, [_vp, _vp, _vp]),

@@ -1040,6 +1040,107 @@ int event_ring(EventRing *&out) {
 }  // namespace
 }  // namespace vs
 
+// Points in host memory: view v's points are copied into staging buffer v % ring on
+// copy_stream while earlier views are binned on `stream`; an event per buffer orders the
+// copy after the previous user of the buffer (its binning and epilogue) and the binning
+// after the copy.  Per view the binning runs on the buffer as a one-view list (local point
+// indices, the view's epoch tag), the epilogue resolves zeros from the same buffer, so the
+// results equal vs_dsm_from_points.
+static size_t host_ring_bytes(int64_t max_view_points, int ring) {
+    return static_cast<size_t>(ring) * ((static_cast<size_t>(max_view_points) * 24 + 255) & ~size_t(255));
+}
+
+extern "C" size_t vs_dsm_from_points_host_workspace_size(int64_t max_view_points, int ring, int64_t xsize,
+                                                          int64_t ysize) {
+    if (max_view_points < 0 || ring < 1 || xsize <= 0 || ysize <= 0) return 0;
+    return carve_raster(nullptr, xsize, ysize, true).bytes + 256 + host_ring_bytes(max_view_points, ring);
+}
+
+extern "C" int vs_dsm_from_points_host(const double *host_points, const int64_t *host_offsets, int n_views,
+                                       double xoff, double yoff, double xresolution, double yresolution,
+                                       int64_t xsize, int64_t ysize, float *dsm, int ring, void *workspace,
+                                       size_t workspace_bytes, void *stream, void *copy_stream) {
+    VS_REQUIRE(n_views > 0 && n_views < (1 << 23) && grid_ok(xsize, ysize) && ring >= 1 && ring <= 8,
+               "vs_dsm_from_points_host: bad sizes views=%d grid=%lldx%lld ring=%d", n_views, (long long)xsize,
+               (long long)ysize, ring);
+    VS_REQUIRE(host_offsets && dsm && workspace, "vs_dsm_from_points_host: null pointer");
+    long long max_pts = 0;
+    for (int v = 0; v < n_views; ++v) {
+        const long long cnt = host_offsets[v + 1] - host_offsets[v];
+        VS_REQUIRE(cnt >= 0 && host_offsets[v] >= 0 && cnt < (1LL << 40), "vs_dsm_from_points_host: bad offsets");
+        max_pts = std::max(max_pts, cnt);
+    }
+    VS_REQUIRE(host_points || max_pts == 0, "vs_dsm_from_points_host: null points");
+    const size_t need = vs_dsm_from_points_host_workspace_size(max_pts, ring, xsize, ysize);
+    if (workspace_bytes < need) {
+        set_error("vs_dsm_from_points_host: workspace %zu < %zu bytes", workspace_bytes, need);
+        return VS_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream), cs = as_stream(copy_stream);
+    RasterWs w = carve_raster(workspace, xsize, ysize, true);
+    const size_t slot = (static_cast<size_t>(max_pts) * 24 + 255) & ~size_t(255);
+    char *ring_base = static_cast<char *>(workspace) + ((w.bytes + 255) & ~size_t(255));
+    Tables tb;
+    const long long cells = xsize * ysize;
+    int s = make_tables(xoff, yoff, xresolution, yresolution, xsize, ysize, w, tb, st);
+    if (s == VS_OK) s = clear(w.keys[0], sizeof(unsigned long long) * cells, st);
+    if (s == VS_OK) s = clear(w.first, sizeof(unsigned long long) * cells, st);
+    if (s != VS_OK) return s;
+    cudaEvent_t freed[8], landed[8];
+    int made = 0;
+    for (; made < ring; ++made) {
+        if (cudaEventCreateWithFlags(&freed[made], cudaEventDisableTiming) != cudaSuccess) break;
+        if (cudaEventCreateWithFlags(&landed[made], cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventDestroy(freed[made]);
+            break;
+        }
+    }
+    if (made < ring) {
+        for (int i = 0; i < made; ++i) {
+            cudaEventDestroy(freed[i]);
+            cudaEventDestroy(landed[i]);
+        }
+        set_error("vs_dsm_from_points_host: cudaEventCreate failed");
+        return VS_ERR_CUDA;
+    }
+    const dim3 egrid(static_cast<unsigned>(ceil_div(xsize, TX)), static_cast<unsigned>(ceil_div(ysize, TILE_Y)));
+    // the copy stream starts after the work already queued on `stream` (tables, clears)
+    if (cudaEventRecord(freed[0], st) != cudaSuccess || cudaStreamWaitEvent(cs, freed[0], 0) != cudaSuccess)
+        s = VS_ERR_CUDA;
+    for (int v = 0; v < n_views && s == VS_OK; ++v) {
+        const int b = v % ring;
+        const long long cnt = host_offsets[v + 1] - host_offsets[v];
+        double *buf = reinterpret_cast<double *>(ring_base + b * slot);
+        if (v >= ring && cudaStreamWaitEvent(cs, freed[b], 0) != cudaSuccess) s = VS_ERR_CUDA;
+        if (s == VS_OK && cnt > 0 &&
+            cudaMemcpyAsync(buf, host_points + 3 * host_offsets[v], static_cast<size_t>(cnt) * 24,
+                            cudaMemcpyHostToDevice, cs) != cudaSuccess)
+            s = VS_ERR_CUDA;
+        if (s == VS_OK && (cudaEventRecord(landed[b], cs) != cudaSuccess ||
+                           cudaStreamWaitEvent(st, landed[b], 0) != cudaSuccess))
+            s = VS_ERR_CUDA;
+        if (s != VS_OK) {
+            set_error("vs_dsm_from_points_host: copy or event call failed at view %d", v);
+            break;
+        }
+        unsigned long long *cur = w.keys[v & 1], *nxt = (v + 1 < n_views) ? w.keys[(v + 1) & 1] : nullptr;
+        if ((s = bin_launch(buf, nullptr, v, cnt, cnt, tb, cur, w.first, st)) != VS_OK) break;
+        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(cur, w.first, buf, dsm + v * cells, nxt,
+                                                            static_cast<int>(ysize), static_cast<int>(xsize));
+        if ((s = check_launch("dsm_epilogue_kernel")) != VS_OK) break;
+        if (cudaEventRecord(freed[b], st) != cudaSuccess) {
+            set_error("vs_dsm_from_points_host: cudaEventRecord failed");
+            s = VS_ERR_CUDA;
+        }
+    }
+    // `stream` covers the copies too (every copy is waited for by a binning on `stream`)
+    for (int i = 0; i < ring; ++i) {
+        cudaEventDestroy(freed[i]);
+        cudaEventDestroy(landed[i]);
+    }
+    return s;
+}
+
 extern "C" size_t vs_dsm_from_points_overlap_workspace_size(int n_views, int64_t xsize, int64_t ysize) {
     if (n_views <= 0 || xsize <= 0 || ysize <= 0) return 0;
     return carve_overlap(nullptr, xsize, ysize).bytes + 256;
