@@ -137,6 +137,24 @@ __device__ __forceinline__ df df_div(df a, df b) {
     float q2 = __fdiv_rn(r.hi, b.hi);
     return fast_two_sum(q1, q2);
 }
+// Double-float sum whose error is ~2^-48 of the operands' magnitudes (not of the result):
+// one TwoSum of the high parts, the low parts added plainly.  For sums whose accuracy
+// budget is absolute in the operands' scale (cancellation harmless).
+__device__ __forceinline__ df df_add_ops(df a, df b) {
+    const df s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+// 1 / w in double-float: an approximate reciprocal refined by one Newton step whose residual
+// 1 - w q is formed exactly (two_prod; 1 - p.hi is exact for p.hi near 1): relative error
+// about the square of the first estimate's, below 2^-43.
+__device__ __forceinline__ df df_recip(df w) {
+    const float q = __fdividef(1.0f, w.hi);
+    const df p = two_prod(w.hi, q);
+    const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p.hi), p.lo), __fmul_rn(w.lo, q));
+    return fast_two_sum(q, __fmul_rn(q, e));
+}
+
 __host__ __device__ inline df df_from_double(double v) {
     float hi = static_cast<float>(v);
     return {hi, static_cast<float>(v - static_cast<double>(hi))};

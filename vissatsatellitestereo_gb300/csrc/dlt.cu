@@ -241,7 +241,7 @@ __device__ __forceinline__ void normalised_point(const NormF &nf, double X, doub
 // Moments of the kept points of view v.  Block b owns points [b * 128 * kChunk, ...);
 // (col, row) come as FP64 arrays (drop-in fit) or as the double-floats of the projection
 // pass (fused camera path, in-image mask from the image size).
-__global__ void __launch_bounds__(kMomThreads) moments_kernel(
+__global__ void __launch_bounds__(kMomThreads, 6) moments_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
     const double *__restrict__ col, const double *__restrict__ row, const float4 *__restrict__ colrow,
     const uint8_t *__restrict__ keep, const float *__restrict__ wh, long long n, const Norm *__restrict__ norm,
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kMomThreads) moments_kernel(
     float count = 0.0f;
     const long long base = static_cast<long long>(blockIdx.x) * kMomThreads * kChunk + threadIdx.x;
     // groups of kAhead points: all loads of a group are issued before its arithmetic
-    constexpr int kAhead = 4;
+    constexpr int kAhead = 2;
 #pragma unroll 1
     for (int j0 = 0; j0 < kChunk; j0 += kAhead) {
         double X[kAhead], Y[kAhead], Z[kAhead];
@@ -685,7 +685,7 @@ __device__ __forceinline__ df dot2(const df *q, float x, float y, float z) {
 //    its own projection, cam = h2 K^-1 [c^ r^ 1], so the distance is
 //    |h2| |delta x d| / |d| with delta = K^-1 [c^ - c, r^ - r, 0]: the pixel residual
 //    enters directly and nothing of the camera's ~1e5-1e6 m depth cancels.
-__global__ void __launch_bounds__(kErrThreads, 3) error_points_kernel(
+__global__ void __launch_bounds__(kErrThreads, 4) error_points_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
     const double *__restrict__ col, const double *__restrict__ row, const float4 *__restrict__ colrow,
     const uint8_t *__restrict__ keep, long long n, const ErrCam *__restrict__ cams, ErrWs w) {

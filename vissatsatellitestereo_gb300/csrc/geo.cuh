@@ -180,14 +180,6 @@ __device__ __forceinline__ unsigned long long fx30_to_bits(long long S) {
     return sign | ((static_cast<unsigned long long>(p - kGeoFxBits + 1022) << 52) + mant);
 }
 
-// Double-float sum whose error is ~2^-48 of the operands' magnitudes (not of the result):
-// one TwoSum of the high parts, the low parts added plainly.  Here every sum's operands
-// are at most ~1e6 m, so the absolute error stays below ~1e-8 m.
-__device__ __forceinline__ df df_add_ops(df a, df b) {
-    const df s = two_sum(a.hi, b.hi);
-    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
-}
-
 // Sum of three double-float products.
 __device__ __forceinline__ df df_dot3(const df (&c)[3], const df (&s)[3]) {
     df acc = df_mul(c[0], s[0]);
@@ -234,16 +226,6 @@ __device__ __forceinline__ bool geo_fast(const GeoFast &f, const df (&enu)[3], u
         bits[o] = fx30_to_bits(f.c0[o] + fx30(v.hi) + fx30(v.lo));
     }
     return true;
-}
-
-// 1 / w in double-float: an approximate reciprocal refined by one Newton step whose residual
-// 1 - w q is formed exactly (two_prod; 1 - p.hi is exact for p.hi near 1): relative error
-// about the square of the first estimate's, below 2^-43.
-__device__ __forceinline__ df df_recip(df w) {
-    const float q = __fdividef(1.0f, w.hi);
-    const df p = two_prod(w.hi, q);
-    const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p.hi), p.lo), __fmul_rn(w.lo, q));
-    return fast_two_sum(q, __fmul_rn(q, e));
 }
 
 // ---- projective stage ---------------------------------------------------------------------

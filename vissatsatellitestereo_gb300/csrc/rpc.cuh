@@ -129,8 +129,10 @@ __device__ __forceinline__ void monomials(float x, float y, float z, float (&m)[
     m[15] = zz * z;      // z^3
 }
 
+// (v - off) * inv: the difference's error is ~2^-48 of |v| (a few 1e-13 degrees), far below
+// what the 1e-4 px bound allows after the scale.
 __device__ __forceinline__ df normalise(df v, df off, df inv) {
-    return df_mul(df_add(v, {-off.hi, -off.lo}), inv);
+    return df_mul(df_add_ops(v, {-off.hi, -off.lo}), inv);
 }
 
 // (col, row) as double-floats for one point given as split lat/lon/alt.
@@ -144,8 +146,9 @@ __device__ __forceinline__ void project_fast(const RpcFast &c, df lat, df lon, d
     const df cd = poly_fast(c.lin[1], c.hot[1], x, y, z, m);
     const df rn = poly_fast(c.lin[2], c.hot[2], x, y, z, m);
     const df rd = poly_fast(c.lin[3], c.hot[3], x, y, z, m);
-    col = df_add(df_mul(df_div(cn, cd), c.col_scale), c.col_off);
-    row = df_add(df_mul(df_div(rn, rd), c.row_scale), c.row_off);
+    // quotients through a Newton-refined reciprocal (relative error < 2^-43)
+    col = df_add_ops(df_mul(df_mul(cn, df_recip(cd)), c.col_scale), c.col_off);
+    row = df_add_ops(df_mul(df_mul(rn, df_recip(rd)), c.row_scale), c.row_off);
 }
 
 // df < float bound, for the in-image mask (col >= 0, col < width)
