@@ -547,7 +547,13 @@ __global__ void __launch_bounds__(64) solve_kernel(const double *__restrict__ pa
         mom[threadIdx.x] = s;
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
+    // warp 0 solves; lane 0 keeps the serial parts (maps, factorisation, outputs), the
+    // Cholesky factor and the triangular solves run across lanes 0..11 (one row each)
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    __shared__ double G[12][12];
+    __shared__ double vec[3][12];          // p, u, w
+    __shared__ double s_floor;
     const Norm nm = norm[v];
     const double count = mom[kMom];
     double K[9], R[9], t[3];
@@ -558,62 +564,84 @@ __global__ void __launch_bounds__(64) solve_kernel(const double *__restrict__ pa
     double P[12];
     if (st == VS_OK) {
         // normalised Gram matrix G = [[S0,0,-Sc],[0,S0,-Sr],[-Sc,-Sr,Sq]]
-        double G[12][12];
-        const int ent[10][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {1, 1}, {1, 2}, {1, 3}, {2, 2}, {2, 3}, {3, 3}};
-        for (int i = 0; i < 12; ++i)
-            for (int j = 0; j < 12; ++j) G[i][j] = 0.0;
-        for (int e = 0; e < 10; ++e) {
-            const int a = ent[e][0], b = ent[e][1];
-            const double s0 = mom[e], sc = mom[10 + e], sr = mom[20 + e], sq = mom[30 + e];
-            G[a][b] = G[b][a] = s0;
-            G[4 + a][4 + b] = G[4 + b][4 + a] = s0;
-            G[a][8 + b] = G[b][8 + a] = G[8 + a][b] = G[8 + b][a] = -sc;
-            G[4 + a][8 + b] = G[4 + b][8 + a] = G[8 + a][4 + b] = G[8 + b][4 + a] = -sr;
-            G[8 + a][8 + b] = G[8 + b][8 + a] = sq;
-        }
-        // Cholesky G = L L^T (a non-positive pivot -- an exactly consistent system -- is
-        // floored; the inverse iteration then lands on the null vector)
-        double dmax = 0.0;
-        for (int i = 0; i < 12; ++i) dmax = fmax(dmax, G[i][i]);
-        const double floor_piv = dmax * 1e-30 + 1e-300;
-        for (int j = 0; j < 12; ++j) {
-            double d = G[j][j];
-            for (int k = 0; k < j; ++k) d -= G[j][k] * G[j][k];
-            d = d > floor_piv ? d : floor_piv;
-            const double l = sqrt(d);
-            G[j][j] = l;
-            for (int i = j + 1; i < 12; ++i) {
-                double s = G[i][j];
-                for (int k = 0; k < j; ++k) s -= G[i][k] * G[j][k];
-                G[i][j] = s / l;
+        if (lane == 0) {
+            const int ent[10][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {1, 1}, {1, 2}, {1, 3}, {2, 2}, {2, 3}, {3, 3}};
+            for (int i = 0; i < 12; ++i)
+                for (int j = 0; j < 12; ++j) G[i][j] = 0.0;
+            for (int e = 0; e < 10; ++e) {
+                const int a = ent[e][0], b = ent[e][1];
+                const double s0 = mom[e], sc = mom[10 + e], sr = mom[20 + e], sq = mom[30 + e];
+                G[a][b] = G[b][a] = s0;
+                G[4 + a][4 + b] = G[4 + b][4 + a] = s0;
+                G[a][8 + b] = G[b][8 + a] = G[8 + a][b] = G[8 + b][a] = -sc;
+                G[4 + a][8 + b] = G[4 + b][8 + a] = G[8 + a][4 + b] = G[8 + b][4 + a] = -sr;
+                G[8 + a][8 + b] = G[8 + b][8 + a] = sq;
             }
+            double dmax = 0.0;
+            for (int i = 0; i < 12; ++i) dmax = fmax(dmax, G[i][i]);
+            s_floor = dmax * 1e-30 + 1e-300;
+        }
+        __syncwarp();
+        // Cholesky G = L L^T, column by column (a non-positive pivot -- an exactly
+        // consistent system -- is floored; the inverse iteration then lands on the null
+        // vector).  Every element keeps the serial operation order.
+        const double floor_piv = s_floor;
+        for (int j = 0; j < 12; ++j) {
+            if (lane == j) {
+                double d = G[j][j];
+                for (int k = 0; k < j; ++k) d -= G[j][k] * G[j][k];
+                d = d > floor_piv ? d : floor_piv;
+                G[j][j] = sqrt(d);
+            }
+            __syncwarp();
+            if (lane > j && lane < 12) {
+                double sum = G[lane][j];
+                for (int k = 0; k < j; ++k) sum -= G[lane][k] * G[j][k];
+                G[lane][j] = sum / G[j][j];
+            }
+            __syncwarp();
         }
         const Mmap mm{nm.cx, nm.cy, nm.cz, nm.s, nm.c0, nm.r0, nm.sp};
-        double p[12], u[12], w[12];
-        for (int i = 0; i < 12; ++i) p[i] = 0.28867513459481287;   // 1/sqrt(12)
+        if (lane < 12) vec[0][lane] = 0.28867513459481287;   // 1/sqrt(12)
+        __syncwarp();
         for (int it = 0; it < 6; ++it) {
-            solve_mt(mm, p, u);
-            for (int i = 0; i < 12; ++i) {          // L w = u
-                double s = u[i];
-                for (int k = 0; k < i; ++k) s -= G[i][k] * w[k];
-                w[i] = s / G[i][i];
+            if (lane == 0) solve_mt(mm, vec[0], vec[1]);
+            __syncwarp();
+            // L w = u: lane i subtracts w[j] L[i][j] as each w[j] is formed
+            double sum = lane < 12 ? vec[1][lane] : 0.0;
+            for (int j = 0; j < 12; ++j) {
+                if (lane == j) vec[2][j] = sum / G[j][j];
+                __syncwarp();
+                if (lane > j && lane < 12) sum -= G[lane][j] * vec[2][j];
             }
-            for (int i = 11; i >= 0; --i) {         // L^T u = w
-                double s = w[i];
-                for (int k = i + 1; k < 12; ++k) s -= G[k][i] * u[k];
-                u[i] = s / G[i][i];
+            __syncwarp();
+            // L^T u = w
+            sum = lane < 12 ? vec[2][lane] : 0.0;
+            for (int j = 11; j >= 0; --j) {
+                if (lane == j) vec[1][j] = sum / G[j][j];
+                __syncwarp();
+                if (lane < j) sum -= G[j][lane] * vec[1][j];
             }
-            solve_m(mm, u, p);
-            double nrm = 0.0;
-            for (int i = 0; i < 12; ++i) nrm += p[i] * p[i];
-            nrm = 1.0 / sqrt(nrm);
-            for (int i = 0; i < 12; ++i) p[i] *= nrm;
+            __syncwarp();
+            if (lane == 0) {
+                double pp[12];
+                solve_m(mm, vec[1], pp);
+                double nrm = 0.0;
+                for (int i = 0; i < 12; ++i) nrm += pp[i] * pp[i];
+                nrm = 1.0 / sqrt(nrm);
+                for (int i = 0; i < 12; ++i) vec[0][i] = pp[i] * nrm;
+            }
+            __syncwarp();
         }
+        if (lane != 0) return;
+        double p[12];
+        for (int i = 0; i < 12; ++i) p[i] = vec[0][i];
         for (int i = 0; i < 12; ++i) P[i] = p[i];
         bool finite = true;
         for (int i = 0; i < 12; ++i) finite &= isfinite(P[i]);
         st = finite ? factorize(P, K, R, t) : VS_ERR_DEGENERATE;
     }
+    if (lane != 0) return;
     for (int i = 0; i < 9; ++i) K_out[v * 9 + i] = K[i], R_out[v * 9 + i] = R[i];
     for (int i = 0; i < 3; ++i) t_out[v * 3 + i] = t[i];
     status[v] = st;
