@@ -1,4 +1,5 @@
-"""On-disk formats of the path's results: PLY point clouds and GeoTIFF DSMs.
+"""On-disk formats around the path: PLY point clouds, GeoTIFF DSMs, COLMAP dense arrays and
+the inverse projection matrices.
 
 * ``np2ply`` -- lib/ply_np_converter.py:38-67.  Binary output is byte-identical to the
   reference's (its vendored plyfile, little endian): the header lines, float32 (or
@@ -12,6 +13,12 @@
   AREA_OR_POINT=Area (PixelIsArea).  NaN is written as ``nodata_val`` when given; the
   reader turns values close to the nodata value back into NaN (np.isclose, as the
   reference) and returns the reference's meta dict fields.
+
+* ``read_array`` / ``write_array`` -- colmap/read_dense.py:36-51: COLMAP's dense arrays
+  (depth and normal maps), an ASCII "width&height&channels&" header and float32 values in
+  column-major order; the reader returns the reference's (height, width[, channels]).
+* ``read_inv_proj_mats`` / ``write_inv_proj_mats`` -- aggregate_2p5d_util.py:55-61: one
+  line per image, its name and the 16 values of its 4x4 inverse projection matrix.
 
 Device tensors are accepted and copied to the host once.
 """
