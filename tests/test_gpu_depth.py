@@ -162,3 +162,44 @@ def test_fused_dsm_on_a_grid_across_a_binade_falls_back():
     ref = median_blur3x3(proj_to_grid(pts, *grid).astype(np.float32))
     assert same_bits(out[0].cpu().numpy(), ref)
     assert np.isfinite(ref).mean() > 0.5
+
+
+def test_equator_straddling_aoi_asserts_like_the_reference():
+    """The reference asserts that all points lie in one hemisphere
+    (lib/latlon_utm_converter.py:40); an AOI across the equator raises the same way, and
+    its plan keeps the fast path off (the box spans both hemispheres)."""
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.aggregate_2p5d_util import depth_map_to_points
+    from vissatsatellitestereo_gb300.coordinate_system import aoi_enu_box, aoi_origin, plan_for
+    case = synth.make_depth_case(27, 1, 64, 64, _utm, aoi_m=400.0, lat0=0.0005, lon0=10.0, n_boxes=5)
+    plan = plan_for(*aoi_origin(case.aoi), case.aoi['zone_number'], False, aoi_enu_box(case.aoi))
+    assert not plan.fast_enabled
+    with pytest.raises(AssertionError):
+        depth_map_to_points(synth.depth_map_torch(case, 0).numpy(), case.inv_proj[0], case.aoi)
+
+
+def test_depth_entry_points_reject_bad_arguments():
+    import ctypes
+    from vissatsatellitestereo_gb300 import _lib, synth
+    from vissatsatellitestereo_gb300.aggregate_2p5d_util import depth_map_to_points
+    from vissatsatellitestereo_gb300.coordinate_system import GeoPlan
+    with pytest.raises(_lib.VsError) as e:
+        GeoPlan(39.0, -84.0, 0.0, 0, False)               # zone 0
+    assert e.value.status == _lib.VS_ERR_ARG
+    case = synth.make_depth_case(28, 1, 16, 16, _utm, aoi_m=40.0, n_boxes=2)
+    d = synth.depth_map_torch(case, 0, 'cuda')
+    bad = case.inv_proj[0].copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(ValueError):
+        depth_map_to_points(d, bad, case.aoi)
+    plan = GeoPlan(39.77, -84.05, -30.0, 16, False)
+    pts = torch.empty((256, 3), dtype=torch.float64, device='cuda')
+    n = torch.zeros(1, dtype=torch.int64, device='cuda')
+    ws = torch.empty(_lib.lib().vs_depth_to_points_workspace_size(16, 16), dtype=torch.uint8, device='cuda')
+    m = np.ascontiguousarray(case.inv_proj[0])
+    args = (d.data_ptr(), 16, 16, m.ctypes.data_as(ctypes.c_void_p), plan.handle)
+    tail = (pts.data_ptr(), n.data_ptr(), None, ws.data_ptr(), ws.numel(), torch.cuda.current_stream().cuda_stream)
+    assert _lib.lib().vs_depth_to_points(*args, 7, *tail) == _lib.VS_ERR_ARG          # bad mode
+    assert _lib.lib().vs_depth_to_points(*args, _lib.VS_GEO_FAST, *tail[:3], ws.data_ptr(), 16,
+                                         tail[-1]) == _lib.VS_ERR_WORKSPACE
+    assert _lib.lib().vs_depth_to_points(*args, _lib.VS_GEO_FAST, *tail) == _lib.VS_OK
