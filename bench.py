@@ -562,6 +562,31 @@ def depth_form(n_views=50, image=4096, cells=2000, res=0.3, steps=3, warmup=1, e
     return res_
 
 
+def fusion_form(n_views=50, cells=2000, steps=20, warmup=3, nan_frac=0.15, seed=3):
+    """The fusion alone (aggregate_2p5d.py:65-81 + the final blur) over n_views float32
+    planes of cells x cells (normal(30, 10) heights, nan_frac NaN), [V][H][W] layout:
+    device time per call by CUDA events."""
+    import torch
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    g = torch.Generator(device='cuda').manual_seed(seed)
+    d = torch.randn((n_views, cells, cells), generator=g, device='cuda') * 10 + 30
+    d[torch.rand(d.shape, generator=g, device='cuda') < nan_frac] = float('nan')
+    out = torch.empty((cells, cells), device='cuda')
+    for _ in range(warmup):
+        fuse_dsms(d, median_blur=True, layout='vhw', out=out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fuse_dsms(d, median_blur=True, layout='vhw', out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / steps
+    return {'workload': f'{n_views} x {cells}x{cells} float32 planes ({nan_frac:.0%} NaN), fusion + blur',
+            'ms_per_call': round(t * 1e3, 4), 'cell_views_per_s': n_views * cells * cells / t,
+            'algorithmic_bytes': n_views * cells * cells * 4 + cells * cells * 4}
+
+
 def plain_aoi_seconds(spec, maps, affines):
     """GPU time of the plain per-view form of one AOI (the reference's structure on the GPU):
     per view the FP64 point list of its height map, proj_to_grid and the blur, one call
@@ -905,9 +930,17 @@ def main():
     ap.add_argument('--serve', type=int, default=400, metavar='REQUESTS',
                     help='requests of the serving form (Poisson 20/s; 2000 is the full stream)')
     ap.add_argument('--serve-only', action='store_true', help='run only the serving form')
+    ap.add_argument('--fusion-only', type=int, default=0, metavar='VIEWS',
+                    help='run only the fusion over VIEWS planes of --cells^2 (0: off)')
     ap.add_argument('--depth-only', type=int, default=0, metavar='VIEWS',
                     help='run only the depth map -> DSM form over VIEWS views (0: off)')
     args = ap.parse_args()
+    if args.fusion_only:
+        from vissatsatellitestereo_gb300.build import build
+        build()
+        print(json.dumps({'fusion_form': fusion_form(n_views=args.fusion_only, cells=args.cells,
+                                                     steps=args.steps, warmup=args.warmup)}))
+        return
     if args.depth_only:
         from vissatsatellitestereo_gb300.build import build
         build()
