@@ -130,13 +130,6 @@ __device__ __forceinline__ df df_mul_f(df a, float b) {
     p.lo = __fmaf_rn(a.lo, b, p.lo);
     return fast_two_sum(p.hi, p.lo);
 }
-__device__ __forceinline__ df df_div(df a, df b) {
-    float q1 = __fdiv_rn(a.hi, b.hi);
-    df p = df_mul_f(b, q1);
-    df r = df_add(a, {-p.hi, -p.lo});
-    float q2 = __fdiv_rn(r.hi, b.hi);
-    return fast_two_sum(q1, q2);
-}
 // Double-float sum whose error is ~2^-48 of the operands' magnitudes (not of the result):
 // one TwoSum of the high parts, the low parts added plainly.  For sums whose accuracy
 // budget is absolute in the operands' scale (cancellation harmless).
