@@ -137,3 +137,27 @@ def test_synthetic_depth_case_lands_on_the_grid():
               (pts[:, 1] <= aoi['ul_northing']) & (pts[:, 1] > aoi['ul_northing'] - aoi['height']))
     assert inside.mean() > 0.5
     assert -32.0 < pts[:, 2].min() and pts[:, 2].max() < 60.0
+
+
+def test_aoi_host_logic(tmp_path):
+    """aoi.json read from a work dir like coordinate_system.py:42-47, the ENU origin (centre
+    latitude/longitude, lowest altitude), a fast-path box that holds the AOI's ENU extent,
+    and produce_dsm's grid (int(width / 0.5) + 1 cells from the upper-left corner)."""
+    import json
+    from vissatsatellitestereo_gb300.aggregate_2p5d_util import aoi_grid
+    from vissatsatellitestereo_gb300.coordinate_system import aoi_enu_box, aoi_origin, load_aoi
+    from vissatsatellitestereo_gb300.geodesy import geodetic_to_enu
+    aoi = {'lat_min': 39.76, 'lat_max': 39.78, 'lon_min': -84.06, 'lon_max': -84.04, 'alt_min': -30.0,
+           'alt_max': 120.0, 'ul_easting': 752374.0, 'ul_northing': 4406693.0, 'width': 713.0, 'height': 651.0,
+           'zone_number': 16, 'hemisphere': 'N'}
+    (tmp_path / 'aoi.json').write_text(json.dumps(aoi))
+    assert load_aoi(str(tmp_path)) == aoi
+    lat0, lon0, alt0 = aoi_origin(str(tmp_path))
+    assert (lat0, lon0, alt0) == ((39.76 + 39.78) / 2.0, (-84.06 + -84.04) / 2.0, -30.0)   # :44-46
+    lo, hi = aoi_enu_box(aoi)
+    for la in (aoi['lat_min'], aoi['lat_max']):
+        for lo_ in (aoi['lon_min'], aoi['lon_max']):
+            for al in (aoi['alt_min'], aoi['alt_max']):
+                e, n, u = geodetic_to_enu(la, lo_, al, lat0, lon0, alt0)
+                assert lo[0] < e < hi[0] and lo[1] < n < hi[1] and lo[2] < u < hi[2]
+    assert aoi_grid(aoi) == (752374.0, 4406693.0, 0.5, 0.5, 1427, 1303)
