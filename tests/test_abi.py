@@ -54,3 +54,27 @@ def test_camera_array_layout():
     with pytest.raises(ValueError):
         bad = dict(meta, rpc=dict(r, rowNum=r['rowNum'][:19]))
         _lib.camera_array([bad])
+
+
+def test_header_compiles_as_c_and_struct_layouts_match(tmp_path):
+    """The boundary is plain C: the header compiles with a C compiler (-std=c99, all
+    warnings as errors), and the structs the Python side mirrors have the same sizes."""
+    import ctypes
+    import shutil
+    import subprocess
+    from vissatsatellitestereo_gb300 import _lib
+    from vissatsatellitestereo_gb300.batch import VsAoi, VsMapView
+    cc = shutil.which('gcc') or shutil.which('cc')
+    if cc is None:
+        pytest.skip('no C compiler')
+    src = tmp_path / 'abi.c'
+    src.write_text('#include "vissat_gb300.h"\n#include <stdio.h>\n'
+                   'int main(void) {\n'
+                   '  printf("%zu %zu %zu %zu\\n", sizeof(VsRpcCamera), sizeof(VsGeoFrame), sizeof(VsAoi),'
+                   ' sizeof(VsMapView));\n  return 0;\n}\n')
+    exe = tmp_path / 'abi'
+    inc = os.path.join(ROOT, 'include')
+    subprocess.run([cc, '-std=c99', '-Wall', '-Wextra', '-Werror', '-I', inc, str(src), '-o', str(exe)], check=True)
+    sizes = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert sizes == [_lib.CAMERA_DOUBLES * 8, ctypes.sizeof(_lib.VsGeoFrame), ctypes.sizeof(VsAoi),
+                     ctypes.sizeof(VsMapView)]
