@@ -10,7 +10,14 @@
 //   VS_CUBE_BF16X3  tensor cores, both factors split into 2 bf16 pieces, products
 //                   hh + lh + hl (mma.sync m16n8k16);
 //   VS_CUBE_TF32X3  tensor cores, 2 tf32 pieces, the same 3 products (m16n8k8);
-//   VS_CUBE_BF16X6  tensor cores, 3 bf16 pieces, the 6 products of order <= 2.
+//   VS_CUBE_BF16X6  tensor cores, 3 bf16 pieces, the 6 products of order <= 2;
+//   VS_CUBE_BF16X3_LIN  BF16X3 for the 16 higher-order terms only, the constant and the
+//                   three linear terms in FP32 on the CUDA cores, added in the epilogue.
+//                   The split forms' error comes from the large linear coefficients
+//                   (|c| ~ 1 at line/sample scale 2048: 2^-16 relative is 0.03 px); the
+//                   higher-order coefficients are ~1e-3, so bf16 pieces are ample there.
+//                   The linear monomials are the last reduction slots of every lane
+//                   (owned monomial q = 0), so one of the four k-steps is dropped.
 //
 // Contraction layout.  A lane (g = lane/4, t = lane%4) of an m16n8 MMA only ever sees the
 // reduction indices k' with k' % 4 == t (tf32 m16n8k8) or k' % 8 in {2t, 2t+1} (bf16
@@ -42,17 +49,22 @@ template <int V>
 struct CubeCfg;
 template <>
 struct CubeCfg<VS_CUBE_BF16X3> {
-    static constexpr bool kBf16 = true;
+    static constexpr bool kBf16 = true, kLin = false;
+    static constexpr int kProducts = 3, kPieces = 2, kSlots = 16, kMTiles = 2, kMinBlocks = 3;
+};
+template <>
+struct CubeCfg<VS_CUBE_BF16X3_LIN> {
+    static constexpr bool kBf16 = true, kLin = true;
     static constexpr int kProducts = 3, kPieces = 2, kSlots = 16, kMTiles = 2, kMinBlocks = 3;
 };
 template <>
 struct CubeCfg<VS_CUBE_BF16X6> {
-    static constexpr bool kBf16 = true;
+    static constexpr bool kBf16 = true, kLin = false;
     static constexpr int kProducts = 6, kPieces = 3, kSlots = 32, kMTiles = 2, kMinBlocks = 2;
 };
 template <>
 struct CubeCfg<VS_CUBE_TF32X3> {
-    static constexpr bool kBf16 = false;
+    static constexpr bool kBf16 = false, kLin = false;
     static constexpr int kProducts = 3, kPieces = 2, kSlots = 16, kMTiles = 2, kMinBlocks = 2;
 };
 
@@ -151,6 +163,7 @@ struct CubeWs {
     uint4 *bfrag;             // [n_ctiles][W/4][32 lanes] uint4: per-lane B slot records
     float *fcoef;             // [20][4C] FP32 coefficients (FP32 variant)
     float2 *denorm;           // [4 n_ctiles]: (scale, offset) of output plane 2*camera + coord
+    float4 *lincoef;          // [n_ctiles][4 lanes][num, den]: constant + linear coefficients (LIN)
 };
 
 inline __host__ __device__ int n_col_tiles(int n_cams) { return (n_cams + 1) / 2; }
@@ -172,7 +185,7 @@ __global__ void cube_prepare_mma_kernel(const VsRpcCamera *__restrict__ cams, in
         const int n_slot = C::kBf16 ? 2 : 1;
         for (int h = 0; h < n_slot; ++h) {
             const int s = C::kBf16 ? 2 * word + h : word;
-            if (cam < n_cams && s < 5 * C::kProducts) {
+            if (cam < n_cams && s < 5 * C::kProducts && !(C::kLin && slot_q(C::kProducts, s) == 0)) {
                 const int q = slot_q(C::kProducts, s), p = slot_p(C::kProducts, s);
                 float pc[C::kPieces];
                 split_f64<C::kBf16, C::kPieces>(column_poly(cams[cam], col & 3)[t + 4 * q], pc);
@@ -191,6 +204,26 @@ __global__ void cube_prepare_mma_kernel(const VsRpcCamera *__restrict__ cams, in
                            : make_float2(static_cast<float>(cams[cam].row_scale), static_cast<float>(cams[cam].row_off));
         w.denorm[i] = v;
     }
+    if constexpr (C::kLin) {
+        // lane t of column tile j: plane 4j + t = camera 2j + t/2, col (t even) or row (t odd)
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 8 * n_ct; i += gridDim.x * blockDim.x) {
+            const int j = i >> 3, t = (i >> 1) & 3, den = i & 1;
+            const int cam = 2 * j + (t >> 1);
+            float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (cam < n_cams) {
+                const double *poly = column_poly(cams[cam], 2 * (t & 1) + den);
+                c = make_float4(static_cast<float>(poly[0]), static_cast<float>(poly[1]), static_cast<float>(poly[2]),
+                                static_cast<float>(poly[3]));
+            }
+            w.lincoef[i] = c;
+        }
+    }
+}
+
+// constant + linear terms (RPC order: 1, y, x, z) added to the tensor cores' higher-order
+// sum in the FP32 variant's order: z, x, y, then the constant
+__device__ __forceinline__ float add_linear(float hot, float4 c, float x, float y, float z) {
+    return __fadd_rn(__fmaf_rn(c.y, y, __fmaf_rn(c.z, x, __fmaf_rn(c.w, z, hot))), c.x);
 }
 
 __global__ void cube_prepare_fp32_kernel(const VsRpcCamera *__restrict__ cams, int n_cams, CubeWs w) {
@@ -320,8 +353,11 @@ __global__ void __launch_bounds__(kCubeWarps * 32, CubeCfg<V>::kMinBlocks) cube_
     extern __shared__ uint4 bsh[];                     // [n_ct][W/4][32]
     const int n_ct = n_col_tiles(n_cams);
     float2 *dn = reinterpret_cast<float2 *>(bsh + n_ct * (W / 4) * 32);
+    float4 *lc = reinterpret_cast<float4 *>(dn + 4 * n_ct);   // LIN: [n_ct][4][2]
     for (int i = threadIdx.x; i < n_ct * (W / 4) * 32; i += blockDim.x) bsh[i] = w.bfrag[i];
     for (int i = threadIdx.x; i < 4 * n_ct; i += blockDim.x) dn[i] = w.denorm[i];
+    if constexpr (C::kLin)
+        for (int i = threadIdx.x; i < 8 * n_ct; i += blockDim.x) lc[i] = w.lincoef[i];
     __syncthreads();
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -333,6 +369,7 @@ __global__ void __launch_bounds__(kCubeWarps * 32, CubeCfg<V>::kMinBlocks) cube_
         const long long p0 = grp * PTS;
         const bool full = p0 + PTS <= n;
         unsigned a[MT][2][W];
+        float px[MT][2], py[MT][2], pz[MT][2];          // the points, for the LIN epilogue
 #pragma unroll
         for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
@@ -344,6 +381,9 @@ __global__ void __launch_bounds__(kCubeWarps * 32, CubeCfg<V>::kMinBlocks) cube_
                     y = __ldg(xyz + n + p);
                     z = __ldg(xyz + 2 * n + p);
                 }
+                px[mt][h] = x;
+                py[mt][h] = y;
+                pz[mt][h] = z;
                 a_record<V>(x, y, z, t, a[mt][h]);
             }
         float *o = out + static_cast<long long>(t) * n + p0 + g;
@@ -361,7 +401,7 @@ __global__ void __launch_bounds__(kCubeWarps * 32, CubeCfg<V>::kMinBlocks) cube_
 #pragma unroll
             for (int mt = 0; mt < MT; ++mt) d[mt][0] = d[mt][1] = d[mt][2] = d[mt][3] = 0.0f;
 #pragma unroll
-            for (int s = 0; s < W / 2; ++s)
+            for (int s = 0; s < W / 2 - (C::kLin ? 1 : 0); ++s)   // LIN: the q = 0 k-step is dropped
 #pragma unroll
                 for (int mt = 0; mt < MT; ++mt) {
                     if constexpr (C::kBf16)
@@ -371,6 +411,16 @@ __global__ void __launch_bounds__(kCubeWarps * 32, CubeCfg<V>::kMinBlocks) cube_
                         mma_tf32(d[mt], a[mt][0][2 * s], a[mt][1][2 * s], a[mt][0][2 * s + 1], a[mt][1][2 * s + 1],
                                  b[2 * s], b[2 * s + 1]);
                 }
+            if constexpr (C::kLin) {
+                const float4 cn = lc[(4 * j + t) * 2], cd = lc[(4 * j + t) * 2 + 1];
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt) {
+                    d[mt][0] = add_linear(d[mt][0], cn, px[mt][0], py[mt][0], pz[mt][0]);
+                    d[mt][1] = add_linear(d[mt][1], cd, px[mt][0], py[mt][0], pz[mt][0]);
+                    d[mt][2] = add_linear(d[mt][2], cn, px[mt][1], py[mt][1], pz[mt][1]);
+                    d[mt][3] = add_linear(d[mt][3], cd, px[mt][1], py[mt][1], pz[mt][1]);
+                }
+            }
             // quotients: the fast form for every value, one warp-uniform check for the rare
             // operands outside its range
             float q[MT][2];
@@ -413,6 +463,7 @@ CubeWs carve_cube(Carver &cv, int n_cams) {
     w.bfrag = cv.take<uint4>(static_cast<size_t>(n_col_tiles(n_cams)) * 4 * 32);   // up to 16 words per lane
     w.fcoef = cv.take<float>(static_cast<size_t>(kTerms) * 4 * n_cams);
     w.denorm = cv.take<float2>(4 * static_cast<size_t>(n_col_tiles(n_cams)));
+    w.lincoef = cv.take<float4>(8 * static_cast<size_t>(n_col_tiles(n_cams)));
     return w;
 }
 
@@ -425,7 +476,7 @@ int launch_mma(const VsRpcCamera *cams, int n_cams, const float *xyz, long long 
     cube_prepare_mma_kernel<V><<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(n_ct) * 32 * W, 256)), 256, 0, st>>>(
         cams, n_cams, w);
     VS_LAUNCH_CHECK("cube_prepare_mma_kernel");
-    const size_t sh = sizeof(uint4) * n_ct * (W / 4) * 32 + sizeof(float2) * 4 * n_ct;
+    const size_t sh = sizeof(uint4) * n_ct * (W / 4) * 32 + sizeof(float2) * 4 * n_ct + (C::kLin ? sizeof(float4) * 8 * n_ct : 0);
     if (cudaFuncSetAttribute(cube_mma_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sh)) !=
         cudaSuccess) {
         set_error("vs_rpc_project_cube: shared memory request of %zu bytes refused", sh);
@@ -464,7 +515,7 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
     VS_REQUIRE(n_cams > 0 && n_cams <= VS_CUBE_MAX_CAMERAS && n >= 0,
                "vs_rpc_project_cube: bad sizes (cameras %d, max %d; n %lld)", n_cams, VS_CUBE_MAX_CAMERAS, (long long)n);
     VS_REQUIRE(variant == VS_CUBE_FP32 || variant == VS_CUBE_BF16X3 || variant == VS_CUBE_TF32X3 ||
-                   variant == VS_CUBE_BF16X6 || variant == VS_CUBE_BF16X3_TC,
+                   variant == VS_CUBE_BF16X6 || variant == VS_CUBE_BF16X3_TC || variant == VS_CUBE_BF16X3_LIN,
                "vs_rpc_project_cube: bad variant %d", variant);
     VS_REQUIRE(cams && workspace && (n == 0 || (xyz && colrow)), "vs_rpc_project_cube: null pointer");
     const size_t need = vs_rpc_project_cube_workspace_size(n_cams);
@@ -480,6 +531,7 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
         case VS_CUBE_BF16X3: return launch_mma<VS_CUBE_BF16X3>(cams, n_cams, xyz, n, colrow, w, st);
         case VS_CUBE_TF32X3: return launch_mma<VS_CUBE_TF32X3>(cams, n_cams, xyz, n, colrow, w, st);
         case VS_CUBE_BF16X6: return launch_mma<VS_CUBE_BF16X6>(cams, n_cams, xyz, n, colrow, w, st);
+        case VS_CUBE_BF16X3_LIN: return launch_mma<VS_CUBE_BF16X3_LIN>(cams, n_cams, xyz, n, colrow, w, st);
         case VS_CUBE_BF16X3_TC: return launch_cube_tc(cams, n_cams, xyz, n, colrow, workspace, st);
         default: break;
     }

@@ -116,7 +116,8 @@ def project_cameras(meta_dicts, lat, lon, alt, mode='fast', shared=True, keep=Fa
 
 
 CUBE_VARIANTS = {'fp32': _lib.VS_CUBE_FP32, 'bf16x3': _lib.VS_CUBE_BF16X3, 'tf32x3': _lib.VS_CUBE_TF32X3,
-                 'bf16x6': _lib.VS_CUBE_BF16X6, 'bf16x3_tc': _lib.VS_CUBE_BF16X3_TC}
+                 'bf16x6': _lib.VS_CUBE_BF16X6, 'bf16x3_tc': _lib.VS_CUBE_BF16X3_TC,
+                 'bf16x3_lin': _lib.VS_CUBE_BF16X3_LIN}
 
 
 def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
@@ -126,7 +127,9 @@ def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
 
     xyz: (3, N) float32 (normalised latitude, longitude, altitude), numpy or CUDA tensor.
     Returns a CUDA float32 tensor (C, 2, N): col plane then row plane per camera.
-    ``variant``: 'fp32' (CUDA cores), 'bf16x3', 'tf32x3', 'bf16x6' (tensor-core split forms).
+    ``variant``: 'fp32' (CUDA cores), 'bf16x3', 'tf32x3', 'bf16x6' (tensor-core split forms),
+    'bf16x3_tc' (BF16X3 on tcgen05), 'bf16x3_lin' (BF16X3 for the higher-order terms, the
+    constant and linear terms in FP32).
     ``out``: optional preallocated (C, 2, N) float32 CUDA tensor.
     """
     require_cuda()
