@@ -93,7 +93,8 @@ int vs_rpc_project(const VsRpcCamera *cams, int n_cams, const double *lat, const
 #define VS_CUBE_BF16X3_TC 4 /* as BF16X3 on tcgen05 (TMEM accumulators), at most 64 cameras   */
 #define VS_CUBE_BF16X3_LIN 5 /* BF16X3 for the 16 higher-order terms; constant + linear terms in
                               * FP32 on CUDA cores (the split forms' error sits in the large
-                              * linear coefficients): below 1e-3 px at BF16X3's cost         */
+                              * linear coefficients): FP32's accuracy, below 1e-3 px, faster
+                              * than BF16X6                                                  */
 #define VS_CUBE_MAX_CAMERAS 128
 size_t vs_rpc_project_cube_workspace_size(int n_cams);
 int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const float *xyz, int64_t n, float *colrow,
