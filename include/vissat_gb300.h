@@ -32,6 +32,7 @@ extern "C" {
 #define VS_ERR_WORKSPACE 3  /* caller workspace smaller than *_workspace_size() */
 #define VS_ERR_FACTORIZE 4  /* per-view: factorisation check failed (the reference asserts) */
 #define VS_ERR_DEGENERATE 5 /* per-view: fewer than 6 kept points / singular system */
+#define VS_ERR_TIMEOUT 6    /* a kernel gave up a bounded wait; its outputs are incomplete */
 
 /* ---- data types ------------------------------------------------------------------ */
 
@@ -99,6 +100,16 @@ int vs_rpc_project(const VsRpcCamera *cams, int n_cams, const double *lat, const
 size_t vs_rpc_project_cube_workspace_size(int n_cams);
 int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const float *xyz, int64_t n, float *colrow,
                         int variant, void *workspace, size_t workspace_bytes, void *stream);
+/* Device-side status of the last vs_rpc_project_cube call that used `workspace` (same
+ * n_cams and variant): copies its error word back and synchronises `stream`.  VS_OK, or
+ * VS_ERR_TIMEOUT when a CTA of the tcgen05 variant gave up its bounded wait for the
+ * tensor cores (its tiles of colrow are then unwritten).  The other variants have no
+ * device-side waits and always report VS_OK.  No counterpart in the reference. */
+int vs_rpc_project_cube_status(const void *workspace, int n_cams, int variant, void *stream);
+/* Polls of the tcgen05 variant's completion wait before a CTA gives up (default 2^24,
+ * far beyond any real completion time); 0 gives up at once, so tests can drive the
+ * timeout path without a faulty device.  Process-wide; not thread-safe. */
+void vs_set_tc_wait_limit(unsigned polls);
 
 /* Replaces RPCModel.inverse_projection (lib/rpc_model.py:170-249) for n_cams cameras:
  * (lon, lat) of image points (col, row) at altitudes alt, by the reference's iteration

@@ -8,27 +8,40 @@ lat/lon to UTM (``lib/latlon_utm_converter.py:38-52`` -> ``utm.from_latlon`` for
 ``pyproj.Proj(proj='utm', ellps='WGS84')`` for the projection).
 
 The three third-party libraries are pinned in the reference's ``requirements.txt`` and are
-absent here: pymap3d==1.7.15, utm==0.4.2, pyproj==2.4.0 (PROJ 6).  Their published
-algorithms are restated:
+absent here: pymap3d==1.7.15, utm==0.4.2, pyproj==2.4.0 (which bundles PROJ 6.2).  Their
+published source is restated step by step (same formulas, same order of operations):
 
-* ENU -> ECEF: the rotation of (east, north, up) by the origin's latitude/longitude plus the
-  origin's ECEF position (pymap3d ``enu2ecef``).
-* ECEF -> geodetic: You, Rey-Jer (2000), "Transformation of Cartesian to Geodetic
-  Coordinates without Iterations", J. Surveying Eng. 126(1): reduced latitude from the
-  confocal-ellipsoid semi-minor axis, one closed-form correction, then latitude, longitude
-  and height (the method pymap3d's ``ecef2geodetic`` names).
-* UTM zone: 6-degree zones from -180 with the Norway (32V) and Svalbard exceptions
-  (utm ``latlon_to_zone_number``).
-* Transverse Mercator: Krueger's series in the third flattening n to order n^6 (Krueger
-  1912; coefficients as tabulated by Karney 2011, "Transverse Mercator with an accuracy of a
-  few nanometers", J. Geodesy 85), k0 = 0.9996, false easting 500 km, false northing
-  10,000 km in the south.  PROJ 6's default ``utm`` is this series (Poder/Engsager).
+* ENU -> ECEF: pymap3d 1.7.15 ``enu2geodetic`` (pymap3d/enu.py) calls ``enu2ecef``, which
+  adds ``enu2uvw``'s rotation of (east, north, up) by the origin's latitude/longitude to
+  the origin's ``geodetic2ecef`` (pymap3d/ecef.py): N = a^2 / sqrt(a^2 cos^2 lat +
+  b^2 sin^2 lat), x = (N + h) cos lat cos lon, y = (N + h) cos lat sin lon,
+  z = (N (b/a)^2 + h) sin lat, with the WGS-84 ellipsoid a = 6378137, f = 1/298.257223563,
+  b = a (1 - f).
+* ECEF -> geodetic: pymap3d's ``ecef2geodetic`` (pymap3d/ecef.py), the method of You,
+  Rey-Jer (2000), "Transformation of Cartesian to Geodetic Coordinates without
+  Iterations", J. Surveying Eng. 126(1): reduced latitude from the confocal ellipsoid's
+  semi-minor axis u, one closed-form correction, latitude atan(a/b tan beta), height
+  hypot(z - b sin beta, Q - a cos beta), negated inside the ellipsoid.
+* UTM zone: utm 0.4.2 ``latlon_to_zone_number`` (6-degree zones from -180 with the Norway
+  32V and Svalbard exceptions), taken from the first point.
+* Transverse Mercator: ``pyproj.Proj(proj='utm', ellps='WGS84', zone=z, south=s)`` runs
+  PROJ 6.2's ``utm``, which is the Poder/Engsager extended transverse Mercator
+  (src/projections/tmerc.cpp, the former etmerc): pyproj converts degrees with pi/180;
+  PROJ subtracts lam0 = (zone - 1 + 0.5) pi / 30 - pi; the geodetic latitude becomes the
+  Gaussian (conformal) latitude by the 6-term trig series ``cbg`` summed by Clenshaw
+  (``gatg``); the spherical transverse Mercator step (atan2 / hypot / asinh(tan)); the
+  6-term Krueger series ``gtu`` summed by complex Clenshaw (``clenS``); x = a Qn Ce + x0,
+  y = a Qn Cn + y0 with Qn = k0 / (1 + n) (1 + n^2/4 + n^4/64 + n^6/256), k0 = 0.9996,
+  x0 = 500 km, y0 = 10,000 km in the south.
 
-Parity against pymap3d/pyproj themselves is unpinned (they are not installed).  The
-restatement is pinned by identities instead: the series on the central meridian equals the
-numerically integrated meridian arc (which fixes every alpha_j and the rectifying radius),
-the forward and inverse series invert each other, and ENU -> geodetic inverts the textbook
-geodetic -> ENU conversion.
+What pins this restatement: the libraries themselves cannot run here, so the oracle is
+pinned to their published code paths as restated above, plus checks that do not depend on
+the restatement: the series on the central meridian equals the numerically integrated
+meridian arc (fixing every coefficient and the rectifying radius), an independent
+closed-form transverse Mercator (Karney 2011, "Transverse Mercator with an accuracy of a
+few nanometers", J. Geodesy 85: exact conformal latitude, direct series) agrees with the
+PROJ path to nanometres, the forward and inverse series invert each other, and ENU ->
+geodetic inverts geodetic -> ENU.
 """
 import numpy as np
 
@@ -70,11 +83,12 @@ ALPHA, BETA, RECT_A = _series()
 
 
 def geodetic_to_ecef(lat, lon, alt):
+    """pymap3d 1.7.15 ``geodetic2ecef`` (``get_radius_normal`` for N)."""
+    a, b = WGS84_A, WGS84_B
     phi, lam = np.radians(lat), np.radians(lon)
-    s = np.sin(phi)
-    nu = WGS84_A / np.sqrt(1.0 - WGS84_E2 * s * s)
-    return ((nu + alt) * np.cos(phi) * np.cos(lam), (nu + alt) * np.cos(phi) * np.sin(lam),
-            (nu * (1.0 - WGS84_E2) + alt) * s)
+    N = a ** 2 / np.sqrt(a ** 2 * np.cos(phi) ** 2 + b ** 2 * np.sin(phi) ** 2)
+    return ((N + alt) * np.cos(phi) * np.cos(lam), (N + alt) * np.cos(phi) * np.sin(lam),
+            (N * (b / a) ** 2 + alt) * np.sin(phi))
 
 
 def enu_to_ecef(e, n, u, lat0, lon0, alt0):
@@ -134,8 +148,84 @@ def central_meridian(zone):
     return (zone - 1) * 6 - 180 + 3
 
 
+def _proj_coefficients():
+    """PROJ 6's etmerc set-up: the 6-term series geodetic -> Gaussian latitude (``cbg``),
+    spherical -> ellipsoidal N, E (``gtu``, Krueger's alpha) and Qn, from the third
+    flattening n (Engsager and Poder 2007)."""
+    n = _N
+    cbg = [n * (-2 + n * (2 / 3 + n * (4 / 3 + n * (-82 / 45 + n * (32 / 45 + n * (4642 / 4725)))))),
+           n ** 2 * (5 / 3 + n * (-16 / 15 + n * (-13 / 9 + n * (904 / 315 + n * (-1522 / 945))))),
+           n ** 3 * (-26 / 15 + n * (34 / 21 + n * (8 / 5 + n * (-12686 / 2835)))),
+           n ** 4 * (1237 / 630 + n * (-12 / 5 + n * (-24832 / 14175))),
+           n ** 5 * (-734 / 315 + n * (109598 / 31185)),
+           n ** 6 * (444337 / 155925)]
+    gtu = [n * (0.5 + n * (-2 / 3 + n * (5 / 16 + n * (41 / 180 + n * (-127 / 288 + n * (7891 / 37800)))))),
+           n ** 2 * (13 / 48 + n * (-3 / 5 + n * (557 / 1440 + n * (281 / 630 + n * (-1983433 / 1935360))))),
+           n ** 3 * (61 / 240 + n * (-103 / 140 + n * (15061 / 26880 + n * (167603 / 181440)))),
+           n ** 4 * (49561 / 161280 + n * (-179 / 168 + n * (6601661 / 7257600))),
+           n ** 5 * (34729 / 80640 + n * (-3418889 / 1995840)),
+           n ** 6 * (212378941 / 319334400)]
+    n2 = n * n
+    qn = UTM_K0 / (1 + n) * (1 + n2 * (1 / 4 + n2 * (1 / 64 + n2 / 256)))
+    return np.array(cbg), np.array(gtu), qn
+
+
+PROJ_CBG, PROJ_GTU, PROJ_QN = _proj_coefficients()
+
+
+def _clenshaw_sin(p, B):
+    """B + sum_k p[k] sin(2 (k+1) B) by Clenshaw's recurrence (PROJ ``gatg``)."""
+    two_cos = 2.0 * np.cos(2.0 * B)
+    h1, h2, h = p[-1], 0.0, 0.0
+    for k in range(len(p) - 2, -1, -1):
+        h = -h2 + two_cos * h1 + p[k]
+        h2, h1 = h1, h
+    return B + h * np.sin(2.0 * B)
+
+
+def _clenshaw_complex(a, arg_r, arg_i):
+    """(Re, Im) of sum_k a[k] sin((k+1) (arg_r + i arg_i)) by complex Clenshaw (PROJ
+    ``clenS``)."""
+    sin_r, cos_r = np.sin(arg_r), np.cos(arg_r)
+    sinh_i, cosh_i = np.sinh(arg_i), np.cosh(arg_i)
+    r = 2.0 * cos_r * cosh_i
+    i = -2.0 * sin_r * sinh_i
+    hr, hi, hr1, hi1 = a[-1], 0.0, 0.0, 0.0
+    for k in range(len(a) - 2, -1, -1):
+        hr2, hi2 = hr1, hi1
+        hr1, hi1 = hr, hi
+        hr = -hr2 + r * hr1 - i * hi1 + a[k]
+        hi = -hi2 + i * hr1 + r * hi1
+    r = sin_r * cosh_i
+    i = cos_r * sinh_i
+    return r * hr - i * hi, r * hi + i * hr
+
+
 def geodetic_to_utm(lat, lon, zone, south):
-    """Krueger series transverse Mercator: (lat, lon) degrees -> (east, north) metres."""
+    """PROJ 6.2 ``utm`` (etmerc forward) as pyproj 2.4 calls it: (lat, lon) degrees ->
+    (east, north) metres."""
+    deg = np.pi / 180.0
+    lam0 = (zone - 1 + 0.5) * np.pi / 30.0 - np.pi
+    phi = np.asarray(lat, dtype=np.float64) * deg
+    lam = np.asarray(lon, dtype=np.float64) * deg - lam0
+    cn = _clenshaw_sin(PROJ_CBG, phi)                       # Gaussian latitude
+    sin_cn, cos_cn = np.sin(cn), np.cos(cn)
+    sin_ce, cos_ce = np.sin(lam), np.cos(lam)
+    cn = np.arctan2(sin_cn, cos_ce * cos_cn)
+    ce = np.arctan2(sin_ce * cos_cn, np.hypot(sin_cn, cos_cn * cos_ce))
+    ce = np.arcsinh(np.tan(ce))
+    dcn, dce = _clenshaw_complex(PROJ_GTU, 2.0 * cn, 2.0 * ce)
+    cn = cn + dcn
+    ce = ce + dce
+    east = WGS84_A * (PROJ_QN * ce) + UTM_FE
+    north = WGS84_A * (PROJ_QN * cn) + (UTM_FN_SOUTH if south else 0.0)
+    return east, north
+
+
+def geodetic_to_utm_karney(lat, lon, zone, south):
+    """Independent closed-form transverse Mercator (Karney 2011: exact conformal latitude,
+    Krueger's series summed directly): (lat, lon) degrees -> (east, north) metres.  Checks
+    the PROJ path."""
     e = np.sqrt(WGS84_E2)
     phi = np.radians(np.asarray(lat, dtype=np.float64))
     dlam = np.radians(np.asarray(lon, dtype=np.float64) - central_meridian(zone))

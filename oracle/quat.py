@@ -1,10 +1,19 @@
 """Oracle: rotation matrix -> unit quaternion (test infrastructure only).
 
 The reference calls ``pyquaternion.Quaternion(matrix=R)`` (camera_approx.py:178;
-pyquaternion 0.9.5, not installed here).  That library converts with the
-branch-on-largest-diagonal method of M. Day, "Converting a Rotation Matrix to a
-Quaternion" (2015), applied to R^T; this restates that published method.  Parity of
-the quaternion's overall sign is unpinned (no reference output is available).
+pyquaternion 0.9.5 pinned in requirements.txt, not installed here) and stores
+``q[0..3]`` = (w, x, y, z).  This restates that library's published source,
+``Quaternion._from_matrix`` in pyquaternion/quaternion.py: after checking that R is
+orthogonal with determinant +1 (``np.allclose``/``np.isclose``, else ValueError), it
+returns ``trace_method(R)``, which applies M. Day's branch-on-diagonal method
+("Converting a Rotation Matrix to a Quaternion", 2015) to m = R^T (the method assumes
+row vectors): the branch is chosen by the sign of m[2,2] and then by comparing m[0,0]
+with m[1,1] (or with -m[1,1]); the branch's pivot component is t = 1 +- the diagonal
+entries, the others are sums/differences of off-diagonal pairs, and all four are scaled
+by 0.5 / sqrt(t).  The constructor does not normalise again.
+
+The sign convention follows from that: the branch's pivot component (w when
+m[2,2] >= 0 and m[0,0] >= -m[1,1]) is +0.5 sqrt(t) > 0.
 """
 import math
 

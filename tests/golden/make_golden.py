@@ -2,7 +2,9 @@
 
 Run once in a container where the reference checkout is present:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout> [--sections ...]
+
+(or with the checkout in $VISSAT_REFERENCE).
 
 It imports the reference modules that import cleanly (``lib/rpc_model.py``,
 ``lib/solve_perspective.py``, ``lib/check_error.py``, ``lib/gen_grid.py``,
@@ -185,11 +187,41 @@ def depth_files(ref, seed):
     np.savez_compressed(os.path.join(HERE, 'depth_enu.npz'), **res)
 
 
+from fit_cases import fit_cases  # noqa: E402
+
+
+def fit_at_size(RPCModel, solve_perspective, check_perspective_error):
+    """Reference fits and error statistics at the benchmarked grid sizes.  The grids are not
+    stored (the tests regenerate them with ``synth.rpc_sample_grid``); a strided sample of
+    each grid is, so a test can tell that its regenerated grid is the one fitted here."""
+    out = {}
+    for name, metas, n_xy, n_z, _ in fit_cases():
+        g = synth.rpc_sample_grid(metas[0], n_xy, n_z)
+        out[f'{name}_probe'] = np.hstack((g.lat, g.lon, g.alt, g.x, g.y, g.z))[::997]
+        for c, meta in enumerate(metas):
+            col, row = RPCModel(meta).projection(g.lat, g.lon, g.alt)
+            w, h = meta['width'], meta['height']
+            keep = np.logical_and(np.logical_and(col >= 0, row >= 0), np.logical_and(col < w, row < h))
+            K, R, t = solve_perspective(g.x, g.y, g.z, col, row, keep)
+            err = check_perspective_error(g.x, g.y, g.z, col, row, K, R, t, keep)
+            key = f'{name}_cam{c}'
+            out[f'{key}_meta'] = np.array(repr(meta))
+            out[f'{key}_K'], out[f'{key}_R'], out[f'{key}_t'] = K, R, t
+            out[f'{key}_err'] = np.array(err, dtype=np.float64)
+            out[f'{key}_kept'] = np.array(int(keep.sum()))
+            print(name, c, 'kept', int(keep.sum()), 'of', keep.size, 'err', np.array(err))
+    np.savez_compressed(os.path.join(HERE, 'perspective_fit_fullsize.npz'), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
-    ap.add_argument('--sections', default='all', help="'all' or a comma list of: base, inverse, formats, depth")
+    ap.add_argument('--ref', default=os.environ.get('VISSAT_REFERENCE'),
+                    help='checkout of the reference (default: $VISSAT_REFERENCE)')
+    ap.add_argument('--sections', default='all',
+                    help="'all' or a comma list of: base, inverse, formats, depth, fitsize")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error('give the reference checkout with --ref or $VISSAT_REFERENCE')
     ref = os.path.abspath(args.ref)
     sys.path.insert(0, ref)
     from lib.rpc_model import RPCModel
@@ -198,7 +230,10 @@ def main():
     from lib.gen_grid import gen_grid
 
     seed = synth.BASE_SEED
-    sections = {'base', 'inverse', 'formats', 'depth'} if args.sections == 'all' else set(args.sections.split(','))
+    sections = {'base', 'inverse', 'formats', 'depth', 'fitsize'} if args.sections == 'all' \
+        else set(args.sections.split(','))
+    if 'fitsize' in sections:
+        fit_at_size(RPCModel, solve_perspective, check_perspective_error)
     if 'depth' in sections:
         depth_files(ref, seed)
     if 'inverse' in sections:

@@ -189,3 +189,17 @@ def test_ecef_to_geodetic_matches_an_independent_iteration():
     assert np.abs(h - al).max() < 1e-6
     assert np.abs(lo - lon).max() < 1e-10
     assert (np.abs(la - lat) * 111320.0)[terrain].max() < 1e-8 and np.abs(al - alt).max() < 1e-6
+
+
+def test_proj_path_matches_closed_form_transverse_mercator():
+    """The restated PROJ 6.2 utm path (Gaussian latitude by Clenshaw, complex Clenshaw of
+    Krueger's series) against an independent closed form (exact conformal latitude, direct
+    series) over the UTM domain of every latitude band, both hemispheres' false northings."""
+    rng = np.random.default_rng(11)
+    lat = rng.uniform(-80.0, 84.0, 100000)
+    for zone in (1, 21, 33, 60):
+        lon = geo.central_meridian(zone) + rng.uniform(-3.5, 3.5, lat.size)
+        for south in (False, True):
+            e1, n1 = geo.geodetic_to_utm(lat, lon, zone, south)
+            e2, n2 = geo.geodetic_to_utm_karney(lat, lon, zone, south)
+            assert np.abs(e1 - e2).max() < 2e-8 and np.abs(n1 - n2).max() < 2e-8

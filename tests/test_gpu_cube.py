@@ -132,3 +132,29 @@ def test_cube_tcgen05_rejects_too_many_cameras(cameras50):
     from vissatsatellitestereo_gb300.rpc_model import project_cube
     with pytest.raises(_lib.VsError):
         project_cube(cameras50 + cameras50[:20], np.zeros((3, 5), np.float32), variant='bf16x3_tc')
+
+
+def test_cube_tcgen05_timeout_is_reported():
+    """A CTA whose bounded wait for the tensor cores runs out sets the error word; the call's
+    status query returns VS_ERR_TIMEOUT and the context stays usable.  The wait limit is
+    set to 0 polls, so every CTA gives up at once (after draining its committed MMAs),
+    without any device fault."""
+    from vissatsatellitestereo_gb300 import _lib, synth
+    from vissatsatellitestereo_gb300.rpc_model import project_cube, project_cube_status
+    metas = [synth.make_rpc_meta(3100 + v, 4096, 4096) for v in range(5)]
+    pts = cube_points(3000, 23)
+    L = _lib.lib()
+    try:
+        L.vs_set_tc_wait_limit(0)
+        with pytest.raises(_lib.VsError) as e:
+            project_cube(metas, pts, variant='bf16x3_tc')
+        assert e.value.status == _lib.VS_ERR_TIMEOUT
+        project_cube(metas, pts, variant='bf16x3_tc', check=False)
+        with pytest.raises(_lib.VsError):
+            project_cube_status(len(metas), 'bf16x3_tc')
+    finally:
+        L.vs_set_tc_wait_limit(1 << 24)
+    got = project_cube(metas, pts, variant='bf16x3_tc').cpu().numpy()      # status clean again
+    assert np.abs(got - oracle_colrow(metas, pts)).max() <= TOL['bf16x3']
+    project_cube_status(len(metas), 'bf16x3_tc')
+    assert project_cube(metas, pts, variant='fp32') is not None

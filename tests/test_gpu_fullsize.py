@@ -1,5 +1,6 @@
-"""Parity at the benchmark's full sizes through size-independent properties (the oracle
-cannot run these sizes in seconds):
+"""Parity at the benchmark's full sizes: against the oracle where it finishes in seconds
+(one full 4096^2 view through proj_to_grid + blur; a 96-row band of the 50-view fusion),
+and through size-independent properties where it cannot:
 
 * rasterisation of 50 views x 4096^2 points onto 2000 x 2000 at 0.3 m: the overlapped
   two-stream schedule and the serial one are bit-identical, and a view rasterised alone
@@ -55,6 +56,35 @@ def test_full_size_raster_schedules_and_batch_independence(aoi50):
     finite = torch.isfinite(serial)
     assert finite.float().mean() > 0.9                      # the views cover the grid
     assert float(serial[finite].min()) > -5.0 and float(serial[finite].max()) < 85.0
+
+
+def test_full_size_view_matches_oracle(aoi50):
+    """One full 4096^2 view (16.8 M points) against the oracle's proj_to_grid + blur, bit-exact."""
+    from oracle import blur, raster
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    pts, offsets, args, n = aoi50
+    v = 17
+    got = dsm_from_points(pts[v * n:(v + 1) * n], torch.tensor([0, n]), *args)[0].cpu().numpy()
+    host = pts[v * n:(v + 1) * n].cpu().numpy()
+    ref = blur.median_blur3x3(raster.proj_to_grid(host, *args).astype(np.float32))
+    assert same_bits(got, ref)
+
+
+def test_full_size_fusion_band_matches_oracle(aoi50):
+    """A 96-row band of the 50-view fusion against the reference's numpy calls, bit-exact,
+    unblurred and blurred (the band's blur is compared away from its cut edges)."""
+    from oracle import blur, fuse
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    pts, offsets, args, n = aoi50
+    dsms = dsm_from_points(pts, offsets, *args)
+    plain = fuse_dsms(dsms, median_blur=False, layout='vhw').cpu().numpy()
+    blurred = fuse_dsms(dsms, median_blur=True, layout='vhw').cpu().numpy()
+    r0, r1 = 952, 1048
+    band = dsms[:, r0:r1].permute(1, 2, 0).contiguous().cpu().numpy()
+    ref = fuse.fuse_numpy(band)
+    assert same_bits(plain[r0:r1], ref)
+    assert same_bits(blurred[r0 + 1:r1 - 1], blur.median_blur3x3(ref)[1:-1])
 
 
 def test_full_size_fusion_layouts_and_range(aoi50):

@@ -293,6 +293,55 @@ def test_dsm_from_points_host_pipeline_equals_device_path():
     assert np.isnan(host[1].cpu().numpy()).all()
 
 
+def _blur_image(rng, H, W):
+    img = rng.integers(-3, 4, (H, W)).astype(np.float32)       # many ties
+    u = rng.random((H, W))
+    img[u < 0.25] = np.nan
+    img[(u >= 0.25) & (u < 0.3)] = -0.0
+    img[(u >= 0.3) & (u < 0.33)] = np.inf
+    img[(u >= 0.33) & (u < 0.36)] = -np.inf
+    return img
+
+
+BLUR_SHAPES = [(1, 1), (1, 2), (1, 9), (9, 1), (2, 2), (3, 5), (5, 6), (4, 7), (6, 10), (7, 13), (33, 70), (40, 1),
+               (1, 41)]
+
+
+@pytest.mark.parametrize('H,W', BLUR_SHAPES)
+def test_median_blur_cv2_network_shapes(H, W):
+    """The standalone blur and the fusion's blur against OpenCV's network (scalar and SSE
+    columns, the 1-D path) on images full of NaN, ties, signed zeros and infinities."""
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3
+    rng = np.random.default_rng(H * 100 + W)
+    img = np.stack([_blur_image(rng, H, W) for _ in range(3)])
+    got = median_blur3x3(img)
+    for b in range(3):
+        assert same_bits(got[b], blur.median_blur3x3(img[b])), b
+    # the fusion's final blur: 3 identical views fuse to the view itself
+    stack = np.repeat(img[0][:, :, None], 3, axis=2)
+    assert same_bits(fuse_dsms(stack, median_blur=True), blur.median_blur3x3(fuse.fuse_numpy(stack)))
+
+
+@pytest.mark.parametrize('H,W', BLUR_SHAPES)
+def test_dsm_epilogue_cv2_network_shapes(H, W):
+    """The fused rasterisation epilogue (nanmax, hole fill, blur in shared memory) on grids
+    of every shape class, including 1-wide and 1-high grids."""
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    rng = np.random.default_rng(H * 1000 + W)
+    xoff, yoff, res = 354000.0, 6182000.0, 1.0
+    n = max(4 * H * W // 3, 1)
+    pts = np.empty((n, 3))
+    pts[:, 0] = xoff + rng.uniform(0, W, n)
+    pts[:, 1] = yoff - rng.uniform(0, H, n)
+    pts[:, 2] = rng.integers(-2, 3, n).astype(np.float64)
+    pts[rng.random(n) < 0.1, 2] = -0.0
+    pts[rng.random(n) < 0.05, 2] = np.inf
+    args = (xoff, yoff, res, res, W, H)
+    got = dsm_from_points(pts, np.array([0, n]), *args).cpu().numpy()[0]
+    assert same_bits(got, blur.median_blur3x3(raster.proj_to_grid(pts, *args).astype(np.float32)))
+
+
 def test_median_blur_matches_oracle():
     from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3
     rng = np.random.default_rng(3)

@@ -7,8 +7,6 @@ through the C ABI, that two calls in a row give exactly what vs_fuse_dsms with a
 workspace gives (fusion is bit-exact), and that grids beyond the array are refused.  The
 file is collected last so that a failure here comes after every other test has run.
 """
-import ctypes
-
 import numpy as np
 import pytest
 import torch
@@ -54,10 +52,20 @@ def test_static_fusion_matches_workspace_fusion(lib):
         assert same_bits(got.cpu().numpy(), ref.cpu().numpy()), f'call {call}'
 
 
-def test_static_fusion_rejects_grids_beyond_its_array(lib):
+@pytest.mark.parametrize('h,w', [
+    (2049, 2048),                                   # one row more than the 2048 x 2048 cells it holds
+    (1 << 32, 1 << 32),                             # h * w wraps to 0 in 64-bit arithmetic
+    (4, (1 << 62) + 1),                             # h * w wraps to 4 cells
+])
+def test_static_fusion_rejects_grids_beyond_its_array(lib, h, w):
     L = lib.lib()
-    h, w = 2049, 2048                               # one row more than the 2048 x 2048 cells it holds
     assert h * w > lib.VS_FUSE_STATIC_MAX_CELLS
-    st = L.vs_fuse_dsms_static(ctypes.c_void_p(1), lib.VS_LAYOUT_VHW, 3, h, w, ctypes.c_void_p(1), 1, None)
+    # real (small) device buffers: if the size check ever regressed, a launch would still
+    # touch only memory this process owns rather than a wild address
+    dsm = torch.zeros(3 * 16, dtype=torch.float32, device='cuda')
+    out = torch.zeros(16, dtype=torch.float32, device='cuda')
+    st = L.vs_fuse_dsms_static(dsm.data_ptr(), lib.VS_LAYOUT_VHW, 3, h, w, out.data_ptr(), 1, None)
+    torch.cuda.synchronize()
     assert st == lib.VS_ERR_ARG
     assert b'exceeds the static scratch' in L.vs_last_error()
+    assert torch.count_nonzero(out).item() == 0

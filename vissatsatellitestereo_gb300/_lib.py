@@ -17,6 +17,7 @@ VS_ERR_CUDA = 2
 VS_ERR_WORKSPACE = 3
 VS_ERR_FACTORIZE = 4
 VS_ERR_DEGENERATE = 5
+VS_ERR_TIMEOUT = 6
 
 VS_PROJ_EXACT = 0
 VS_PROJ_FAST = 1
@@ -53,6 +54,8 @@ SIGNATURES = {
     'vs_rpc_project': (_int, [_vp, _int, _vp, _vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
     'vs_rpc_project_cube_workspace_size': (_sz, [_int]),
     'vs_rpc_project_cube': (_int, [_vp, _int, _vp, _i64, _vp, _int, _vp, _sz, _vp]),
+    'vs_rpc_project_cube_status': (_int, [_vp, _int, _int, _vp]),
+    'vs_set_tc_wait_limit': (None, [ctypes.c_uint]),
     'vs_rpc_inverse_project_workspace_size': (_sz, [_int, _i64]),
     'vs_rpc_inverse_project': (_int, [_vp, _int, _vp, _vp, _vp, _i64, _i64, _int, _vp, _vp, _vp, _int, _vp, _vp, _sz,
                                       _vp]),

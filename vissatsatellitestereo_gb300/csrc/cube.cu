@@ -496,6 +496,7 @@ int launch_mma(const VsRpcCamera *cams, int n_cams, const float *xyz, long long 
 }  // namespace
 
 size_t cube_tc_workspace_bytes(int n_cams);
+int cube_tc_status(const void *ws, int n_cams, cudaStream_t st);
 int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
                    cudaStream_t st);
 
@@ -549,4 +550,10 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
     cube_fp32_kernel<<<static_cast<unsigned>(blocks), kFp32Threads, sh, st>>>(xyz, n, n_cams, w, colrow);
     VS_LAUNCH_CHECK("cube_fp32_kernel");
     return VS_OK;
+}
+
+extern "C" int vs_rpc_project_cube_status(const void *workspace, int n_cams, int variant, void *stream) {
+    VS_REQUIRE(workspace && n_cams > 0 && n_cams <= VS_CUBE_MAX_CAMERAS, "vs_rpc_project_cube_status: bad arguments");
+    if (variant != VS_CUBE_BF16X3_TC) return VS_OK;     // the other variants have no device-side waits
+    return cube_tc_status(workspace, n_cams, as_stream(stream));
 }

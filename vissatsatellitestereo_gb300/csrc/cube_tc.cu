@@ -73,11 +73,15 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned phase) {
     return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase) {
-    for (unsigned it = 0; it < kWaitLimit; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase, unsigned limit = kWaitLimit) {
+    for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
 }
+
+// Polls of the completion wait before a CTA gives up (vs_set_tc_wait_limit; 0 makes every
+// CTA give up at once, which exercises the timeout path).
+unsigned g_tc_wait_limit = kWaitLimit;
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -154,7 +158,7 @@ __global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int
 __global__ void __launch_bounds__(kTcThreads) cube_tc_kernel(const float *__restrict__ xyz, long long n, int n_cams,
                                                             int n_pad, const uint4 *__restrict__ bglob,
                                                             const float2 *__restrict__ denorm, float *__restrict__ out,
-                                                            int *__restrict__ error) {
+                                                            int *__restrict__ error, unsigned wait_limit) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sa = smem;                                  // A: 128 x 64 bf16 (16 KB)
     unsigned char *sb = smem + 128 * kTcRowBytes;              // B: n_pad x 64 bf16
@@ -234,7 +238,7 @@ __global__ void __launch_bounds__(kTcThreads) cube_tc_kernel(const float *__rest
             umma_commit(bar);
         }
         // the outcome of the wait is made block-uniform before anyone leaves the loop
-        const bool done = mbar_wait_bounded(bar, phase);
+        const bool done = mbar_wait_bounded(bar, phase, wait_limit);
         if (__syncthreads_or(!done)) {
             failed = true;
             break;
@@ -263,7 +267,7 @@ __global__ void __launch_bounds__(kTcThreads) cube_tc_kernel(const float *__rest
     }
     if (failed) {
         if (tid == 0) atomicExch(error, 1);
-        mbar_wait_bounded(bar, phase);     // the committed MMAs, if they ever complete
+        mbar_wait_bounded(bar, phase);     // the committed MMAs (full limit) before TMEM is freed
     }
     tc_fence_before();
     __syncthreads();
@@ -278,6 +282,39 @@ size_t cube_tc_workspace_bytes(int n_cams) {
     return static_cast<size_t>(n_pad) * kTcRowBytes + 256 + sizeof(float2) * 2 * n_cams + 256 + 256;
 }
 
+// The workspace layout of the tcgen05 variant: coefficient pieces, denormalisation, error word.
+struct CubeTcWs {
+    __nv_bfloat16 *b;
+    float2 *den;
+    int *err;
+};
+static CubeTcWs carve_cube_tc(void *ws, int n_cams) {
+    const int n_pad = ((4 * n_cams + 15) / 16) * 16;
+    Carver cv(ws);
+    CubeTcWs w;
+    w.b = cv.take<__nv_bfloat16>(static_cast<size_t>(n_pad) * kTcK);
+    w.den = cv.take<float2>(2 * static_cast<size_t>(n_cams));
+    w.err = cv.take<int>(1);
+    return w;
+}
+
+// Reads back the error word of the last tcgen05 launch that used `ws` (synchronises `st`).
+int cube_tc_status(const void *ws, int n_cams, cudaStream_t st) {
+    const CubeTcWs w = carve_cube_tc(const_cast<void *>(ws), n_cams);
+    int h = 0;
+    if (cudaMemcpyAsync(&h, w.err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error("vs_rpc_project_cube_status: reading the error word failed");
+        return VS_ERR_CUDA;
+    }
+    if (h) {
+        set_error("vs_rpc_project_cube: a CTA of the tcgen05 kernel gave up waiting for its tensor-core work; "
+                  "its tiles of colrow were not written");
+        return VS_ERR_TIMEOUT;
+    }
+    return VS_OK;
+}
+
 int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
                    cudaStream_t st) {
     const int n_pad = ((4 * n_cams + 15) / 16) * 16;
@@ -285,10 +322,10 @@ int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long l
         set_error("vs_rpc_project_cube: the tcgen05 variant takes at most 64 cameras (%d given)", n_cams);
         return VS_ERR_ARG;
     }
-    Carver cv(ws);
-    __nv_bfloat16 *b = cv.take<__nv_bfloat16>(static_cast<size_t>(n_pad) * kTcK);
-    float2 *den = cv.take<float2>(2 * static_cast<size_t>(n_cams));
-    int *err = cv.take<int>(1);
+    const CubeTcWs w = carve_cube_tc(ws, n_cams);
+    __nv_bfloat16 *b = w.b;
+    float2 *den = w.den;
+    int *err = w.err;
     if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) {
         set_error("vs_rpc_project_cube: cudaMemsetAsync failed");
         return VS_ERR_CUDA;
@@ -309,9 +346,11 @@ int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long l
     const long long tiles = ceil_div(n, 128);
     const unsigned grid = static_cast<unsigned>(std::max(1LL, std::min<long long>(tiles, 2LL * sm_count())));
     cube_tc_kernel<<<grid, kTcThreads, sh, st>>>(xyz, n, n_cams, n_pad, reinterpret_cast<const uint4 *>(b), den,
-                                                 colrow, err);
+                                                 colrow, err, g_tc_wait_limit);
     VS_LAUNCH_CHECK("cube_tc_kernel");
     return VS_OK;
 }
 
 }  // namespace vs
+
+extern "C" void vs_set_tc_wait_limit(unsigned polls) { vs::g_tc_wait_limit = polls; }

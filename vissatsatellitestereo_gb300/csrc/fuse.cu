@@ -275,14 +275,25 @@ void launch_fuse(const float *dsm, int layout, int V, long long cells, float *ou
 
 using namespace vs;
 
+// Largest grid (cells) the fusion accepts: the float32 grid plus its slack must stay well
+// inside int64 (and size_t) arithmetic.
+constexpr long long kMaxFuseCells = (1LL << 60) / static_cast<long long>(sizeof(float));
+
+// h * w without overflow: 0 when either side is not positive or the product exceeds `limit`.
+static long long checked_cells(int64_t h, int64_t w, long long limit) {
+    if (h <= 0 || w <= 0 || h > limit || w > limit / h) return 0;
+    return static_cast<long long>(h) * w;
+}
+
 extern "C" size_t vs_fuse_dsms_workspace_size(int64_t h, int64_t w) {
-    if (h <= 0 || w <= 0) return 0;
-    return sizeof(float) * static_cast<size_t>(h) * w + 256;
+    const long long cells = checked_cells(h, w, kMaxFuseCells);
+    if (!cells) return 0;
+    return sizeof(float) * static_cast<size_t>(cells) + 256;
 }
 
 extern "C" int vs_fuse_dsms(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
                             int median_blur, void *workspace, size_t workspace_bytes, void *stream) {
-    VS_REQUIRE(h > 0 && w > 0 && n_views > 0 && n_views <= kMaxViewsLocal,
+    VS_REQUIRE(checked_cells(h, w, kMaxFuseCells) > 0 && n_views > 0 && n_views <= kMaxViewsLocal,
                "vs_fuse_dsms: bad sizes views=%lld grid=%lldx%lld", (long long)n_views, (long long)h,
                (long long)w);
     VS_REQUIRE(layout == VS_LAYOUT_HWV || layout == VS_LAYOUT_VHW, "vs_fuse_dsms: bad layout %d", layout);
@@ -331,9 +342,10 @@ float *g_scratch_ptr[kMaxDevices] = {};
 extern "C" int vs_fuse_dsms_static(const float *dsm, int layout, int64_t n_views, int64_t h, int64_t w, float *out,
                                    int median_blur, void *stream) {
     VS_REQUIRE(h > 0 && w > 0, "vs_fuse_dsms_static: bad grid %lldx%lld", (long long)h, (long long)w);
-    VS_REQUIRE(h * w <= VS_FUSE_STATIC_MAX_CELLS,
-               "vs_fuse_dsms_static: grid %lldx%lld = %lld cells exceeds the static scratch of %d cells",
-               (long long)h, (long long)w, (long long)(h * w), VS_FUSE_STATIC_MAX_CELLS);
+    // h and w are bounded before they are multiplied, so no product can wrap
+    VS_REQUIRE(checked_cells(h, w, VS_FUSE_STATIC_MAX_CELLS) > 0,
+               "vs_fuse_dsms_static: grid %lldx%lld exceeds the static scratch of %d cells", (long long)h,
+               (long long)w, VS_FUSE_STATIC_MAX_CELLS);
     if (!median_blur) return vs_fuse_dsms(dsm, layout, n_views, h, w, out, 0, nullptr, 0, stream);
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {

@@ -425,31 +425,56 @@ __global__ void hole_fill_kernel(const double *__restrict__ in, double *__restri
     }
 }
 
-// ---- 3x3 median blur (float32, replicate border, NaN after every number) -----------------
-__device__ __forceinline__ unsigned blur_key(float v) {
-    const unsigned b = __float_as_uint(v);
-    return (b & 0x7fffffffu) > 0x7f800000u ? 0xffffffffu : key_from_float(v);
+// ---- 3x3 median blur: cv2.medianBlur(float32, ksize 3) ---------------------------------
+// OpenCV 4.0's medianBlur_SortNet for ksize 3: Paeth's 9-input median network in
+// Devillard's order (19 compare-exchanges, output p4), replicate border.  Its
+// compare-exchange is `t = a; a = min(a, b); b = max(b, t)`, which decides what NaN does:
+//   * scalar columns (MinMax32f, std::min/std::max): exchanged only when b < a;
+//   * vector columns (MinMaxVec32f, SSE minps/maxps, which return the second operand
+//     unless the comparison holds): kept only when a < b, so ties and NaN exchange.
+// Per row OpenCV runs column 0 scalar, then 4 columns at a time from column 1 while
+// j <= W - 5, then the remaining columns scalar.  A 1-high or 1-wide image is a median
+// of 3 along the line with the scalar op.
+template <bool VEC>
+__device__ __forceinline__ void cv_exchange(float &a, float &b) {
+    const bool x = VEC ? !(a < b) : (b < a);
+    const float t = a;
+    a = x ? b : a;
+    b = x ? t : b;
 }
-__device__ __forceinline__ void sort3(unsigned &a, unsigned &b, unsigned &c) {
-    unsigned lo = min(a, b), hi = max(a, b);
-    a = lo; b = hi;
-    lo = min(b, c); hi = max(b, c);
-    b = lo; c = hi;
-    lo = min(a, b); hi = max(a, b);
-    a = lo; b = hi;
+
+template <bool VEC>
+__device__ __forceinline__ float cv_median9(float p0, float p1, float p2, float p3, float p4, float p5, float p6,
+                                            float p7, float p8) {
+    cv_exchange<VEC>(p1, p2); cv_exchange<VEC>(p4, p5); cv_exchange<VEC>(p7, p8);
+    cv_exchange<VEC>(p0, p1); cv_exchange<VEC>(p3, p4); cv_exchange<VEC>(p6, p7);
+    cv_exchange<VEC>(p1, p2); cv_exchange<VEC>(p4, p5); cv_exchange<VEC>(p7, p8);
+    cv_exchange<VEC>(p0, p3); cv_exchange<VEC>(p5, p8); cv_exchange<VEC>(p4, p7);
+    cv_exchange<VEC>(p3, p6); cv_exchange<VEC>(p1, p4); cv_exchange<VEC>(p2, p5);
+    cv_exchange<VEC>(p4, p7); cv_exchange<VEC>(p4, p2); cv_exchange<VEC>(p6, p4);
+    cv_exchange<VEC>(p4, p2);
+    return p4;
 }
-__device__ __forceinline__ unsigned med3(unsigned a, unsigned b, unsigned c) {
-    return max(min(a, b), min(max(a, b), c));
+
+// p0..p8 = the window row by row; `vec` = the column is one of OpenCV's SSE columns.
+__device__ __forceinline__ float cv_median9(bool vec, float p0, float p1, float p2, float p3, float p4, float p5,
+                                            float p6, float p7, float p8) {
+    return vec ? cv_median9<true>(p0, p1, p2, p3, p4, p5, p6, p7, p8)
+               : cv_median9<false>(p0, p1, p2, p3, p4, p5, p6, p7, p8);
 }
-// Median of 9 from three sorted columns: med3(max of lows, med3 of mids, min of highs).
-__device__ __forceinline__ float median9(unsigned a0, unsigned a1, unsigned a2, unsigned b0,
-                                         unsigned b1, unsigned b2, unsigned c0, unsigned c1,
-                                         unsigned c2) {
-    sort3(a0, a1, a2);
-    sort3(b0, b1, b2);
-    sort3(c0, c1, c2);
-    unsigned k = med3(max(max(a0, b0), c0), med3(a1, b1, c1), min(min(a2, b2), c2));
-    return k == 0xffffffffu ? __uint_as_float(0x7fffffffu) : float_from_key(k);
+
+// The 1-D path (image 1 high or 1 wide): p0, p1, p2 consecutive along the line.
+__device__ __forceinline__ float cv_median3_line(float p0, float p1, float p2) {
+    cv_exchange<false>(p0, p1);
+    cv_exchange<false>(p1, p2);
+    cv_exchange<false>(p0, p1);
+    return p1;
+}
+
+// Columns [1, 1 + 4 nv) of a W-wide image go through OpenCV's 4-lane loop.
+__device__ __forceinline__ bool cv_vector_column(long long c, long long W) {
+    const long long nv = W >= 6 ? (W - 6) / 4 + 1 : 0;
+    return c >= 1 && c < 1 + 4 * nv;
 }
 
 template <typename T>
@@ -468,20 +493,26 @@ __global__ void median_blur3x3_kernel(const T *__restrict__ in, float *__restric
         const T *img = in + plane * H * W;
         const long long rm = r > 0 ? r - 1 : 0, rp = r + 1 < H ? r + 1 : H - 1;
         const long long cm = col > 0 ? col - 1 : 0, cp = col + 1 < W ? col + 1 : W - 1;
-        unsigned k[9];
+        if (H == 1 || W == 1) {
+            // the line runs along the dimension that is longer than 1 (both 1: the value)
+            const long long a = H == 1 ? cm : rm * W, b = H == 1 ? col : r * W, d = H == 1 ? cp : rp * W;
+            out[c] = cv_median3_line(as_f32(img[a]), as_f32(img[b]), as_f32(img[d]));
+            continue;
+        }
+        float p[9];
         const long long rows[3] = {rm, r, rp}, cols[3] = {cm, col, cp};
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) k[3 * b + a] = blur_key(as_f32(img[rows[a] * W + cols[b]]));
-        out[c] = median9(k[0], k[1], k[2], k[3], k[4], k[5], k[6], k[7], k[8]);
+            for (int b = 0; b < 3; ++b) p[3 * a + b] = as_f32(img[rows[a] * W + cols[b]]);
+        out[c] = cv_median9(cv_vector_column(col, W), p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8]);
     }
 }
 
 // ---- fused produce_dsm epilogue: keys -> nanmax -> hole fill -> float32 -> blur ---------
 // One 32x32 output tile per CTA of 32x8 threads (4 outputs per thread, rows ty + 8j).  The
 // key tile carries a 2-cell halo (hole fill needs the 3x3 neighbourhood of each blurred
-// cell's 3x3 neighbourhood); the hole-filled float32 values are staged as blur keys;
+// cell's 3x3 neighbourhood); the hole-filled float32 values are staged for the blur;
 // 32-bit indexing (grid dimensions < 2^31).
 constexpr int TX = 32, TY = 8, TILE_Y = 32;
 constexpr int RAW_W = TX + 4, RAW_H = TILE_Y + 4, FK_W = TX + 2, FK_H = TILE_Y + 2;
@@ -489,7 +520,7 @@ constexpr int RAW_W = TX + 4, RAW_H = TILE_Y + 4, FK_W = TX + 2, FK_H = TILE_Y +
 // Shared-memory working set of one epilogue tile.
 struct EpilogueSmem {
     unsigned long long raw[RAW_H * RAW_W];   // 0: empty cell or outside the image
-    unsigned fk[FK_H][FK_W];                 // blur keys of the hole-filled cells
+    float fk[FK_H][FK_W];                    // hole-filled cells as float32 (the blur's input)
     unsigned short holes[FK_H * FK_W];
     int n_holes;
 };
@@ -523,7 +554,7 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
         const bool in = i < FK_H * FK_W;
         const int ly = i / FK_W, lx = i - ly * FK_W;
         const unsigned long long k = in ? sm.raw[(ly + 1) * RAW_W + lx + 1] : 1ull;
-        if (in && k != kEmptyKey) sm.fk[ly][lx] = blur_key(f64_to_f32(double_from_key(k)));
+        if (in && k != kEmptyKey) sm.fk[ly][lx] = f64_to_f32(double_from_key(k));
         // warp-aggregated append of the empty cells to the hole list
         const unsigned empty = __ballot_sync(0xffffffffu, in && k == kEmptyKey);
         if (empty) {
@@ -548,7 +579,7 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
         bool any = false;
 #pragma unroll
         for (int q = 0; q < 8; ++q) any |= s8[q] != kEmptyKey;
-        sm.fk[ly][lx] = any ? blur_key(f64_to_f32(median8_keys(s8))) : 0xffffffffu;
+        sm.fk[ly][lx] = any ? f64_to_f32(median8_keys(s8)) : __uint_as_float(0x7fffffffu);
     }
     __syncthreads();
     const int c = c0 + tx;
@@ -556,6 +587,7 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
     int xa = tx, xb = tx + 1, xc = tx + 2;
     if (c == 0) xa = xb;                 // replicate border: clamp the neighbours into the image
     if (c == W - 1) xc = xb;
+    const bool vec = cv_vector_column(c, W);
 #pragma unroll
     for (int j = 0; j < TILE_Y / TY; ++j) {
         const int oy = ty + TY * j, r = r0 + oy;
@@ -565,8 +597,13 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
         if (r == H - 1) yc = yb;
         const long long cell = static_cast<long long>(r) * W + c;
         if (next_keys) next_keys[cell] = kEmptyKey;
-        out[cell] = median9(sm.fk[ya][xa], sm.fk[yb][xa], sm.fk[yc][xa], sm.fk[ya][xb], sm.fk[yb][xb], sm.fk[yc][xb],
-                            sm.fk[ya][xc], sm.fk[yb][xc], sm.fk[yc][xc]);
+        if (H == 1)
+            out[cell] = cv_median3_line(sm.fk[yb][xa], sm.fk[yb][xb], sm.fk[yb][xc]);
+        else if (W == 1)
+            out[cell] = cv_median3_line(sm.fk[ya][xb], sm.fk[yb][xb], sm.fk[yc][xb]);
+        else
+            out[cell] = cv_median9(vec, sm.fk[ya][xa], sm.fk[ya][xb], sm.fk[ya][xc], sm.fk[yb][xa], sm.fk[yb][xb],
+                                   sm.fk[yb][xc], sm.fk[yc][xa], sm.fk[yc][xb], sm.fk[yc][xc]);
     }
 }
 

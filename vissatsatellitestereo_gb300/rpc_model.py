@@ -120,7 +120,7 @@ CUBE_VARIANTS = {'fp32': _lib.VS_CUBE_FP32, 'bf16x3': _lib.VS_CUBE_BF16X3, 'tf32
                  'bf16x3_lin': _lib.VS_CUBE_BF16X3_LIN}
 
 
-def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
+def project_cube(meta_dicts, xyz, variant='tf32x3', out=None, check=True):
     """Precision form of ``RPCModel.projection`` for C cameras over one point set already in
     the normalised frame (the monomial x coefficient contraction of lib/rpc_model.py:40-79,
     denormalised as in :164-168).
@@ -131,6 +131,9 @@ def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
     'bf16x3_tc' (BF16X3 on tcgen05), 'bf16x3_lin' (BF16X3 for the higher-order terms, the
     constant and linear terms in FP32).
     ``out``: optional preallocated (C, 2, N) float32 CUDA tensor.
+    ``check``: for 'bf16x3_tc', read the kernel's device-side status back (synchronises the
+    stream) and raise ``VsError`` (VS_ERR_TIMEOUT) if a CTA gave up waiting for the tensor
+    cores; with ``check=False`` the caller reads it later with ``project_cube_status``.
     """
     require_cuda()
     if variant not in CUBE_VARIANTS:
@@ -150,7 +153,16 @@ def project_cube(meta_dicts, xyz, variant='tf32x3', out=None):
     ws_ptr, ws_len = workspace(ws_bytes)
     _lib.call('vs_rpc_project_cube', ptr(cams), C, ptr(pts), n, ptr(out), CUBE_VARIANTS[variant], ws_ptr, ws_len,
               stream_handle())
+    if check and variant == 'bf16x3_tc' and n > 0:
+        project_cube_status(C, variant)
     return out
+
+
+def project_cube_status(n_cams, variant):
+    """Raise ``VsError`` if the last ``project_cube`` call of ``variant`` over ``n_cams``
+    cameras on the current stream reported a device-side timeout (synchronises the stream)."""
+    ws_ptr, _ = workspace(_lib.lib().vs_rpc_project_cube_workspace_size(n_cams))
+    _lib.call('vs_rpc_project_cube_status', ws_ptr, n_cams, CUBE_VARIANTS[variant], stream_handle())
 
 
 def inverse_project_cameras(meta_dicts, col, row, alt, shared=True, normalized=False, max_iter=1000):
