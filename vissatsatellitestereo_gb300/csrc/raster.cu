@@ -254,6 +254,97 @@ __device__ __noinline__ int axis_correct(const long long *thr, int r, long long 
     return r;
 }
 
+// Row/column of a contained axis from the coordinate's bit pattern.  d is the wrapped
+// 64-bit difference of the bit patterns; one unsigned compare with tmax rejects every
+// coordinate off the grid, including those of the other sign or another binade (their
+// wrapped difference is at least the origin's bit pattern, far above tmax, because the
+// grid +-2 cells lies inside the origin's binade) and NaN/inf.
+template <bool FLIP>
+__device__ __forceinline__ bool axis_contained(const FastAxis &a, long long bv, int &r, long long &d, bool &sure) {
+    const unsigned long long ud = FLIP ? static_cast<unsigned long long>(a.off_bits) - static_cast<unsigned long long>(bv)
+                                       : static_cast<unsigned long long>(bv) - static_cast<unsigned long long>(a.off_bits);
+    d = static_cast<long long>(ud);
+    const bool ok = ud < static_cast<unsigned long long>(a.tmax);
+    const unsigned u = static_cast<unsigned>(ud >> a.shift);
+    const float q = __fmul_rn(__uint2float_rn(u), a.scale);
+    const float big = __fadd_rn(q, 12582912.0f);
+    const float fr = __fsub_rn(q, __fsub_rn(big, 12582912.0f));
+    const int rn = static_cast<int>(static_cast<unsigned>(__float_as_int(big)) - 0x4b400000u);
+    r = min(max(rn - (fr < 0.0f ? 1 : 0), 0), a.nm1);
+    sure = fabsf(fr) > __fmaf_rn(a.err_rel, q, a.err_abs);
+    return ok;
+}
+
+// The kPts points of one thread: 3 * kPts raw 64-bit words (x, y, z per point).
+struct PointBlock {
+    long long w[3 * kPts];
+};
+
+__device__ __forceinline__ void load_block(const long long *__restrict__ bits, long long i, long long end,
+                                           PointBlock &b) {
+    const long long *src = bits + 3 * i;
+    if (i + kPts <= end && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+        const longlong2 *s2 = reinterpret_cast<const longlong2 *>(src);
+#pragma unroll
+        for (int k = 0; k < 3 * kPts / 2; ++k) {
+            const longlong2 a = __ldcs(s2 + k);
+            b.w[2 * k] = a.x;
+            b.w[2 * k + 1] = a.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kPts; ++k) {
+            const bool in = i + k < end;
+            b.w[3 * k] = in ? __ldcs(src + 3 * k) : 0ll;
+            b.w[3 * k + 1] = in ? __ldcs(src + 3 * k + 1) : 0ll;
+            b.w[3 * k + 2] = in ? __ldcs(src + 3 * k + 2) : 0x7ff8000000000000ll;
+        }
+    }
+}
+
+// Bins the kPts points of one block (first point index i): cells as 32-bit indices (the
+// grid holds < 2^31 cells), runs of consecutive points in one cell merged before the
+// atomics.
+template <bool FLIP_ROW, bool FLIP_COL>
+__device__ __forceinline__ void bin_block(const PointBlock &b, long long i, const FastAxis &R, const FastAxis &C,
+                                          unsigned ncols, unsigned long long tag, unsigned long long *__restrict__ vk,
+                                          unsigned long long *__restrict__ first) {
+    unsigned cell[kPts];
+    unsigned long long key[kPts];
+    bool okk[kPts];
+#pragma unroll
+    for (int k = 0; k < kPts; ++k) {
+        const unsigned long long zb = static_cast<unsigned long long>(b.w[3 * k + 2]);
+        int r, c;
+        long long dr, dc;
+        bool sr, sc;
+        bool ok = axis_contained<FLIP_ROW>(R, b.w[3 * k + 1], r, dr, sr);
+        ok &= axis_contained<FLIP_COL>(C, b.w[3 * k], c, dc, sc);
+        ok &= !is_nan_bits(zb);
+        if (ok && !sr) r = axis_correct(R.thr, r, dr);
+        if (ok && !sc) c = axis_correct(C.thr, c, dc);
+        const unsigned cl = static_cast<unsigned>(r) * ncols + static_cast<unsigned>(c);
+        const bool zero = (zb << 1) == 0;
+        if (ok && zero) atomicMax(first + cl, tag | (kIdxMask - static_cast<unsigned long long>(i + k)));
+        const unsigned long long kz = (zb >> 63) ? ~zb : (zb | 0x8000000000000000ull);
+        key[k] = ok ? (zero ? kZeroKey : kz) : kEmptyKey;
+        cell[k] = cl;
+        okk[k] = ok;
+    }
+#pragma unroll
+    for (int k = 1; k < kPts; ++k) {     // merge runs of consecutive points in one cell
+        const bool same = okk[k] & okk[k - 1] & (cell[k] == cell[k - 1]);
+        key[k] = same ? max(key[k], key[k - 1]) : key[k];
+        key[k - 1] = same ? kEmptyKey : key[k - 1];
+    }
+#pragma unroll
+    for (int k = 0; k < kPts; ++k)
+        if (key[k] != kEmptyKey) atomicMax(vk + cell[k], key[k]);
+}
+
+// Grid-stride over blocks of kPts points with two register buffers: the loads of the next
+// block are issued before the current one is binned, so every thread keeps 96 bytes in
+// flight while it works (the binning chain alone would leave the loads exposed).
 template <bool FLIP_ROW, bool FLIP_COL>
 __global__ void __launch_bounds__(256) bin_fast_kernel(const double *__restrict__ pts,
                                                        const long long *__restrict__ offsets, int v,
@@ -265,58 +356,19 @@ __global__ void __launch_bounds__(256) bin_fast_kernel(const double *__restrict_
     const long long stride = static_cast<long long>(gridDim.x) * blockDim.x * kPts;
     const unsigned long long tag = epoch_tag(v);
     const FastAxis R = ra, C = ca;
-    const unsigned long long ncols = static_cast<unsigned>(C.nm1 + 1);
+    const unsigned ncols = static_cast<unsigned>(C.nm1 + 1);
     const long long *bits = reinterpret_cast<const long long *>(pts);
-    for (long long i = begin + (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kPts; i < end;
-         i += stride) {
-        long long p[3 * kPts];
-        const long long *src = bits + 3 * i;
-        if (i + kPts <= end && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
-            const longlong2 *s2 = reinterpret_cast<const longlong2 *>(src);
-#pragma unroll
-            for (int k = 0; k < 3 * kPts / 2; ++k) {
-                const longlong2 a = __ldcs(s2 + k);
-                p[2 * k] = a.x;
-                p[2 * k + 1] = a.y;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < kPts; ++k) {
-                const bool in = i + k < end;
-                p[3 * k] = in ? __ldcs(src + 3 * k) : 0ll;
-                p[3 * k + 1] = in ? __ldcs(src + 3 * k + 1) : 0ll;
-                p[3 * k + 2] = in ? __ldcs(src + 3 * k + 2) : 0x7ff8000000000000ll;
-            }
-        }
-        long long cell[kPts];
-        unsigned long long key[kPts];
-#pragma unroll
-        for (int k = 0; k < kPts; ++k) {
-            const unsigned long long zb = static_cast<unsigned long long>(p[3 * k + 2]);
-            int r, c;
-            long long dr, dc;
-            bool sr, sc;
-            bool ok = axis_fast<FLIP_ROW>(R, p[3 * k + 1], r, dr, sr);
-            ok &= axis_fast<FLIP_COL>(C, p[3 * k], c, dc, sc);
-            ok &= !is_nan_bits(zb);
-            if (ok && !sr) r = axis_correct(R.thr, r, dr);
-            if (ok && !sc) c = axis_correct(C.thr, c, dc);
-            const long long cl = static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(r)) * ncols) + c;
-            const bool zero = (zb << 1) == 0;
-            if (ok && zero) atomicMax(first + cl, tag | (kIdxMask - static_cast<unsigned long long>(i + k)));
-            const unsigned long long kz = (zb >> 63) ? ~zb : (zb | 0x8000000000000000ull);
-            key[k] = ok ? (zero ? kZeroKey : kz) : kEmptyKey;
-            cell[k] = ok ? cl : -1 - k;
-        }
-#pragma unroll
-        for (int k = 1; k < kPts; ++k) {     // merge runs of consecutive points in one cell
-            const bool same = cell[k] == cell[k - 1];
-            key[k] = same ? max(key[k], key[k - 1]) : key[k];
-            key[k - 1] = same ? kEmptyKey : key[k - 1];
-        }
-#pragma unroll
-        for (int k = 0; k < kPts; ++k)
-            if (key[k] != kEmptyKey) atomicMax(vk + cell[k], key[k]);
+    long long i = begin + (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kPts;
+    PointBlock a, b;
+    if (i < end) load_block(bits, i, end, a);
+    while (i < end) {
+        if (i + stride < end) load_block(bits, i + stride, end, b);
+        bin_block<FLIP_ROW, FLIP_COL>(a, i, R, C, ncols, tag, vk, first);
+        i += stride;
+        if (i >= end) break;
+        if (i + stride < end) load_block(bits, i + stride, end, a);
+        bin_block<FLIP_ROW, FLIP_COL>(b, i, R, C, ncols, tag, vk, first);
+        i += stride;
     }
 }
 
@@ -716,7 +768,7 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
     long long want = ceil_div(ceil_div(max_points, kPts), threads);
     long long cap = static_cast<long long>(sm_count()) * 8;
     unsigned gx = static_cast<unsigned>(std::max(1LL, std::min(want, cap)));
-    if (tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained) {
+    if (tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained && tb.row.n * tb.col.n < (1LL << 31)) {
         FastAxis fa[2];
         const Axis *ax[2] = {&tb.row, &tb.col};
         for (int a = 0; a < 2; ++a) {
@@ -732,6 +784,16 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
         }
         // rows: a = off - v unless the origin is negative; columns: a = v - off unless negative
         const bool flip_row = !tb.row.neg, flip_col = tb.col.neg != 0;
+        // a resident grid (every CTA streams to the end of the view with its loads pipelined)
+        static int resident = 0;
+        if (!resident) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bin_fast_kernel<true, false>, threads, 0) !=
+                    cudaSuccess || per_sm <= 0)
+                per_sm = 2;
+            resident = per_sm;
+        }
+        gx = static_cast<unsigned>(std::max(1LL, std::min(want, static_cast<long long>(sm_count()) * resident)));
         if (flip_row && !flip_col)
             bin_fast_kernel<true, false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
         else if (flip_row && flip_col)
