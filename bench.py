@@ -589,41 +589,97 @@ def fusion_form(n_views=50, cells=2000, steps=20, warmup=3, nan_frac=0.15, seed=
 
 def plain_aoi_seconds(spec, maps, affines):
     """GPU time of the plain per-view form of one AOI (the reference's structure on the GPU):
-    per view the FP64 point list of its height map, proj_to_grid and the blur, one call
-    each, then the fusion."""
+    per view the FP64 point list of its height map (one kernel, vs_map_points), proj_to_grid
+    and the blur, one call each, then the fusion."""
     import torch
     from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.batch import map_points
     from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3, proj_to_grid
     s = spec
+    pts = torch.empty((s.image * s.image, 3), dtype=torch.float64, device='cuda')
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     dsms = []
     e0.record()
     for m, aff in zip(maps, affines):
-        m = m[:s.image, :s.image]
-        dj = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[None, :]
-        di = (2 * torch.arange(s.image, device='cuda', dtype=torch.int64) + 1 - s.image)[:, None]
-        east = (aff['e0'] + aff['ej'] * dj + aff['ei'] * di).double() * 2.0 ** -28
-        north = (aff['n0'] + aff['nj'] * dj + aff['ni'] * di).double() * 2.0 ** -28
-        pts = torch.stack([east.reshape(-1), north.reshape(-1), m.reshape(-1).double()], dim=1)
+        map_points(m, aff, width=s.image, height=s.image, out=pts)
         d = proj_to_grid(pts, s.xoff, s.yoff, s.res, s.res, s.xsize, s.ysize)
         dsms.append(median_blur3x3(d))
-        del pts, east, north
     fuse_dsms(torch.stack(dsms), median_blur=True, layout='vhw')
     e1.record()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / 1e3
 
 
-def serving_form(n_requests=400, rate=20.0, n_aois=400, budget_gb=150, pool_maps=32, seed=None, plain_aois=3):
+def plain_serve(specs, source, metas, requests, fit_grid=(200, 20), time_limit_s=90.0):
+    """The plain per-view GPU path serving the same arrivals, measured: no resident state, so
+    every request rebuilds its AOI in the reference's structure -- per view the exact
+    RPCModel projection of the AOI's grid, solve_perspective and check_perspective_error,
+    the view's point list (vs_map_points), proj_to_grid and the blur -- then fuses and copies
+    the fused DSM back; one request at a time in arrival order (FIFO), each call a
+    drop-in call of one reference routine.  Stops after `time_limit_s` (reports how many
+    requests it served: their latencies are those of the stream's first requests)."""
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.aggregate_2p5d import fuse_dsms
+    from vissatsatellitestereo_gb300.batch import map_points
+    from vissatsatellitestereo_gb300.check_error import perspective_error_batch
+    from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3, proj_to_grid
+    from vissatsatellitestereo_gb300.rpc_model import RPCModel
+    from vissatsatellitestereo_gb300.solve_perspective import solve_perspective_batch
+
+    def serve_one(a):
+        s = specs[a]
+        g = synth.rpc_sample_grid_torch(metas[a][0], fit_grid[0], fit_grid[1], 'cuda')
+        pts = torch.empty((s.image * s.image, 3), dtype=torch.float64, device='cuda')
+        dsms = torch.empty((s.n_views, s.ysize, s.xsize), dtype=torch.float32, device='cuda')
+        for v, (h, w, hh, aff) in enumerate(source(a)):
+            m = RPCModel(metas[a][v])
+            col, row = m.projection(g['lat'], g['lon'], g['alt'])
+            keep = (col >= 0) & (row >= 0) & (col < m.width) & (row < m.height)
+            K, R, t, st = solve_perspective_batch(g['x'], g['y'], g['z'], col.view(1, -1), row.view(1, -1),
+                                                  keep.view(1, -1))
+            perspective_error_batch(g['x'], g['y'], g['z'], col.view(1, -1), row.view(1, -1), K, R, t,
+                                    keep.view(1, -1))
+            map_points(h, aff, width=w, height=hh, out=pts)
+            dsms[v] = median_blur3x3(proj_to_grid(pts, s.xoff, s.yoff, s.res, s.res, s.xsize, s.ysize))
+        return fuse_dsms(dsms, median_blur=True, layout='vhw').cpu()
+
+    serve_one(requests[0].aoi)                   # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat, busy, served = [], 0.0, 0
+    for r in requests:
+        now = time.perf_counter() - t0
+        if now < r.arrival:
+            time.sleep(r.arrival - now)
+        b0 = time.perf_counter()
+        serve_one(r.aoi)
+        b1 = time.perf_counter()
+        busy += b1 - b0
+        lat.append(b1 - t0 - r.arrival)
+        served += 1
+        if b1 - t0 > time_limit_s:
+            break
+    lat = np.array(lat)
+    pix = sum(specs[r.aoi].n_views * specs[r.aoi].image ** 2 for r in requests[:served])
+    return {'requests_served': served, 'of_requests': len(requests), 'wall_s': round(time.perf_counter() - t0, 3),
+            'p50_latency_ms': round(float(np.percentile(lat, 50)) * 1e3, 2),
+            'p99_latency_ms': round(float(np.percentile(lat, 99)) * 1e3, 2),
+            'mean_service_ms': round(busy / served * 1e3, 2), 'pixels_per_s_busy': pix / busy,
+            'form': 'measured: FIFO, per request per view RPCModel(exact).projection + solve_perspective + '
+                    'check_perspective_error + vs_map_points + proj_to_grid + medianBlur, then fuse_dsms and the '
+                    'copy to the host; no resident state'}
+
+
+def serving_form(n_requests=400, rate=20.0, n_aois=400, budget_gb=150, pool_maps=32, seed=None, slots=3):
     """A stream of AOI fusion requests (Poisson arrivals at `rate`/s, Zipf popularity over a
     catalog of `n_aois` AOIs with config-3 size ranges drawn log-uniformly) served in real
     time with HBM-resident camera sets and per-view DSMs under a `budget_gb` admission
-    budget and continuous batching.  The plain per-view GPU path has no resident state:
-    its latencies come from a FIFO model fed with its measured per-pixel GPU time."""
+    budget, continuous batching and up to `slots` batches in flight; then the same arrivals
+    served by the plain per-view GPU path (measured, no resident state)."""
     import torch
     from vissatsatellitestereo_gb300 import synth
-    from vissatsatellitestereo_gb300.serve import (FusionServer, Request, fifo_latencies, pool_view_source,
-                                                    poisson_stream)
+    from vissatsatellitestereo_gb300.serve import FusionServer, Request, pool_view_source, poisson_stream
     seed = synth.BASE_SEED if seed is None else seed
     specs = synth.make_aoi_catalog(n_aois, seed)
     size = max(s.image for s in specs)
@@ -632,38 +688,21 @@ def serving_form(n_requests=400, rate=20.0, n_aois=400, budget_gb=150, pool_maps
     metas = [synth.aoi_rpc_metas(s) for s in specs]
     source = pool_view_source(specs, pool, affines)
     # warm-up on a throw-away server (library setup, allocator growth)
-    warm = FusionServer(specs, source, metas, budget_bytes=int(budget_gb) << 30)
+    warm = FusionServer(specs, source, metas, budget_bytes=int(budget_gb) << 30, slots=slots)
     warm.run_stream([Request(0, 0, 0.0), Request(1, 1, 0.0)], realtime=False)
     del warm
     torch.cuda.synchronize()
-    srv = FusionServer(specs, source, metas, budget_bytes=int(budget_gb) << 30)
+    srv = FusionServer(specs, source, metas, budget_bytes=int(budget_gb) << 30, slots=slots)
     stream = poisson_stream(n_requests, rate, n_aois, seed)
     stats = srv.run_stream(stream, realtime=True)
-    # plain per-view path: measured on a few AOIs, per-request service = pixels / rate + fuse
-    first = [0]
-    for s in specs:
-        first.append(first[-1] + s.n_views)
-    plain_t, plain_pix = 0.0, 0
-    for a in range(plain_aois):
-        maps = [pool[(first[a] + v) % pool_maps] for v in range(specs[a].n_views)]
-        plain_aoi_seconds(specs[a], maps, affines[a])          # warm
-        plain_t += plain_aoi_seconds(specs[a], maps, affines[a])
-        plain_pix += specs[a].n_views * specs[a].image ** 2
-    per_pixel = plain_t / plain_pix
-    service = [specs[r.aoi].n_views * specs[r.aoi].image ** 2 * per_pixel for r in stream]
-    lat = fifo_latencies([r.arrival for r in stream], service)
-    res = {'workload': f'{n_requests} AOI fusion requests, Poisson {rate}/s, Zipf(1.0) over {n_aois} AOIs '
-                       f'(config-3 ranges, log-uniform), {budget_gb} GB resident budget',
-           'served': stats,
-           'plain_per_view_model': {
-               'per_request_service_ms_mean': round(float(np.mean(service)) * 1e3, 2),
-               'utilisation_at_rate': round(float(np.sum(service) / stream[-1].arrival), 3),
-               'p50_latency_ms': round(float(np.percentile(lat, 50)) * 1e3, 1),
-               'p99_latency_ms': round(float(np.percentile(lat, 99)) * 1e3, 1),
-               'pixels_per_s': 1.0 / per_pixel,
-               'basis': f'FIFO queue of the same arrivals; service = measured plain per-view GPU time per pixel '
-                        f'({plain_aois} AOIs) x the AOI pixels (no resident state)'}}
-    del srv, pool
+    del srv
+    torch.cuda.empty_cache()
+    plain = plain_serve(specs, source, metas, poisson_stream(n_requests, rate, n_aois, seed))
+    res = {'workload': f'{n_requests} AOI fusion requests (config 4 streams 2000), Poisson {rate}/s, Zipf(1.0) '
+                       f'over {n_aois} AOIs (config-3 ranges, log-uniform), {budget_gb} GB resident budget',
+           'served': stats, 'plain_per_view_measured': plain,
+           'p99_speedup_vs_plain': round(plain['p99_latency_ms'] / stats['p99_latency_ms'], 2)}
+    del pool
     torch.cuda.empty_cache()
     return res
 

@@ -107,3 +107,21 @@ def test_plan_rejects_unsupported_grids_and_views():
         AoiBatch([AoiGrid(400000.0, 5000020.0, 0.5, 0.5, 40, 40)], [[MapView(m, 8, 8, big)]])
     with pytest.raises(ValueError):
         AoiBatch([AoiGrid(400000.0, 5000020.0, 0.5, 0.5, 40, 40)], [[MapView(m.double(), 8, 8, aff)]])
+
+
+def test_map_points_kernel_matches_oracle(small_case):
+    """vs_map_points (the plain per-view path's point list) against oracle/maps.map_points,
+    bit-exact, on padded strides; its points through proj_to_grid + blur give the oracle's
+    per-view DSM."""
+    from vissatsatellitestereo_gb300.batch import map_points
+    from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3, proj_to_grid
+    specs, maps, affines, (ref_views, _) = small_case
+    for a, s in enumerate(specs):
+        for k, (m, aff) in enumerate(zip(maps[a], affines[a])):
+            H, W = m.shape
+            store = np.full((H, W + 3), 5.0, dtype=np.float32)
+            store[:, :W] = m
+            pts = map_points(torch.from_numpy(store).cuda(), aff, width=W, height=H)
+            assert same_bits(pts.cpu().numpy(), omaps.map_points(m, aff))
+            d = median_blur3x3(proj_to_grid(pts, s.xoff, s.yoff, s.res, s.res, s.xsize, s.ysize))
+            assert same_bits(d.cpu().numpy() if isinstance(d, torch.Tensor) else d, ref_views[a][k])

@@ -62,3 +62,30 @@ def test_eviction_and_recompute_give_the_same_bits(catalog):
     assert recomputed
     for r in reqs:
         assert same_bits(outs[r.rid], ref[r.aoi])
+
+
+def test_overlapping_batches_match_alone_and_the_oracle(catalog):
+    """Batches of one request each on three streams: every batch starts with a bounded GPU
+    delay (torch.cuda._sleep, ~10 ms), so the host issues the next batches while earlier
+    ones are still on the device -- with hits on AOIs that another in-flight batch is still
+    building.  Every fused DSM (copied back to the host) equals the one served alone and the
+    oracle's."""
+    from vissatsatellitestereo_gb300.serve import FusionServer, Request
+    specs, views_of, ref = catalog
+    aois = [0, 1, 0, 2, 1, 2, 0, 1]
+    _, reqs_a, alone = serve(specs, views_of, aois, batched=False)
+    srv = FusionServer(specs, views_of, budget_bytes=1 << 30, max_batch=1, slots=3)
+    issue = srv.issue
+
+    def delayed_issue(batch):
+        torch.cuda._sleep(20_000_000)           # a fixed number of GPU clock cycles
+        return issue(batch)
+    srv.issue = delayed_issue
+    reqs = [Request(i, a, 0.0) for i, a in enumerate(aois)]
+    stats, outs = srv.run_stream(reqs, realtime=False, keep_outputs=True)
+    assert stats['max_batches_in_flight'] >= 2 and srv.batches == len(aois)
+    assert any(r.hit for r in reqs)
+    for r in reqs:
+        got = outs[r.rid].numpy()
+        assert same_bits(got, alone[r.rid])
+        assert same_bits(got, ref[r.aoi])

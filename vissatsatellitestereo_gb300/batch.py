@@ -178,3 +178,24 @@ class AoiBatch:
     def fused_dsm(self, buf, a):
         g = self.grids[a]
         return buf[self.fused_off[a]:self.fused_off[a + 1]].view(g.ysize, g.xsize)
+
+
+def map_points(heights, affine, width=None, height=None, out=None):
+    """FP64 point list (H*W, 3) [easting, northing, height] of one height-map view in pixel
+    order (``vs_map_points``): the per-view points the plain per-view path rasterises.
+    ``heights``: CUDA float32 (rows, stride) with unit column stride; ``affine``: MapAffine
+    or its dict; the view is heights[:height, :width]."""
+    require_cuda()
+    if not (heights.is_cuda and heights.dtype == torch.float32 and heights.dim() == 2 and heights.stride(1) == 1):
+        raise ValueError('heights must be a 2-D CUDA float32 tensor with unit column stride')
+    height = heights.shape[0] if height is None else int(height)
+    width = heights.shape[1] if width is None else int(width)
+    m = affine if isinstance(affine, MapAffine) else MapAffine(**affine)
+    n = width * height
+    if out is None:
+        out = torch.empty((n, 3), dtype=torch.float64, device='cuda')
+    elif out.shape != (n, 3) or out.dtype != torch.float64 or not out.is_contiguous():
+        raise ValueError('out must be a contiguous (H*W, 3) float64 CUDA tensor')
+    _lib.call('vs_map_points', heights.data_ptr(), heights.stride(0), width, height, m.e0, m.n0, m.ej, m.ei, m.nj,
+              m.ni, out.data_ptr(), stream_handle())
+    return out

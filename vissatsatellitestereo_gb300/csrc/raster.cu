@@ -30,6 +30,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -818,6 +819,25 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
 // So each pixel is binned with integer and FP32 operations only, reading 4 bytes.
 constexpr unsigned long long kMapIdxLimit = 1ull << 28;   // pixels per view
 constexpr unsigned long long kMapZeroSpan = kMapIdxLimit << 1;
+
+// FP64 point list of one height map in pixel order (the plain per-view form's input):
+// pixel (i, j) -> (easting, northing, height) with easting = (e0 + ej (2j+1-W) + ei (2i+1-H))
+// 2^-28 m (exact doubles: the integers stay below 2^53).
+__global__ void map_points_kernel(const float *__restrict__ map, long long stride, int W, int H, long long e0,
+                                  long long n0, long long ej, long long ei, long long nj, long long ni,
+                                  double *__restrict__ pts) {
+    const long long total = static_cast<long long>(W) * H;
+    for (long long p = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; p < total;
+         p += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long i = p / W, j = p - i * W;
+        const long long dj = 2 * j + 1 - W, di = 2 * i + 1 - H;
+        const double east = __ll2double_rn(e0 + ej * dj + ei * di) * 0x1p-28;
+        const double north = __ll2double_rn(n0 + nj * dj + ni * di) * 0x1p-28;
+        pts[3 * p] = east;
+        pts[3 * p + 1] = north;
+        pts[3 * p + 2] = static_cast<double>(map[i * stride + j]);
+    }
+}
 
 struct MapViewDev {
     const float *map;
@@ -1789,5 +1809,23 @@ extern "C" int vs_dsm_from_depth_maps(const float *const *depths, const int64_t 
                                                               static_cast<int>(ysize), static_cast<int>(xsize));
         VS_LAUNCH_CHECK("depth_epilogue_kernel");
     }
+    return VS_OK;
+}
+
+extern "C" int vs_map_points(const float *heights, int64_t row_stride, int width, int height, int64_t e0, int64_t n0,
+                             int64_t ej, int64_t ei, int64_t nj, int64_t ni, double *points, void *stream) {
+    VS_REQUIRE(heights && points && width > 0 && height > 0 && row_stride >= width,
+               "vs_map_points: bad arguments (%dx%d, stride %lld)", width, height, (long long)row_stride);
+    const long long total = static_cast<long long>(width) * height;
+    // |e0| + (|ej| + |ei|) * 2^31 < 2^53 keeps every coordinate an exact double
+    const long long lim = 1LL << 52;
+    VS_REQUIRE(std::llabs(e0) < lim && std::llabs(n0) < lim && std::llabs(ej) < (1LL << 20) &&
+                   std::llabs(ei) < (1LL << 20) && std::llabs(nj) < (1LL << 20) && std::llabs(ni) < (1LL << 20),
+               "vs_map_points: affine map out of the exact range");
+    const int threads = 256;
+    const unsigned g = static_cast<unsigned>(std::min<long long>(ceil_div(total, threads), sm_count() * 16LL));
+    map_points_kernel<<<g, threads, 0, as_stream(stream)>>>(heights, row_stride, width, height, e0, n0, ej, ei, nj, ni,
+                                                            points);
+    VS_LAUNCH_CHECK("map_points_kernel");
     return VS_OK;
 }

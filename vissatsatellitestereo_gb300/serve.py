@@ -4,13 +4,20 @@ A request asks for the fused DSM of one AOI of a catalog (aggregate_2p5d.py:65-8
 the AOI's per-view DSMs of produce_dsm.py:46-58).  The server keeps, per AOI, its camera
 set (the perspective fits of camera_approx.py:150-204) and its partial DSMs (one float32
 DSM per view) resident in HBM under an admission budget, evicting the least recently used
-AOIs that the current batch does not need.  A request for a resident AOI costs one fusion;
-a miss first rasterises all of the AOI's views (one persistent binning launch and one
-epilogue launch for all misses of the batch, straight into the resident stacks) and fits
-its cameras.  Requests are batched continuously: every iteration takes all requests that
-have arrived (up to ``max_batch``), so a burst shares the rasterisation launches.  The
-result of a request does not depend on what it is batched with (every kernel writes only
-its own AOI's buffers).
+AOIs that no batch on the device still needs.  A request for a resident AOI costs one
+fusion; a miss first rasterises all of the AOI's views (one persistent binning launch and
+one epilogue launch for all misses of the batch, straight into the resident stacks) and
+fits its cameras.
+
+Continuous batching with overlap on the device: every iteration takes all requests that
+have arrived (up to ``max_batch``) as one batch and issues its work -- misses, fits,
+fusions and the copy of each fused DSM into pinned host memory -- on one of ``slots``
+CUDA streams, without waiting for it.  The loop then polls the batches' completion events,
+finishes the requests of completed batches (their latency includes the copy back), and
+admits newly arrived requests as soon as a slot is free, so batches run concurrently on
+the GPU.  A batch that needs an AOI another in-flight batch is still materialising waits
+for it on the device (an event), not on the host.  The result of a request does not depend
+on what it is batched or overlapped with (every kernel writes only its own AOI's buffers).
 """
 import collections
 import time
@@ -111,12 +118,22 @@ def pool_view_source(specs, pool, affines):
     return views_of
 
 
+class _InFlight:
+    """A batch whose work is on the device: its requests, host copies, completion event and
+    everything that must stay alive until the event fires."""
+
+    def __init__(self, index, batch, stream, outs, hosts, event, keep, aois):
+        self.index, self.batch, self.stream = index, batch, stream
+        self.outs, self.hosts, self.event, self.keep, self.aois = outs, hosts, event, keep, aois
+
+
 class FusionServer:
     def __init__(self, specs, view_source, metas=None, budget_bytes=150 << 30, max_batch=64, rows_per_item=32,
-                 bin_blocks_per_sm=8, scratch_cap_bytes=32 << 30, fit_grid=(200, 20)):
+                 bin_blocks_per_sm=8, scratch_cap_bytes=16 << 30, fit_grid=(200, 20), slots=3):
         """specs: the AOI catalog (``synth.AoiSpec``: grid and view count); view_source(a):
         the AOI's views as (CUDA float32 heights, width, height, fixed-point affine dict);
-        metas: per AOI the views' RPC meta_dicts (None: no camera fits)."""
+        metas: per AOI the views' RPC meta_dicts (None: no camera fits); slots: batches that
+        may be on the device at once (one CUDA stream each)."""
         self.specs = list(specs)
         self.view_source = view_source
         self.metas = metas
@@ -126,7 +143,11 @@ class FusionServer:
         self.bin_blocks_per_sm = bin_blocks_per_sm
         self.scratch_cap = int(scratch_cap_bytes)
         self.fit_grid = fit_grid
-        self.scratch = torch.empty(0, dtype=torch.uint8, device='cuda')
+        self.slots = max(1, int(slots))
+        self.streams = [torch.cuda.Stream() for _ in range(self.slots)]
+        self.scratch = {}             # stream -> rasterisation scratch
+        self.inflight = []
+        self.max_inflight = 0
         self.pixels = 0               # height-map pixels rasterised
         self.cell_views = 0           # per-view DSM cells produced
         self.fused_cell_views = 0     # cell-views read by fusions
@@ -142,9 +163,12 @@ class FusionServer:
         grids = [AoiGrid(self.specs[a].xoff, self.specs[a].yoff, self.specs[a].res, self.specs[a].res,
                          self.specs[a].xsize, self.specs[a].ysize) for a in aois]
         plan = AoiBatch(grids, [self._views(a, stacks[a]) for a in aois], rows_per_item=self.rows_per_item)
-        if self.scratch.numel() < plan.scratch_bytes:
-            self.scratch = torch.empty(plan.scratch_bytes, dtype=torch.uint8, device='cuda')
-        plan.run(None, self.scratch, bin_blocks_per_sm=self.bin_blocks_per_sm)
+        st = torch.cuda.current_stream()
+        scratch = self.scratch.get(st)
+        if scratch is None or scratch.numel() < plan.scratch_bytes:
+            scratch = torch.empty(plan.scratch_bytes, dtype=torch.uint8, device='cuda')
+            self.scratch[st] = scratch
+        plan.run(None, scratch, bin_blocks_per_sm=self.bin_blocks_per_sm)
         self.pixels += plan.pixels
         self.cell_views += plan.view_cells
         return plan
@@ -159,9 +183,10 @@ class FusionServer:
         return params, err, status
 
     def _materialise(self, misses, pinned):
-        """Admit, rasterise and fit the missing AOIs (rasterisation batched in groups whose
-        key-grid scratch stays under the cap)."""
-        stacks, group, group_bytes, plans = {}, [], 0, []
+        """Admit, rasterise and fit the missing AOIs on the current stream (rasterisation
+        batched in groups whose key-grid scratch stays under the cap).  Returns the plans,
+        which must outlive the work."""
+        stacks, group, group_bytes, plans, states = {}, [], 0, [], []
         for a in misses:
             s = self.specs[a]
             self.store.admit(state_bytes(s), pinned)
@@ -174,16 +199,31 @@ class FusionServer:
             group.append(a)
             group_bytes += need
             cams = self._fit(a) if self.metas is not None else None
-            self.store.put(a, {'stack': stack, 'cameras': cams}, state_bytes(s))
+            state = {'stack': stack, 'cameras': cams, 'stream': torch.cuda.current_stream(), 'ready': None}
+            states.append(state)
+            self.store.put(a, state, state_bytes(s))
         if group:
             plans.append(self._rasterise(group, stacks))
+        ready = torch.cuda.Event()
+        ready.record()
+        for st in states:
+            st['ready'] = ready
         return plans
 
     # ---- requests ---------------------------------------------------------------------
-    def process(self, batch):
-        """Serve one batch of requests; returns their fused DSMs (device tensors)."""
-        self.batches += 1
+    def _pinned(self, batch):
         pinned = {r.aoi for r in batch}
+        for f in self.inflight:
+            pinned |= f.aois
+        return pinned
+
+    def issue(self, batch):
+        """Issue one batch's work on the current stream without waiting for it; returns the
+        fused DSMs (device tensors, valid once the stream reaches them) and the objects that
+        must stay alive until then."""
+        self.batches += 1
+        pinned = self._pinned(batch)
+        st = torch.cuda.current_stream()
         misses = []
         for r in batch:
             hit = r.aoi in self.store and r.aoi not in misses
@@ -197,42 +237,85 @@ class FusionServer:
         plans = self._materialise(misses, pinned) if misses else []
         outs = []
         for r in batch:
-            st = self.store.get(r.aoi)
-            stack = st['stack']
+            state = self.store.get(r.aoi)
+            stack = state['stack']
+            if state['stream'] != st:
+                # built on another stream: order after it on the device, and tell the
+                # allocator that this stream uses the stack too
+                if state['ready'] is not None:
+                    st.wait_event(state['ready'])
+                stack.record_stream(st)
             outs.append(fuse_dsms(stack, median_blur=True, layout='vhw'))
             self.fused_cell_views += stack.numel()
+        return outs, plans
+
+    def process(self, batch):
+        """Serve one batch of requests on the current stream; returns their fused DSMs
+        (device tensors; synchronise the stream before reading them on the host)."""
+        outs, plans = self.issue(batch)
+        torch.cuda.current_stream().synchronize()
         for p in plans:
             p.close()
         return outs
 
+    def _retire(self, f, t_done, outputs, keep_outputs, on_batch):
+        for r, h in zip(f.batch, f.hosts):
+            r.done = t_done
+            r.batch = f.index
+            if keep_outputs:
+                outputs[r.rid] = h
+        if on_batch:
+            on_batch(f.batch, f.hosts)
+        for p in f.keep:
+            p.close()
+
     def run_stream(self, requests, realtime=True, keep_outputs=False, on_batch=None):
         """Serve ``requests`` (sorted by arrival).  In real time, a request cannot be taken
-        before its arrival time; every iteration takes all arrived requests (up to
-        max_batch).  Returns the latency statistics."""
+        before its arrival time.  Each batch (all arrived requests, up to max_batch) goes to
+        a free slot's stream; completed batches are found by polling their events.  A
+        request is done when its fused DSM is in host memory.  Returns the latency
+        statistics (and the host DSMs by request id with ``keep_outputs``)."""
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         outputs = {}
         t0 = time.perf_counter()
-        busy = 0.0
-        while pending:
+        busy, busy_since = 0.0, None
+        next_stream = 0
+        while pending or self.inflight:
             now = time.perf_counter() - t0
-            if realtime and pending[0].arrival > now:
-                time.sleep(min(pending[0].arrival - now, 0.05))
+            for f in [f for f in self.inflight if f.event.query()]:
+                self.inflight.remove(f)
+                self._retire(f, time.perf_counter() - t0, outputs, keep_outputs, on_batch)
+            if not self.inflight and busy_since is not None:
+                busy += time.perf_counter() - t0 - busy_since
+                busy_since = None
+            now = time.perf_counter() - t0
+            if pending and len(self.inflight) < self.slots and (not realtime or pending[0].arrival <= now):
+                batch = []
+                while pending and len(batch) < self.max_batch and (not realtime or pending[0].arrival <= now):
+                    batch.append(pending.popleft())
+                stream = self.streams[next_stream % self.slots]
+                next_stream += 1
+                if busy_since is None:
+                    busy_since = now
+                with torch.cuda.stream(stream):
+                    outs, plans = self.issue(batch)
+                    hosts = []
+                    for o in outs:
+                        h = torch.empty(o.shape, dtype=o.dtype, pin_memory=True)
+                        h.copy_(o, non_blocking=True)
+                        hosts.append(h)
+                    ev = torch.cuda.Event()
+                    ev.record(stream)
+                self.inflight.append(_InFlight(self.batches, batch, stream, outs, hosts, ev, plans,
+                                               {r.aoi for r in batch}))
+                self.max_inflight = max(self.max_inflight, len(self.inflight))
                 continue
-            batch = []
-            while pending and len(batch) < self.max_batch and (not realtime or pending[0].arrival <= now):
-                batch.append(pending.popleft())
-            b0 = time.perf_counter()
-            outs = self.process(batch)
-            torch.cuda.synchronize()
-            b1 = time.perf_counter()
-            busy += b1 - b0
-            for r, o in zip(batch, outs):
-                r.done = b1 - t0
-                r.batch = self.batches
-                if keep_outputs:
-                    outputs[r.rid] = o
-            if on_batch:
-                on_batch(batch, outs)
+            if self.inflight:
+                time.sleep(5e-5)
+            elif pending and realtime:
+                time.sleep(min(max(pending[0].arrival - now, 0.0), 0.05))
+        if busy_since is not None:
+            busy += time.perf_counter() - t0 - busy_since
         wall = time.perf_counter() - t0
         lat = np.array([r.done - r.arrival for r in requests])
         hits = np.array([bool(r.hit) for r in requests])
@@ -244,11 +327,14 @@ class FusionServer:
             'p50_hit_latency_ms': round(float(np.percentile(lat[hits], 50)) * 1e3, 3) if hits.any() else None,
             'p99_miss_latency_ms': round(float(np.percentile(lat[~hits], 99)) * 1e3, 3) if (~hits).any() else None,
             'hit_rate': round(float(hits.mean()), 4), 'evictions': self.store.evictions, 'batches': self.batches,
+            'slots': self.slots, 'max_batches_in_flight': self.max_inflight,
             'resident_gb_end': round(self.store.used / 2 ** 30, 2),
             'pixels_per_s_busy': self.pixels / busy if busy else None,
             'dsm_cells_per_s_busy': self.cell_views / busy if busy else None,
             'fused_cell_views_per_s_busy': self.fused_cell_views / busy if busy else None,
             'rpc_fit_pts_per_s_busy': self.fit_points / busy if busy else None,
+            'latency': 'arrival to the fused DSM in host memory (pinned), polled completion events',
+            'busy': 'wall time during which at least one batch was on the device',
         }
         return (stats, outputs) if keep_outputs else stats
 
