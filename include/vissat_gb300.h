@@ -96,17 +96,19 @@ int vs_rpc_project(const VsRpcCamera *cams, int n_cams, const double *lat, const
                               * FP32 on CUDA cores (the split forms' error sits in the large
                               * linear coefficients): FP32's accuracy, below 1e-3 px, faster
                               * than BF16X6                                                  */
+#define VS_CUBE_BF16X3_LIN_TC 6 /* as BF16X3_LIN with the contraction on tcgen05 (TMEM
+                                 * accumulators, overlapped epilogue), at most 64 cameras     */
 #define VS_CUBE_MAX_CAMERAS 128
 size_t vs_rpc_project_cube_workspace_size(int n_cams);
 int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const float *xyz, int64_t n, float *colrow,
                         int variant, void *workspace, size_t workspace_bytes, void *stream);
 /* Device-side status of the last vs_rpc_project_cube call that used `workspace` (same
  * n_cams and variant): copies its error word back and synchronises `stream`.  VS_OK, or
- * VS_ERR_TIMEOUT when a CTA of the tcgen05 variant gave up its bounded wait for the
+ * VS_ERR_TIMEOUT when a CTA of a tcgen05 variant gave up its bounded wait for the
  * tensor cores (its tiles of colrow are then unwritten).  The other variants have no
  * device-side waits and always report VS_OK.  No counterpart in the reference. */
 int vs_rpc_project_cube_status(const void *workspace, int n_cams, int variant, void *stream);
-/* Polls of the tcgen05 variant's completion wait before a CTA gives up (default 2^24,
+/* Polls of the tcgen05 variants' completion waits before a CTA gives up (default 2^24,
  * far beyond any real completion time); 0 gives up at once, so tests can drive the
  * timeout path without a faulty device.  Process-wide; not thread-safe. */
 void vs_set_tc_wait_limit(unsigned polls);

@@ -1,34 +1,35 @@
-// Precision form of the RPC projection (BF16X3 split products) on the 5th-generation
-// tensor cores: tcgen05.mma with both operands in shared memory and the FP32 accumulators
-// in tensor memory.
+// Precision form of the RPC projection on the 5th-generation tensor cores (tcgen05):
+// the contraction [N x monomials] x [monomials x 4C coefficients] of lib/rpc_model.py:40-79
+// with split bf16 products, FP32 accumulators in tensor memory, and the ratio and
+// denormalisation of RPCModel.projection (lib/rpc_model.py:164-168) in the epilogue.
 //
-// A CTA of 128 threads owns a tile of 128 points at a time.  Each thread computes its
-// point's 20 monomials, splits them into bf16 pieces and writes its row of A into shared
-// memory; the coefficient pieces B (all cameras' 4 polynomials, N = 4 cameras rounded up
-// to 16 columns) are loaded into shared memory once.  One thread issues the K = 64
-// contraction as four 128 x N x 16 MMAs into a TMEM accumulator and commits them to an
-// mbarrier; the four warps then read their 32 lanes (points) back with tcgen05.ld, form
-// num/den, denormalise and stream the col/row planes out (consecutive threads write
-// consecutive points, so the stores coalesce).
+// Split schemes (reduction slot s = 3 j + p of the scheme's j-th monomial, product p):
+//   X3   (VS_CUBE_BF16X3_TC): all 20 monomials, A pieces (hi, lo, hi) x B pieces
+//        (hi, hi, lo) = hh + lh + hl; K = 60 slots padded to 64.
+//   LIN  (VS_CUBE_BF16X3_LIN_TC): the 16 higher-order monomials only (K = 48); the
+//        constant and linear terms -- whose large coefficients carry the split forms'
+//        error -- are added in FP32 in the epilogue (z, x, y, then the constant).
+// Monomials enter the reduction from the highest order down, so the large terms come last.
 //
-// Measured (16 M points x 50 cameras): correct to the bit pattern of BF16X3's error
-// (max 0.0376 px) but 3.3 ms against 1.75 ms for the warp-level mma.sync kernel.  The
-// contraction is tiny (K = 64) and the kernel is bound by its output stream; here every
-// tile runs A-build, MMA and epilogue back to back behind CTA barriers (8 warps per SM),
-// while the warp-level kernel keeps 24 independent warps per SM.  A 256-thread variant
-// (two warps per lane quadrant) measured 3.75 ms.  Overlapping the phases would need a
-// warp-specialised producer/consumer pipeline over two TMEM accumulators.
+// One persistent CTA per SM, two warpgroups (256 threads).  Per tile of 128 points:
+//   1. every thread builds half of a point's A row (bf16 pieces) into shared memory
+//      (two A buffers, canonical no-swizzle K-major layout);
+//   2. one thread issues the K/16 MMAs (M = 128, N = 4C rounded up to 16) into one of two
+//      TMEM accumulators and commits them to that accumulator's mbarrier;
+//   3. meanwhile all threads finish the PREVIOUS tile from the other accumulator: each
+//      warp reads its 32 lanes (points) with tcgen05.ld -- warpgroup 0 the first half of
+//      the cameras, warpgroup 1 the rest -- forms the quotients, denormalises and streams
+//      the col/row planes out (a warp writes 32 consecutive points of a plane).
+// The coefficient tile B (all cameras' pieces, prepared once per call) is copied into
+// shared memory once per CTA by the bulk-copy (TMA) engine.
 //
-// Reduction axis: slot k' = 3q + p for monomial q (0..19) and split product p: A holds
-// (hi, lo, hi)[p] of the monomial, B holds (hi, hi, lo)[p] of the coefficient, so the sum
-// over k' is hh + lh + hl; slots 60..63 are zero.
+// Operand layout (no swizzle, K-major): 8-row x 16-byte core matrices; cores adjacent along
+// K are 128 bytes apart (leading byte offset), along M/N K/8 * 128 bytes (stride offset).
 //
-// Operand layout (no swizzle, K-major): 8-row x 16-byte core matrices, rows of a core
-// 16 bytes apart; cores adjacent along K 128 bytes apart (leading byte offset), cores
-// adjacent along M/N 1024 bytes apart (stride byte offset).
-//
-// Every wait is bounded: a CTA that times out sets the error word, still waits (bounded)
-// for its committed MMAs, frees its tensor memory and returns.
+// Every wait is bounded.  A thread that gives up sets the error word and the CTA stops at
+// its next barrier; before freeing its tensor memory the CTA waits (bounded) for the
+// coefficient copy and for every MMA it committed.  vs_rpc_project_cube_status reads the
+// word back.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -38,11 +39,22 @@
 namespace vs {
 namespace {
 
-constexpr int kTcThreads = 128;     // one warpgroup: thread = TMEM lane = point of the tile
-constexpr int kTcK = 64;            // padded reduction length (bf16)
-constexpr int kTcRowBytes = kTcK * 2;
-constexpr int kTcTmemCols = 256;
+constexpr int kTcThreads = 256;     // two warpgroups
+constexpr int kTcTile = 128;        // points per tile = TMEM lanes
+constexpr int kTcTmemCols = 512;    // two accumulators of up to 256 columns
+constexpr int kTcMaxN = 256;
+constexpr int kTcMaxCams = kTcMaxN / 4;
 constexpr unsigned kWaitLimit = 1u << 24;
+
+template <bool LIN>
+struct TcScheme {
+    static constexpr int kFirst = LIN ? 4 : 0;            // first monomial in the contraction
+    static constexpr int kMonos = 20 - kFirst;
+    static constexpr int kK = LIN ? 48 : 64;              // slots, padded to whole K=16 steps
+    static constexpr int kRowBytes = kK * 2;
+    // monomial of contraction slot group j (highest order first)
+    static __host__ __device__ constexpr int mono(int j) { return 19 - j; }
+};
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -79,10 +91,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase, 
     return false;
 }
 
-// Polls of the completion wait before a CTA gives up (vs_set_tc_wait_limit; 0 makes every
-// CTA give up at once, which exercises the timeout path).
-unsigned g_tc_wait_limit = kWaitLimit;
-
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -100,202 +108,303 @@ __device__ __forceinline__ void umma_commit(unsigned bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(unsigned taddr, float (&v)[16]) {
-    unsigned r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+// 8 consecutive accumulator columns of this thread's lane (complete after tmem_wait)
+__device__ __forceinline__ void tmem_ld8(unsigned taddr, unsigned (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
 }
+__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ float bf16_round(float v) { return __bfloat162float(__float2bfloat16_rn(v)); }
 
-// byte offset of element (row, k) in the canonical layout: [row/8][k/8][row%8][k%8]
-__host__ __device__ __forceinline__ unsigned canon_offset(int row, int k) {
-    return static_cast<unsigned>(((row >> 3) * (kTcK / 8) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+__device__ __forceinline__ unsigned pack_bf16x2(float lo, float hi) {
+    return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 
+// byte offset of element (row, k) in the canonical layout of a K-slot operand:
+// [row/8][k/8][row%8][k%8]
+__host__ __device__ __forceinline__ unsigned canon_offset(int row, int k, int K) {
+    return static_cast<unsigned>(((row >> 3) * (K / 8) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// num / den: approximate reciprocal refined by one residual correction; IEEE division
+// outside the range where that is accurate
+__device__ __noinline__ float tc_quotient_ieee(float num, float den) { return __fdiv_rn(num, den); }
 __device__ __forceinline__ float tc_quotient(float num, float den) {
-    if (fabsf(den) > 1e-30f && fabsf(den) < 1e30f && fabsf(num) < 1e30f) {
-        float r;
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(den));
-        const float q0 = num * r;
-        return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
-    }
-    return __fdiv_rn(num, den);
+    if (__builtin_expect(!(fabsf(den) > 1e-30f && fabsf(den) < 1e30f && fabsf(num) < 1e30f), 0))
+        return tc_quotient_ieee(num, den);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(den));
+    const float q0 = num * r;
+    return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
 }
 
-// B (canonical layout, bf16) and the denormalisation of every output plane
-__global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int n_cams, int n_pad,
-                                       __nv_bfloat16 *__restrict__ b, float2 *__restrict__ denorm) {
-    const int total = n_pad * kTcK;
+// constant + linear terms (RPC order: 1, y, x, z) added to the tensor cores' sum:
+// z, x, y, then the constant
+__device__ __forceinline__ float add_linear(float hot, float4 c, float x, float y, float z) {
+    return __fadd_rn(__fmaf_rn(c.y, y, __fmaf_rn(c.z, x, __fmaf_rn(c.w, z, hot))), c.x);
+}
+
+__device__ __forceinline__ const double *column_poly(const VsRpcCamera &cam, int p) {
+    return p == 0 ? cam.col_num : p == 1 ? cam.col_den : p == 2 ? cam.row_num : cam.row_den;
+}
+
+// The per-call constants in the workspace: B pieces (canonical layout), the (scale,
+// offset) of each output plane, (LIN) the FP32 constant + linear coefficients, and the
+// error word.
+struct CubeTcWs {
+    __nv_bfloat16 *b;          // [n_pad x K]
+    float2 *den;               // [2C]
+    float4 *lin;               // [C][4 polys]
+    int *err;
+};
+
+inline int tc_n_pad(int n_cams) { return ((4 * n_cams + 15) / 16) * 16; }
+
+CubeTcWs carve_cube_tc(void *ws, int n_cams) {
+    Carver cv(ws);
+    CubeTcWs w;
+    w.b = cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * 64);
+    w.den = cv.take<float2>(2 * static_cast<size_t>(n_cams));
+    w.lin = cv.take<float4>(4 * static_cast<size_t>(n_cams));
+    w.err = cv.take<int>(1);
+    return w;
+}
+
+template <bool LIN>
+__global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int n_cams, int n_pad, CubeTcWs w) {
+    using S = TcScheme<LIN>;
+    const int total = n_pad * S::kK;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const int col = i / kTcK, k = i - col * kTcK;
+        const int col = i / S::kK, k = i - col * S::kK;
         const int cam = col >> 2, p = col & 3;
         float v = 0.0f;
-        if (cam < n_cams && k < 60) {
-            const VsRpcCamera &c = cams[cam];
-            const double *poly = p == 0 ? c.col_num : p == 1 ? c.col_den : p == 2 ? c.row_num : c.row_den;
-            const double coef = poly[k / 3];
+        if (cam < n_cams && k < 3 * S::kMonos) {
+            const double coef = column_poly(cams[cam], p)[S::mono(k / 3)];
             const float hi = bf16_round(static_cast<float>(coef));
             const float lo = bf16_round(static_cast<float>(coef - static_cast<double>(hi)));
-            v = (k % 3 == 2) ? lo : hi;
+            v = (k % 3 == 2) ? lo : hi;           // B pieces (hi, hi, lo)
         }
-        b[canon_offset(col, k) / 2] = __float2bfloat16_rn(v);
+        w.b[canon_offset(col, k, S::kK) / 2] = __float2bfloat16_rn(v);
     }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * n_cams; i += gridDim.x * blockDim.x) {
         const VsRpcCamera &c = cams[i >> 1];
-        denorm[i] = (i & 1) == 0 ? make_float2(static_cast<float>(c.col_scale), static_cast<float>(c.col_off))
-                                 : make_float2(static_cast<float>(c.row_scale), static_cast<float>(c.row_off));
+        w.den[i] = (i & 1) == 0 ? make_float2(static_cast<float>(c.col_scale), static_cast<float>(c.col_off))
+                                : make_float2(static_cast<float>(c.row_scale), static_cast<float>(c.row_off));
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * n_cams; i += gridDim.x * blockDim.x) {
+        const double *poly = column_poly(cams[i >> 2], i & 3);
+        w.lin[i] = make_float4(static_cast<float>(poly[0]), static_cast<float>(poly[1]), static_cast<float>(poly[2]),
+                               static_cast<float>(poly[3]));
     }
 }
 
-__global__ void __launch_bounds__(kTcThreads) cube_tc_kernel(const float *__restrict__ xyz, long long n, int n_cams,
-                                                            int n_pad, const uint4 *__restrict__ bglob,
-                                                            const float2 *__restrict__ denorm, float *__restrict__ out,
-                                                            int *__restrict__ error, unsigned wait_limit) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sa = smem;                                  // A: 128 x 64 bf16 (16 KB)
-    unsigned char *sb = smem + 128 * kTcRowBytes;              // B: n_pad x 64 bf16
-    float2 *sden = reinterpret_cast<float2 *>(sb + n_pad * kTcRowBytes);
-    __shared__ __align__(8) unsigned long long mbar;
-    __shared__ unsigned tmem_base;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    // B and the denormalisation into shared memory (visible to the tensor cores' proxy)
-    for (int i = tid; i < n_pad * kTcRowBytes / 16; i += kTcThreads) reinterpret_cast<uint4 *>(sb)[i] = bglob[i];
-    for (int i = tid; i < 2 * n_cams; i += kTcThreads) sden[i] = denorm[i];
-    const unsigned bar = smem_addr(&mbar);
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+// Half H of a point's A row: 16-byte chunks [H * K/16, (H+1) * K/16) of 8 slots each.
+template <bool LIN, int H>
+__device__ __forceinline__ void build_a_half(unsigned char *a_tile, int row, float x, float y, float z) {
+    using S = TcScheme<LIN>;
+    const float yx = y * x, yz = y * z, xz = x * z, yy = y * y, xx = x * x, zz = z * z;
+    const float m[20] = {1.0f,   y,      x,      z,      yx,     yz,     xz,     yy,     xx,     zz,
+                         yx * z, yy * y, y * xx, y * zz, yy * x, xx * x, x * zz, yy * z, xx * z, zz * z};
+    constexpr int kHalfChunks = S::kK / 16;
+#pragma unroll
+    for (int cc = 0; cc < kHalfChunks; ++cc) {
+        const int c = H * kHalfChunks + cc;
+        unsigned words[4];
+#pragma unroll
+        for (int wd = 0; wd < 4; ++wd) {
+            float e[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int k = 8 * c + 2 * wd + q;
+                float v = 0.0f;
+                if (k < 3 * S::kMonos) {
+                    const float mv = m[S::mono(k / 3)];
+                    const float hi = bf16_round(mv);
+                    v = (k % 3 == 1) ? bf16_round(mv - hi) : hi;   // A pieces (hi, lo, hi)
+                }
+                e[q] = v;
+            }
+            words[wd] = pack_bf16x2(e[0], e[1]);
+        }
+        *reinterpret_cast<uint4 *>(a_tile + canon_offset(row, 8 * c, S::kK)) =
+            make_uint4(words[0], words[1], words[2], words[3]);
     }
+}
+
+template <bool LIN>
+__global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__restrict__ xyz, long long n, int n_cams,
+                                                               int n_pad, CubeTcWs w, float *__restrict__ out,
+                                                               unsigned wait_limit) {
+    using S = TcScheme<LIN>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *sb = smem;                                           // B: n_pad x K
+    unsigned char *sa0 = sb + kTcMaxN * S::kRowBytes;                   // A buffers: 128 x K each, adjacent
+    float2 *sden = reinterpret_cast<float2 *>(sb + (kTcMaxN + 2 * kTcTile) * S::kRowBytes);
+    float4 *slin = reinterpret_cast<float4 *>(sden + 2 * kTcMaxCams);
+    __shared__ __align__(8) unsigned long long bar_mma[2], bar_b, bar_drain;
+    __shared__ unsigned tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, lane = tid & 31, wg = tid >> 7;
+    const unsigned b_bytes = static_cast<unsigned>(n_pad * S::kRowBytes);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_mma[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_mma[1])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_b)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_drain)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // B into shared memory by the bulk-copy engine (16-byte aligned, size a multiple of 16)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bar_b)), "r"(b_bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_addr(sb)),
+            "l"(w.b), "r"(b_bytes), "r"(smem_addr(&bar_b))
+            : "memory");
+    }
+    for (int i = tid; i < 2 * n_cams; i += kTcThreads) sden[i] = w.den[i];
+    if (LIN)
+        for (int i = tid; i < 4 * n_cams; i += kTcThreads) slin[i] = w.lin[i];
+    __syncwarp();
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
                      "r"(kTcTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = tmem_base;
+    bool failed = !mbar_wait_bounded(smem_addr(&bar_b), 0, wait_limit);
     const unsigned idesc = umma_idesc_bf16(n_pad);
-    const unsigned a_base = smem_addr(sa), b_base = smem_addr(sb);
-    const long long tiles = (n + 127) / 128;
-    unsigned phase = 0;
-    bool failed = false;
-    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        // ---- A row of this thread's point: 20 monomials -> (hi, lo, hi) bf16 pieces
-        const long long p = tile * 128 + tid;
-        float x = 0.0f, y = 0.0f, z = 0.0f;
-        if (p < n) {
-            x = __ldg(xyz + p);
-            y = __ldg(xyz + n + p);
-            z = __ldg(xyz + 2 * n + p);
-        }
-        const float yx = y * x, yz = y * z, xz = x * z, yy = y * y, xx = x * x, zz = z * z;
-        const float m[20] = {1.0f,   y,      x,      z,      yx,     yz,     xz,     yy,     xx,     zz,
-                             yx * z, yy * y, y * xx, y * zz, yy * x, xx * x, x * zz, yy * z, xx * z, zz * z};
-        unsigned words[kTcK / 2];
-#pragma unroll
-        for (int w = 0; w < kTcK / 2; ++w) {
-            float e[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int k = 2 * w + h;
-                if (k < 60) {
-                    const float mv = m[k / 3];
-                    const float hi = bf16_round(mv);
-                    e[h] = (k % 3 == 1) ? bf16_round(mv - hi) : hi;
-                } else {
-                    e[h] = 0.0f;
-                }
+    const unsigned sbo = static_cast<unsigned>(S::kK / 8 * 128);
+    const unsigned b_base = smem_addr(sb);
+    const long long tiles = (n + kTcTile - 1) / kTcTile;
+    // this warpgroup's cameras: [c_begin, c_end), c_begin even (8-column TMEM loads)
+    const int half = ((n_cams + 1) / 2 + 1) & ~1;
+    const int c_begin = wg == 0 ? 0 : min(half, n_cams), c_end = wg == 0 ? min(half, n_cams) : n_cams;
+    // this thread builds half (wg) of row `row` and finishes the same point: row = TMEM lane
+    const int row = quad * 32 + lane;
+    float px = 0.0f, py = 0.0f, pz = 0.0f;       // the previous tile's point (LIN epilogue)
+    long long prev_tile = -1;
+    int k = 0;
+    for (long long tile = blockIdx.x;; tile += gridDim.x, ++k) {
+        const bool have = tile < tiles;
+        const int buf = k & 1;
+        float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+        if (have && !failed) {
+            const long long p = tile * kTcTile + row;
+            if (p < n) {
+                cx = __ldg(xyz + p);
+                cy = __ldg(xyz + n + p);
+                cz = __ldg(xyz + 2 * n + p);
             }
-            words[w] = __byte_perm(__float_as_uint(e[0]), __float_as_uint(e[1]), 0x7632);
+            unsigned char *a_tile = sa0 + buf * (kTcTile * S::kRowBytes);
+            if (wg == 0) build_a_half<LIN, 0>(a_tile, row, cx, cy, cz);
+            else build_a_half<LIN, 1>(a_tile, row, cx, cy, cz);
         }
-#pragma unroll
-        for (int c = 0; c < kTcK / 8; ++c)
-            *reinterpret_cast<uint4 *>(sa + canon_offset(tid, 8 * c)) =
-                make_uint4(words[4 * c], words[4 * c + 1], words[4 * c + 2], words[4 * c + 3]);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
-        __syncthreads();
+        const bool any_failed = __syncthreads_or(failed) != 0;
         tc_fence_after();
-        // ---- one thread issues the contraction
-        if (tid == 0) {
-#pragma unroll
-            for (int ks = 0; ks < kTcK / 16; ++ks) {
-                const unsigned long long da = umma_desc(a_base + ks * 256, 128, 1024);
-                const unsigned long long db = umma_desc(b_base + ks * 256, 128, 1024);
-                umma_bf16(tmem, da, db, idesc, ks > 0 ? 1u : 0u);
-            }
-            umma_commit(bar);
-        }
-        // the outcome of the wait is made block-uniform before anyone leaves the loop
-        const bool done = mbar_wait_bounded(bar, phase, wait_limit);
-        if (__syncthreads_or(!done)) {
+        if (any_failed) {
             failed = true;
             break;
         }
-        phase ^= 1u;
-        tc_fence_after();
-        // ---- epilogue: warp w reads lanes 32w..32w+31 (its points), 16 columns at a time
-        const unsigned lane_base = tmem + (static_cast<unsigned>(warp * 32) << 16);
-        for (int c0 = 0; c0 < n_pad; c0 += 16) {
-            float v[16];
-            tmem_ld16(lane_base + c0, v);
+        if (have && tid == 0) {
+            const unsigned d = tmem + static_cast<unsigned>(buf * 256);
+            const unsigned a_base = smem_addr(sa0) + static_cast<unsigned>(buf * kTcTile * S::kRowBytes);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int cam = (c0 >> 2) + q;
-                if (cam < n_cams && p < n) {
-                    const float2 dc = sden[2 * cam], dr = sden[2 * cam + 1];
-                    __stcs(out + (2LL * cam) * n + p, __fmaf_rn(tc_quotient(v[4 * q], v[4 * q + 1]), dc.x, dc.y));
-                    __stcs(out + (2LL * cam + 1) * n + p,
-                           __fmaf_rn(tc_quotient(v[4 * q + 2], v[4 * q + 3]), dr.x, dr.y));
+            for (int ks = 0; ks < S::kK / 16; ++ks)
+                umma_bf16(d, umma_desc(a_base + ks * 256, 128, sbo), umma_desc(b_base + ks * 256, 128, sbo), idesc,
+                          ks > 0 ? 1u : 0u);
+            umma_commit(smem_addr(&bar_mma[buf]));
+        }
+        // ---- epilogue of the previous tile (the other accumulator) ----
+        if (prev_tile >= 0) {
+            const int pb = buf ^ 1;
+            const unsigned parity = static_cast<unsigned>(((k - 1) >> 1) & 1);
+            if (!mbar_wait_bounded(smem_addr(&bar_mma[pb]), parity, wait_limit)) {
+                failed = true;
+            } else {
+                tc_fence_after();
+                const long long p = prev_tile * kTcTile + row;
+                const unsigned lane_base = tmem + (static_cast<unsigned>(quad * 32) << 16) + static_cast<unsigned>(pb * 256);
+                for (int cb = c_begin; cb < c_end; cb += 8) {
+                    unsigned r[4][8];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (cb + 2 * j < c_end) tmem_ld8(lane_base + 4 * (cb + 2 * j), r[j]);   // warp-uniform
+                    tmem_wait();
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int cam = cb + 2 * j + h;
+                            if (cam < c_end && p < n) {
+                                float cn = __uint_as_float(r[j][4 * h]), cd = __uint_as_float(r[j][4 * h + 1]);
+                                float rn = __uint_as_float(r[j][4 * h + 2]), rd = __uint_as_float(r[j][4 * h + 3]);
+                                if (LIN) {
+                                    const float4 *lc = slin + 4 * cam;
+                                    cn = add_linear(cn, lc[0], px, py, pz);
+                                    cd = add_linear(cd, lc[1], px, py, pz);
+                                    rn = add_linear(rn, lc[2], px, py, pz);
+                                    rd = add_linear(rd, lc[3], px, py, pz);
+                                }
+                                const float2 dc = sden[2 * cam], dr = sden[2 * cam + 1];
+                                __stcs(out + (2LL * cam) * n + p, __fmaf_rn(tc_quotient(cn, cd), dc.x, dc.y));
+                                __stcs(out + (2LL * cam + 1) * n + p, __fmaf_rn(tc_quotient(rn, rd), dr.x, dr.y));
+                            }
+                        }
                 }
             }
         }
-        tc_fence_before();
-        __syncthreads();   // TMEM and the A tile are free for the next tile
-        tc_fence_after();
+        if (!have) break;
+        prev_tile = tile;
+        px = cx;
+        py = cy;
+        pz = cz;
     }
-    if (failed) {
-        if (tid == 0) atomicExch(error, 1);
-        mbar_wait_bounded(bar, phase);     // the committed MMAs (full limit) before TMEM is freed
-    }
+    if (failed && tid == 0) atomicExch(w.err, 1);
+    // the coefficient copy and every committed MMA have completed before the CTA's shared
+    // and tensor memory are released (bounded waits, full limit)
     tc_fence_before();
     __syncthreads();
+    if (tid == 0) {
+        mbar_wait_bounded(smem_addr(&bar_b), 0);
+        umma_commit(smem_addr(&bar_drain));
+        mbar_wait_bounded(smem_addr(&bar_drain), 0);
+    }
+    __syncthreads();
+    tc_fence_after();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
 }
 
-}  // namespace
-
-size_t cube_tc_workspace_bytes(int n_cams) {
-    const int n_pad = ((4 * n_cams + 15) / 16) * 16;
-    return static_cast<size_t>(n_pad) * kTcRowBytes + 256 + sizeof(float2) * 2 * n_cams + 256 + 256;
+template <bool LIN>
+size_t cube_tc_smem() {
+    using S = TcScheme<LIN>;
+    // at least half of the SM's shared memory: one CTA per SM, which owns all 512 TMEM columns
+    const size_t need = static_cast<size_t>(kTcMaxN + 2 * kTcTile) * S::kRowBytes + sizeof(float2) * 2 * kTcMaxCams +
+                        sizeof(float4) * 4 * kTcMaxCams + 1024;
+    return std::max<size_t>(need, 120 * 1024);
 }
 
-// The workspace layout of the tcgen05 variant: coefficient pieces, denormalisation, error word.
-struct CubeTcWs {
-    __nv_bfloat16 *b;
-    float2 *den;
-    int *err;
-};
-static CubeTcWs carve_cube_tc(void *ws, int n_cams) {
-    const int n_pad = ((4 * n_cams + 15) / 16) * 16;
-    Carver cv(ws);
-    CubeTcWs w;
-    w.b = cv.take<__nv_bfloat16>(static_cast<size_t>(n_pad) * kTcK);
-    w.den = cv.take<float2>(2 * static_cast<size_t>(n_cams));
-    w.err = cv.take<int>(1);
-    return w;
+}  // namespace
+
+// Polls of a completion wait before a thread gives up (vs_set_tc_wait_limit; 0 makes the
+// first wait of every CTA give up at once, which exercises the timeout path).
+unsigned g_tc_wait_limit = kWaitLimit;
+
+size_t cube_tc_workspace_bytes(int n_cams) {
+    Carver cv(nullptr);
+    cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * 64);
+    cv.take<float2>(2 * static_cast<size_t>(n_cams));
+    cv.take<float4>(4 * static_cast<size_t>(n_cams));
+    cv.take<int>(1);
+    return cv.used + 256;
 }
 
 // Reads back the error word of the last tcgen05 launch that used `ws` (synchronises `st`).
@@ -315,40 +424,39 @@ int cube_tc_status(const void *ws, int n_cams, cudaStream_t st) {
     return VS_OK;
 }
 
-int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
-                   cudaStream_t st) {
-    const int n_pad = ((4 * n_cams + 15) / 16) * 16;
-    if (n_pad > 256) {
-        set_error("vs_rpc_project_cube: the tcgen05 variant takes at most 64 cameras (%d given)", n_cams);
+template <bool LIN>
+static int launch_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
+                     cudaStream_t st) {
+    const int n_pad = tc_n_pad(n_cams);
+    if (n_cams > kTcMaxCams) {
+        set_error("vs_rpc_project_cube: the tcgen05 variants take at most %d cameras (%d given)", kTcMaxCams, n_cams);
         return VS_ERR_ARG;
     }
     const CubeTcWs w = carve_cube_tc(ws, n_cams);
-    __nv_bfloat16 *b = w.b;
-    float2 *den = w.den;
-    int *err = w.err;
-    if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) {
+    if (cudaMemsetAsync(w.err, 0, sizeof(int), st) != cudaSuccess) {
         set_error("vs_rpc_project_cube: cudaMemsetAsync failed");
         return VS_ERR_CUDA;
     }
-    cube_tc_prepare_kernel<<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(n_pad) * kTcK, 256)), 256, 0, st>>>(
-        cams, n_cams, n_pad, b, den);
+    cube_tc_prepare_kernel<LIN><<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(n_pad) * TcScheme<LIN>::kK, 256)),
+                                   256, 0, st>>>(cams, n_cams, n_pad, w);
     VS_LAUNCH_CHECK("cube_tc_prepare_kernel");
-    // at least 100 KB of shared memory: at most two CTAs per SM, which share its 512 TMEM
-    // columns (256 each), so no allocation has to wait for another CTA to finish
-    const size_t need_sh = static_cast<size_t>(128 + n_pad) * kTcRowBytes + sizeof(float2) * 2 * n_cams + 1024;
-    const size_t sh = std::max<size_t>(need_sh, 100 * 1024);
-    if (cudaFuncSetAttribute(cube_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sh)) !=
+    const size_t sh = cube_tc_smem<LIN>();
+    if (cudaFuncSetAttribute(cube_tc_kernel<LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sh)) !=
         cudaSuccess) {
         set_error("vs_rpc_project_cube: shared memory request of %zu bytes refused", sh);
         return VS_ERR_CUDA;
     }
-    // two CTAs per SM share its 512 TMEM columns
-    const long long tiles = ceil_div(n, 128);
-    const unsigned grid = static_cast<unsigned>(std::max(1LL, std::min<long long>(tiles, 2LL * sm_count())));
-    cube_tc_kernel<<<grid, kTcThreads, sh, st>>>(xyz, n, n_cams, n_pad, reinterpret_cast<const uint4 *>(b), den,
-                                                 colrow, err, g_tc_wait_limit);
+    const long long tiles = ceil_div(n, static_cast<long long>(kTcTile));
+    const unsigned grid = static_cast<unsigned>(std::max(1LL, std::min<long long>(tiles, sm_count())));
+    cube_tc_kernel<LIN><<<grid, kTcThreads, sh, st>>>(xyz, n, n_cams, n_pad, w, colrow, g_tc_wait_limit);
     VS_LAUNCH_CHECK("cube_tc_kernel");
     return VS_OK;
+}
+
+int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
+                   cudaStream_t st, bool lin) {
+    return lin ? launch_tc<true>(cams, n_cams, xyz, n, colrow, ws, st)
+               : launch_tc<false>(cams, n_cams, xyz, n, colrow, ws, st);
 }
 
 }  // namespace vs

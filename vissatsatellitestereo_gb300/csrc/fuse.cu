@@ -9,11 +9,6 @@
 //          (8 accumulators for 8 <= V <= 128, halving above), started from 0, then the
 //          float32 division by the kept count                     (:78)
 // then optionally the 3x3 median blur (:81), launched from raster.cu's blur kernel.
-//
-// One thread owns one cell; the V values live in registers (V padded to a power of two,
-// template parameter) and are sorted with a bitonic network on order-preserving integer
-// keys (NaN -> all ones, so missing values sort last); the MAD's deviations, taken in
-// sorted order, form a bitonic sequence and need only the merge half of the network.
 // Views beyond 64 use a local-memory path with the same arithmetic.
 #include <algorithm>
 #include <math.h>
@@ -26,158 +21,9 @@ int launch_blur_f32(const float *in, float *out, long long h, long long w, cudaS
 
 namespace {
 
-constexpr unsigned kMissing = 0xffffffffu;
-
-__device__ __forceinline__ unsigned fkey(float v) { return isnan(v) ? kMissing : key_from_float(v); }
-
-template <int N>
-__device__ __forceinline__ void bitonic_sort(unsigned (&a)[N]) {
-#pragma unroll
-    for (int k = 2; k <= N; k <<= 1)
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const unsigned lo = min(a[i], a[l]), hi = max(a[i], a[l]);
-                    if ((i & k) == 0) { a[i] = lo; a[l] = hi; }
-                    else { a[i] = hi; a[l] = lo; }
-                }
-            }
-}
-
-// Sorts a bitonic sequence (a cyclic shift of non-decreasing then non-increasing, e.g.
-// non-increasing then non-decreasing) ascending: the merge half of the bitonic network.
-template <int N>
-__device__ __forceinline__ void bitonic_merge(unsigned (&a)[N]) {
-#pragma unroll
-    for (int j = N >> 1; j > 0; j >>= 1)
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            const int l = i ^ j;
-            if (l > i) {
-                const unsigned lo = min(a[i], a[l]), hi = max(a[i], a[l]);
-                a[i] = lo;
-                a[l] = hi;
-            }
-        }
-}
-
-// select sorted[idx] with compile-time indexing (keeps the array in registers)
-template <int N>
-__device__ __forceinline__ unsigned pick(const unsigned (&a)[N], int idx) {
-    unsigned r = 0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) r = (i == idx) ? a[i] : r;
-    return r;
-}
-
 __device__ __forceinline__ float median_of_sorted(unsigned lo_key, unsigned hi_key) {
     const float lo = float_from_key(lo_key), hi = float_from_key(hi_key);
     return __fdiv_rn(__fadd_rn(__fadd_rn(0.0f, lo), hi), 2.0f);
-}
-
-// numpy float32 pairwise sum of the first V entries of x (V <= 128), plus the outer 0.
-template <int N>
-__device__ __forceinline__ float numpy_sum(const float (&x)[N], int V) {
-    float res;
-    if (V < 8) {
-        res = 0.0f;
-#pragma unroll
-        for (int i = 0; i < (N < 8 ? N : 8); ++i)
-            if (i < V) res = __fadd_rn(res, x[i]);
-    } else {
-        float r[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) r[j] = (j < N) ? x[j] : 0.0f;
-        const int full = V - (V % 8);
-#pragma unroll
-        for (int b = 8; b < N; b += 8)
-            if (b < full)
-#pragma unroll
-                for (int j = 0; j < 8; ++j) r[j] = __fadd_rn(r[j], x[(b + j) < N ? b + j : 0]);
-        res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
-                        __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
-#pragma unroll
-        for (int i = 8; i < N; ++i)
-            if (i >= full && i < V) res = __fadd_rn(res, x[i]);
-    }
-    return __fadd_rn(0.0f, res);
-}
-
-template <int N>
-__device__ float fuse_cell(const float (&x)[N], int V) {
-    unsigned k[N];
-    int n = 0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        k[i] = (i < V) ? fkey(x[i]) : kMissing;
-        n += (k[i] != kMissing);
-    }
-    if (n <= 2) return __int_as_float(0x7fffffff);
-    bitonic_sort(k);
-    const float med = median_of_sorted(pick(k, (n - 1) >> 1), pick(k, n >> 1));
-    // deviations |x - med| of the valid values; NaN deviations (inf - inf) are missing.
-    // With a finite median, the deviations of the sorted values are non-increasing up to
-    // the median and non-decreasing after it (fl(x - med) is monotone in x), and the missing
-    // slots sort last: a bitonic sequence, so one merge sorts it.
-    unsigned dk[N];
-    int nd = 0;
-    float mad = __int_as_float(0x7fffffff);
-    if (isfinite(med)) {
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            const float d = fabsf(__fsub_rn(float_from_key(k[i]), med));
-            dk[i] = (k[i] != kMissing) ? fkey(d) : kMissing;
-        }
-        nd = n;
-        bitonic_merge(dk);
-        mad = median_of_sorted(pick(dk, (nd - 1) >> 1), pick(dk, nd >> 1));
-    } else {
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-            float d = (i < V && !isnan(x[i])) ? fabsf(__fsub_rn(x[i], med)) : __int_as_float(0x7fffffff);
-            dk[i] = fkey(d);
-            nd += (dk[i] != kMissing);
-        }
-        if (nd > 0) {
-            bitonic_sort(dk);
-            mad = median_of_sorted(pick(dk, (nd - 1) >> 1), pick(dk, nd >> 1));
-        }
-    }
-    float kept[N];
-    int cnt = 0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        bool keep = false;
-        if (i < V && !isnan(x[i])) {
-            const float d = fabsf(__fsub_rn(x[i], med));
-            keep = !(d > mad);
-        }
-        kept[i] = keep ? x[i] : 0.0f;
-        cnt += keep;
-    }
-    const float tot = numpy_sum(kept, V);
-    return __fdiv_rn(tot, static_cast<float>(cnt));   // cnt == 0 -> 0/0 = NaN
-}
-
-template <int N>
-__global__ void __launch_bounds__(128) fuse_kernel(const float *__restrict__ dsm, int layout, int V,
-                                                   long long cells, float *__restrict__ out) {
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < cells;
-         c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        float x[N];
-        if (layout == VS_LAYOUT_VHW) {
-#pragma unroll
-            for (int i = 0; i < N; ++i) x[i] = (i < V) ? __ldcs(dsm + i * cells + c) : 0.0f;
-        } else {
-            const float *p = dsm + c * V;
-#pragma unroll
-            for (int i = 0; i < N; ++i) x[i] = (i < V) ? __ldcs(p + i) : 0.0f;
-        }
-        out[c] = fuse_cell(x, V);
-    }
 }
 
 // ---- V > 64: same arithmetic with local arrays -----------------------------------------
@@ -262,25 +108,28 @@ __global__ void fuse_kernel_large(const float *__restrict__ dsm, int layout, int
     }
 }
 
-// ---- tile-staged fusion (V <= 64) ---------------------------------------------------------
-// A CTA of 128 threads fuses tiles of 128 consecutive cells.  The tile's V view rows (or, in
-// the [H][W][V] layout, its 128 x V block) are copied into shared memory with cp.async,
-// double-buffered: the copies of the next tile are in flight while the current one is
-// fused.  Each thread then works on its cell's V values in registers:
-//   * values as float32 with NaN replaced by +inf: the valid values are the n smallest
-//     slots (ties with a valid +inf are the same value), so no key conversion is needed,
-//     and the sign of a zero cannot change ((0 + lo) + hi) / 2, |x - med| or the mask;
-//   * Batcher's odd-even merge sort on N = V rounded up to 8 slots, derived from the
-//     power-of-two network by dropping the comparators that touch a slot >= N (those slots
-//     hold +inf and every comparator puts its maximum on the higher slot, so they never
-//     change);
-//   * the median's two middle order statistics read back from a per-thread row of shared
-//     memory (only ranks <= N/2 can be needed, so only those are stored);
-//   * with a finite median the deviations of the sorted values, +inf beyond n, form a
-//     V shape (fl(x - med) is monotone in x): one bitonic merge sorts them;
-//   * the keep mask and numpy's pairwise mean read the values again from the staged tile.
-// The copies use the hardware's own completion tracking (cp.async.wait_group): no spin
-// waits.
+// ---- fusion for V <= 64 -------------------------------------------------------------------
+// One thread fuses one cell:
+//   * its V values as float32 with NaN replaced by +inf: the valid values are the n
+//     smallest slots (ties with a valid +inf are the same value), so no key conversion is
+//     needed, and the sign of a zero cannot change ((0 + lo) + hi) / 2, |x - med| or the
+//     mask;
+//   * Batcher's odd-even merge sort on N = V rounded up to 4 slots, derived from the
+//     64-slot network by dropping the comparators that touch a slot >= N (those slots hold
+//     +inf and every comparator puts its maximum on the higher slot, so they never change);
+//   * the sorted values go to a per-thread column of shared memory, from which the
+//     median's two middle order statistics are read;
+//   * with a finite median m, the deviations of the sorted values split into two sorted
+//     runs: fl(med - s) for the values left of the middle (ascending from the middle out)
+//     and fl(s - med) for those right of it (fl(x - med) is monotone in x).  The MAD's
+//     order statistics are the k-th and (k+1)-th smallest of the two runs: a binary search
+//     over how many come from the left run (merge path), reading the column;
+//   * the keep mask and numpy's pairwise mean read the values again in view order.
+// The main kernel stages each tile of 128 cells (its V view rows, or its 128 x V block in
+// the [H][W][V] layout) in shared memory with cp.async (the hardware tracks completion:
+// no spin waits); each thread sorts its cell into its column of a view-major scratch
+// block beside the tile (conflict-free) and reads the originals for the mean from the
+// tile.  Unaligned inputs take the same cell code with the values read from global memory.
 constexpr int kTileCells = 128;
 
 __device__ __forceinline__ void cp_async16(float *smem_dst, const float *gmem_src) {
@@ -288,7 +137,6 @@ __device__ __forceinline__ void cp_async16(float *smem_dst, const float *gmem_sr
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 template <int N>
@@ -330,32 +178,16 @@ __device__ __forceinline__ void oems_sort(float (&a)[N]) {
     for (int c = 0; c < kCount; ++c) cmpx(a, net.i[c], net.l[c]);
 }
 
-// Ascending bitonic merge of a V-shaped a[0..N) (power-of-two half-cleaners, slots >= N
-// implicitly +inf).
-template <int N>
-__device__ __forceinline__ void bitonic_merge_asc(float (&a)[N]) {
-    constexpr int P2 = pow2_ceil(N);
-#pragma unroll
-    for (int j = P2 >> 1; j > 0; j >>= 1)
-#pragma unroll
-        for (int i = 0; i < P2; ++i)
-            if ((i & j) == 0 && (i | j) < N) cmpx(a, i, i | j);
+__device__ __forceinline__ float median_pair(float lo, float hi) {
+    return __fdiv_rn(__fadd_rn(__fadd_rn(0.0f, lo), hi), 2.0f);
 }
 
-constexpr int row_slots(int N) { return ((N / 2 + 1 + 3) / 4) * 4; }   // ranks 0..N/2, whole float4s
-constexpr int row_stride(int N) { return row_slots(N) + 4; }          // odd number of float4s: no bank conflicts
-
+// The cell's values: value i at xs[i * si] (shared memory or global); sorted values are
+// written to srt[i * ss] (shared memory); the values are read again, in view order, at
+// xg[i * sg].
 template <int N>
-__device__ __forceinline__ void store_low_ranks(const float (&a)[N], float *row) {
-#pragma unroll
-    for (int q = 0; q < row_slots(N) / 4; ++q)
-        reinterpret_cast<float4 *>(row)[q] =
-            make_float4(a[4 * q], 4 * q + 1 < N ? a[4 * q + 1] : 0.0f, 4 * q + 2 < N ? a[4 * q + 2] : 0.0f,
-                        4 * q + 3 < N ? a[4 * q + 3] : 0.0f);
-}
-
-template <int N>
-__device__ __forceinline__ float fuse_cell_staged(const float *__restrict__ xs, int si, int V, float *row) {
+__device__ __forceinline__ float fuse_cell_v64(const float *xs, long long si, int V, float *srt, int ss,
+                                               const float *__restrict__ xg, long long sg) {
     const float inf = __int_as_float(0x7f800000);
     float a[N];
     int n = 0;
@@ -372,15 +204,33 @@ __device__ __forceinline__ float fuse_cell_staged(const float *__restrict__ xs, 
     }
     if (n <= 2) return __int_as_float(0x7fffffff);
     oems_sort(a);
-    store_low_ranks(a, row);
-    const float med = __fdiv_rn(__fadd_rn(__fadd_rn(0.0f, row[(n - 1) >> 1]), row[n >> 1]), 2.0f);
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        if (i < V) srt[i * ss] = a[i];
+    const float med = median_pair(srt[((n - 1) >> 1) * ss], srt[(n >> 1) * ss]);
     float mad = __int_as_float(0x7fffffff);
     if (isfinite(med)) {
-#pragma unroll
-        for (int i = 0; i < N; ++i) a[i] = i < n ? fabsf(__fsub_rn(a[i], med)) : inf;
-        bitonic_merge_asc(a);
-        store_low_ranks(a, row);
-        mad = __fdiv_rn(__fadd_rn(__fadd_rn(0.0f, row[(n - 1) >> 1]), row[n >> 1]), 2.0f);
+        // left run A_j = med - s[m-1-j] (j < m), right run B_j = s[m+j] - med (j < n-m)
+        const int m = (n & 1) ? (n - 1) >> 1 : n >> 1, nb = n - m;
+        const float *left = srt + (m - 1) * ss, *right = srt + m * ss;
+        const int k = (n - 1) >> 1;
+        int lo = max(0, k + 1 - nb), hi = min(k + 1, m);
+        while (lo < hi) {
+            const int i = (lo + hi) >> 1, j = k + 1 - i;
+            if (__fsub_rn(med, left[-i * ss]) < __fsub_rn(right[(j - 1) * ss], med)) lo = i + 1;
+            else hi = i;
+        }
+        const int i = lo, j = k + 1 - i;
+        const float a_last = i > 0 ? __fsub_rn(med, left[-(i - 1) * ss]) : -inf;
+        const float b_last = j > 0 ? __fsub_rn(right[(j - 1) * ss], med) : -inf;
+        const float kth = fmaxf(a_last, b_last);
+        float nxt = kth;
+        if (!(n & 1)) {
+            const float a_next = i < m ? __fsub_rn(med, left[-i * ss]) : inf;
+            const float b_next = j < nb ? __fsub_rn(right[j * ss], med) : inf;
+            nxt = fminf(a_next, b_next);
+        }
+        mad = median_pair(kth, nxt);
     } else {
         // deviations of the original values (inf - inf is NaN: missing)
         int nd = 0;
@@ -388,7 +238,7 @@ __device__ __forceinline__ float fuse_cell_staged(const float *__restrict__ xs, 
         for (int i = 0; i < N; ++i) {
             float v = inf;
             if (i < V) {
-                const float d = fabsf(__fsub_rn(xs[i * si], med));
+                const float d = fabsf(__fsub_rn(xg[i * sg], med));
                 const bool ok = !isnan(d);
                 nd += ok;
                 v = ok ? d : inf;
@@ -397,15 +247,17 @@ __device__ __forceinline__ float fuse_cell_staged(const float *__restrict__ xs, 
         }
         if (nd > 0) {
             oems_sort(a);
-            store_low_ranks(a, row);
-            mad = __fdiv_rn(__fadd_rn(__fadd_rn(0.0f, row[(nd - 1) >> 1]), row[nd >> 1]), 2.0f);
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+                if (i < V) srt[i * ss] = a[i];
+            mad = median_pair(srt[((nd - 1) >> 1) * ss], srt[(nd >> 1) * ss]);
         }
     }
     // keep |x - med| <= mad (NaN compares false), then numpy's float32 pairwise sum of the
     // kept values (others 0) over the V slots in view order, from 0, / kept count
     int cnt = 0;
     auto kept = [&](int i, float &acc) {
-        const float x = xs[i * si];
+        const float x = xg[i * sg];
         const bool keep = !isnan(x) && !(fabsf(__fsub_rn(x, med)) > mad);
         cnt += keep;
         acc = __fadd_rn(acc, keep ? x : 0.0f);
@@ -428,7 +280,8 @@ __device__ __forceinline__ float fuse_cell_staged(const float *__restrict__ xs, 
         for (int b = 8; b < N; b += 8)
             if (b < full)
 #pragma unroll
-                for (int j = 0; j < 8; ++j) kept(b + j, r[j]);
+                for (int j = 0; j < 8; ++j)
+                    if (b + j < N) kept(b + j, r[j]);
         res = __fadd_rn(__fadd_rn(__fadd_rn(r[0], r[1]), __fadd_rn(r[2], r[3])),
                         __fadd_rn(__fadd_rn(r[4], r[5]), __fadd_rn(r[6], r[7])));
 #pragma unroll
@@ -442,59 +295,62 @@ template <int N>
 __global__ void __launch_bounds__(kTileCells) fuse_tile_kernel(const float *__restrict__ dsm, int layout, int V,
                                                                long long cells, float *__restrict__ out,
                                                                long long n_tiles) {
-    extern __shared__ __align__(16) float fsm[];
+    extern __shared__ __align__(16) float fsm[];           // the tile: V x 128 (VHW) or 128 x V (HWV)
+    float *scratch = fsm + V * kTileCells;                 // sorted columns: N x 128
     const int t = threadIdx.x;
-    const int tile_floats = V * kTileCells;
-    float *buf0 = fsm, *buf1 = fsm + tile_floats;
-    float *row = fsm + 2 * tile_floats + t * row_stride(N);
-    // VHW: value i of cell t at [i][t]; HWV: at [t][i]
-    const int sv = layout == VS_LAYOUT_VHW ? 1 : V, si = layout == VS_LAYOUT_VHW ? kTileCells : 1;
-    auto issue = [&](long long tl, float *dst) {
+    const bool vhw = layout == VS_LAYOUT_VHW;
+    for (long long tl = blockIdx.x; tl < n_tiles; tl += gridDim.x) {
         const long long c0 = tl * kTileCells;
         const int len = static_cast<int>(min(static_cast<long long>(kTileCells), cells - c0));   // multiple of 4
-        if (layout == VS_LAYOUT_VHW) {
+        if (vhw) {
             const int chunks = len >> 2;
             for (int q = t; q < V * (kTileCells / 4); q += kTileCells) {
                 const int v = q / (kTileCells / 4), ch = q - v * (kTileCells / 4);
-                if (ch < chunks) cp_async16(dst + v * kTileCells + 4 * ch, dsm + v * cells + c0 + 4 * ch);
+                if (ch < chunks) cp_async16(fsm + v * kTileCells + 4 * ch, dsm + v * cells + c0 + 4 * ch);
             }
         } else {
             const int chunks = (len * V) >> 2;
-            for (int q = t; q < chunks; q += kTileCells) cp_async16(dst + 4 * q, dsm + c0 * V + 4 * q);
+            for (int q = t; q < chunks; q += kTileCells) cp_async16(fsm + 4 * q, dsm + c0 * V + 4 * q);
         }
         cp_async_commit();
-    };
-    long long tl = blockIdx.x;
-    if (tl < n_tiles) issue(tl, buf0);
-    for (; tl < n_tiles; tl += gridDim.x) {
-        const long long nxt = tl + gridDim.x;
-        if (nxt < n_tiles) issue(nxt, buf1);
-        else cp_async_commit();                    // an empty group keeps "all but the newest" exact
-        cp_async_wait_prev();
+        cp_async_wait_all();
         __syncthreads();
-        const long long c = tl * kTileCells + t;
-        if (c < cells) out[c] = fuse_cell_staged<N>(buf0 + t * sv, si, V, row);
-        __syncthreads();                           // buf0 is refilled next
-        float *tmp = buf0;
-        buf0 = buf1;
-        buf1 = tmp;
+        const long long c = c0 + t;
+        if (c < cells) {
+            const float *col = vhw ? fsm + t : fsm + t * V;
+            const int si = vhw ? kTileCells : 1;
+            out[c] = fuse_cell_v64<N>(col, si, V, scratch + t, kTileCells, col, si);
+        }
+        __syncthreads();                           // the tile is refilled next
     }
-    cp_async_wait_all();
 }
 
-size_t fuse_tile_smem(int V, int N) {
-    return sizeof(float) * (2 * static_cast<size_t>(V) * kTileCells + static_cast<size_t>(kTileCells) * row_stride(N));
+// Unaligned inputs: the values straight from global memory, the sorted column in shared
+// memory (one column per thread, odd stride against bank conflicts).
+template <int N>
+__global__ void __launch_bounds__(kTileCells) fuse_direct_kernel(const float *__restrict__ dsm, int layout, int V,
+                                                                 long long cells, float *__restrict__ out) {
+    __shared__ float cols[kTileCells * (N + 1)];
+    float *col = cols + threadIdx.x * (N + 1);
+    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < cells;
+         c += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const float *xg = layout == VS_LAYOUT_VHW ? dsm + c : dsm + c * V;
+        const long long sg = layout == VS_LAYOUT_VHW ? cells : 1;
+        out[c] = fuse_cell_v64<N>(xg, sg, V, col, 1, xg, sg);
+    }
 }
+
+size_t fuse_tile_smem(int V, int N) { return sizeof(float) * static_cast<size_t>(V + N) * kTileCells; }
 
 template <int N>
-bool launch_fuse_tile(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
+bool launch_fuse_v64(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
     const size_t sh = fuse_tile_smem(V, N);
-    static size_t configured = 0;     // per instantiation: the largest dynamic size set so far
-    if (sh > configured) {
+    static bool configured = false;     // per instantiation: room for the largest tile (V = N)
+    if (!configured) {
         if (cudaFuncSetAttribute(fuse_tile_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(fuse_tile_smem(64, N))) != cudaSuccess)
+                                 static_cast<int>(fuse_tile_smem(N, N))) != cudaSuccess)
             return false;
-        configured = fuse_tile_smem(64, N);
+        configured = true;
     }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fuse_tile_kernel<N>, kTileCells, sh) != cudaSuccess ||
@@ -508,21 +364,42 @@ bool launch_fuse_tile(const float *dsm, int layout, int V, long long cells, floa
 
 // The staged kernel needs 16-byte aligned view rows (VHW) or blocks (HWV).
 bool fuse_tile_ok(const float *dsm, int layout, int V, long long cells) {
-    if (V > 64 || (reinterpret_cast<uintptr_t>(dsm) & 15)) return false;
-    return layout == VS_LAYOUT_VHW ? (cells % 4 == 0) : ((cells % 4 == 0) && ((static_cast<long long>(V) * 4) % 4 == 0));
+    (void)layout;
+    (void)V;
+    return (reinterpret_cast<uintptr_t>(dsm) & 15) == 0 && cells % 4 == 0;
 }
 
-int launch_fuse_staged(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
+int launch_fuse_small(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
+    const bool staged = fuse_tile_ok(dsm, layout, V, cells);
+    if (!staged) {   // unaligned: one 64-slot instantiation (rare inputs)
+        const int threads = kTileCells;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fuse_direct_kernel<64>, threads, 0) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 1;
+        const unsigned g = static_cast<unsigned>(
+            std::max(1LL, std::min<long long>(ceil_div(cells, threads), 1LL * sm_count() * per_sm)));
+        fuse_direct_kernel<64><<<g, threads, 0, st>>>(dsm, layout, V, cells, out);
+        return VS_OK;
+    }
     bool ok = false;
-    switch ((V + 7) / 8) {
-        case 1: ok = launch_fuse_tile<8>(dsm, layout, V, cells, out, st); break;
-        case 2: ok = launch_fuse_tile<16>(dsm, layout, V, cells, out, st); break;
-        case 3: ok = launch_fuse_tile<24>(dsm, layout, V, cells, out, st); break;
-        case 4: ok = launch_fuse_tile<32>(dsm, layout, V, cells, out, st); break;
-        case 5: ok = launch_fuse_tile<40>(dsm, layout, V, cells, out, st); break;
-        case 6: ok = launch_fuse_tile<48>(dsm, layout, V, cells, out, st); break;
-        case 7: ok = launch_fuse_tile<56>(dsm, layout, V, cells, out, st); break;
-        default: ok = launch_fuse_tile<64>(dsm, layout, V, cells, out, st); break;
+    switch ((V + 3) / 4) {
+        case 0: case 1: ok = launch_fuse_v64<4>(dsm, layout, V, cells, out, st); break;
+        case 2: ok = launch_fuse_v64<8>(dsm, layout, V, cells, out, st); break;
+        case 3: ok = launch_fuse_v64<12>(dsm, layout, V, cells, out, st); break;
+        case 4: ok = launch_fuse_v64<16>(dsm, layout, V, cells, out, st); break;
+        case 5: ok = launch_fuse_v64<20>(dsm, layout, V, cells, out, st); break;
+        case 6: ok = launch_fuse_v64<24>(dsm, layout, V, cells, out, st); break;
+        case 7: ok = launch_fuse_v64<28>(dsm, layout, V, cells, out, st); break;
+        case 8: ok = launch_fuse_v64<32>(dsm, layout, V, cells, out, st); break;
+        case 9: ok = launch_fuse_v64<36>(dsm, layout, V, cells, out, st); break;
+        case 10: ok = launch_fuse_v64<40>(dsm, layout, V, cells, out, st); break;
+        case 11: ok = launch_fuse_v64<44>(dsm, layout, V, cells, out, st); break;
+        case 12: ok = launch_fuse_v64<48>(dsm, layout, V, cells, out, st); break;
+        case 13: ok = launch_fuse_v64<52>(dsm, layout, V, cells, out, st); break;
+        case 14: ok = launch_fuse_v64<56>(dsm, layout, V, cells, out, st); break;
+        case 15: ok = launch_fuse_v64<60>(dsm, layout, V, cells, out, st); break;
+        default: ok = launch_fuse_v64<64>(dsm, layout, V, cells, out, st); break;
     }
     if (!ok) {
         set_error("fuse_tile_kernel: launch configuration refused");
@@ -531,13 +408,6 @@ int launch_fuse_staged(const float *dsm, int layout, int V, long long cells, flo
     return VS_OK;
 }
 
-template <int N>
-void launch_fuse(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
-    const int threads = 128;
-    long long want = ceil_div(cells, threads);
-    unsigned g = static_cast<unsigned>(std::min<long long>(want, sm_count() * 16LL));
-    fuse_kernel<N><<<g, threads, 0, st>>>(dsm, layout, V, cells, out);
-}
 
 }  // namespace
 }  // namespace vs
@@ -580,14 +450,10 @@ extern "C" int vs_fuse_dsms(const float *dsm, int layout, int64_t n_views, int64
         dst = static_cast<float *>(workspace);
     }
     const int V = static_cast<int>(n_views);
-    if (fuse_tile_ok(dsm, layout, V, cells)) {
-        const int s = launch_fuse_staged(dsm, layout, V, cells, dst, st);
+    if (V <= 64) {
+        const int s = launch_fuse_small(dsm, layout, V, cells, dst, st);
         if (s != VS_OK) return s;
-    } else if (V <= 8) launch_fuse<8>(dsm, layout, V, cells, dst, st);
-    else if (V <= 16) launch_fuse<16>(dsm, layout, V, cells, dst, st);
-    else if (V <= 32) launch_fuse<32>(dsm, layout, V, cells, dst, st);
-    else if (V <= 64) launch_fuse<64>(dsm, layout, V, cells, dst, st);
-    else {
+    } else {
         const int threads = 64;
         unsigned g = static_cast<unsigned>(std::min<long long>(ceil_div(cells, threads), sm_count() * 8LL));
         fuse_kernel_large<<<g, threads, 0, st>>>(dsm, layout, V, cells, dst);

@@ -117,7 +117,8 @@ def project_cameras(meta_dicts, lat, lon, alt, mode='fast', shared=True, keep=Fa
 
 CUBE_VARIANTS = {'fp32': _lib.VS_CUBE_FP32, 'bf16x3': _lib.VS_CUBE_BF16X3, 'tf32x3': _lib.VS_CUBE_TF32X3,
                  'bf16x6': _lib.VS_CUBE_BF16X6, 'bf16x3_tc': _lib.VS_CUBE_BF16X3_TC,
-                 'bf16x3_lin': _lib.VS_CUBE_BF16X3_LIN}
+                 'bf16x3_lin': _lib.VS_CUBE_BF16X3_LIN, 'bf16x3_lin_tc': _lib.VS_CUBE_BF16X3_LIN_TC}
+TC_VARIANTS = ('bf16x3_tc', 'bf16x3_lin_tc')
 
 
 def project_cube(meta_dicts, xyz, variant='tf32x3', out=None, check=True):
@@ -129,9 +130,10 @@ def project_cube(meta_dicts, xyz, variant='tf32x3', out=None, check=True):
     Returns a CUDA float32 tensor (C, 2, N): col plane then row plane per camera.
     ``variant``: 'fp32' (CUDA cores), 'bf16x3', 'tf32x3', 'bf16x6' (tensor-core split forms),
     'bf16x3_tc' (BF16X3 on tcgen05), 'bf16x3_lin' (BF16X3 for the higher-order terms, the
-    constant and linear terms in FP32).
+    constant and linear terms in FP32), 'bf16x3_lin_tc' (the same with the contraction on
+    tcgen05).
     ``out``: optional preallocated (C, 2, N) float32 CUDA tensor.
-    ``check``: for 'bf16x3_tc', read the kernel's device-side status back (synchronises the
+    ``check``: for the tcgen05 variants, read the kernel's device-side status back (synchronises the
     stream) and raise ``VsError`` (VS_ERR_TIMEOUT) if a CTA gave up waiting for the tensor
     cores; with ``check=False`` the caller reads it later with ``project_cube_status``.
     """
@@ -153,7 +155,7 @@ def project_cube(meta_dicts, xyz, variant='tf32x3', out=None, check=True):
     ws_ptr, ws_len = workspace(ws_bytes)
     _lib.call('vs_rpc_project_cube', ptr(cams), C, ptr(pts), n, ptr(out), CUBE_VARIANTS[variant], ws_ptr, ws_len,
               stream_handle())
-    if check and variant == 'bf16x3_tc' and n > 0:
+    if check and variant in TC_VARIANTS and n > 0:
         project_cube_status(C, variant)
     return out
 
