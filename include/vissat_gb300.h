@@ -303,7 +303,8 @@ void vs_aoi_batch_destroy(VsAoiBatch *plan);
  * easting = (e0 + ej (2j+1-W) + ei (2i+1-H)) 2^-28, northing likewise with n0, nj, ni.
  * The per-view point list the reference builds from a depth map (aggregate_2p5d_util.py:75-98,
  * vs_depth_to_points here) in the synthetic height-map form, for the plain per-view path
- * (points -> vs_proj_to_grid -> blur).  |ej|, |ei|, |nj|, |ni| < 2^20 and |e0|, |n0| < 2^52. */
+ * (points -> vs_proj_to_grid -> blur).  Requires |e0| + |ej| W + |ei| H < 2^52 (and the same
+ * for n0, nj, ni), so that every coordinate is an exact double. */
 int vs_map_points(const float *heights, int64_t row_stride, int width, int height, int64_t e0, int64_t n0,
                   int64_t ej, int64_t ei, int64_t nj, int64_t ni, double *points, void *stream);
 

@@ -11,15 +11,16 @@
 //        error -- are added in FP32 in the epilogue (z, x, y, then the constant).
 // Monomials enter the reduction from the highest order down, so the large terms come last.
 //
-// One persistent CTA per SM, two warpgroups (256 threads).  Per tile of 128 points:
-//   1. every thread builds half of a point's A row (bf16 pieces) into shared memory
-//      (two A buffers, canonical no-swizzle K-major layout);
+// One persistent CTA per SM, four warpgroups (512 threads).  Per tile of 128 points:
+//   1. four threads build a point's A row (bf16 pieces) into shared memory (two A
+//      buffers, canonical no-swizzle K-major layout);
 //   2. one thread issues the K/16 MMAs (M = 128, N = 4C rounded up to 16) into one of two
 //      TMEM accumulators and commits them to that accumulator's mbarrier;
 //   3. meanwhile all threads finish the PREVIOUS tile from the other accumulator: each
-//      warp reads its 32 lanes (points) with tcgen05.ld -- warpgroup 0 the first half of
-//      the cameras, warpgroup 1 the rest -- forms the quotients, denormalises and streams
-//      the col/row planes out (a warp writes 32 consecutive points of a plane).
+//      warp reads its 32 lanes (points) with tcgen05.ld -- warpgroup g a quarter of the
+//      cameras -- forms the quotients (the fast form for a chunk of 8 cameras at once, one
+//      warp-uniform check for rare operands), denormalises and streams the col/row planes
+//      out (a warp writes 32 consecutive points of a plane).
 // The coefficient tile B (all cameras' pieces, prepared once per call) is copied into
 // shared memory once per CTA by the bulk-copy (TMA) engine.
 //
@@ -39,7 +40,8 @@
 namespace vs {
 namespace {
 
-constexpr int kTcThreads = 256;     // two warpgroups
+constexpr int kTcThreads = 512;     // four warpgroups
+constexpr int kTcGroups = kTcThreads / 128;
 constexpr int kTcTile = 128;        // points per tile = TMEM lanes
 constexpr int kTcTmemCols = 512;    // two accumulators of up to 256 columns
 constexpr int kTcMaxN = 256;
@@ -132,14 +134,6 @@ __host__ __device__ __forceinline__ unsigned canon_offset(int row, int k, int K)
 // num / den: approximate reciprocal refined by one residual correction; IEEE division
 // outside the range where that is accurate
 __device__ __noinline__ float tc_quotient_ieee(float num, float den) { return __fdiv_rn(num, den); }
-__device__ __forceinline__ float tc_quotient(float num, float den) {
-    if (__builtin_expect(!(fabsf(den) > 1e-30f && fabsf(den) < 1e30f && fabsf(num) < 1e30f), 0))
-        return tc_quotient_ieee(num, den);
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(den));
-    const float q0 = num * r;
-    return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
-}
 
 // constant + linear terms (RPC order: 1, y, x, z) added to the tensor cores' sum:
 // z, x, y, then the constant
@@ -201,17 +195,15 @@ __global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int
     }
 }
 
-// Half H of a point's A row: 16-byte chunks [H * K/16, (H+1) * K/16) of 8 slots each.
-template <bool LIN, int H>
-__device__ __forceinline__ void build_a_half(unsigned char *a_tile, int row, float x, float y, float z) {
+// Part P of a point's A row: the 16-byte chunks c (8 slots each) with c % 4 == P.
+template <bool LIN, int P>
+__device__ __forceinline__ void build_a_part(unsigned char *a_tile, int row, float x, float y, float z) {
     using S = TcScheme<LIN>;
     const float yx = y * x, yz = y * z, xz = x * z, yy = y * y, xx = x * x, zz = z * z;
     const float m[20] = {1.0f,   y,      x,      z,      yx,     yz,     xz,     yy,     xx,     zz,
                          yx * z, yy * y, y * xx, y * zz, yy * x, xx * x, x * zz, yy * z, xx * z, zz * z};
-    constexpr int kHalfChunks = S::kK / 16;
 #pragma unroll
-    for (int cc = 0; cc < kHalfChunks; ++cc) {
-        const int c = H * kHalfChunks + cc;
+    for (int c = P; c < S::kK / 8; c += kTcGroups) {
         unsigned words[4];
 #pragma unroll
         for (int wd = 0; wd < 4; ++wd) {
@@ -234,6 +226,16 @@ __device__ __forceinline__ void build_a_half(unsigned char *a_tile, int row, flo
     }
 }
 
+__device__ __forceinline__ bool quotient_fast_ok(float num, float den) {
+    return fabsf(den) > 1e-30f && fabsf(den) < 1e30f && fabsf(num) < 1e30f;
+}
+__device__ __forceinline__ float quotient_fast(float num, float den) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(den));
+    const float q0 = num * r;
+    return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
+}
+
 template <bool LIN>
 __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__restrict__ xyz, long long n, int n_cams,
                                                                int n_pad, CubeTcWs w, float *__restrict__ out,
@@ -246,7 +248,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
     float4 *slin = reinterpret_cast<float4 *>(sden + 2 * kTcMaxCams);
     __shared__ __align__(8) unsigned long long bar_mma[2], bar_b, bar_drain;
     __shared__ unsigned tmem_base;
-    const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, lane = tid & 31, wg = tid >> 7;
+    const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, lane = tid & 31, grp = tid >> 7;
     const unsigned b_bytes = static_cast<unsigned>(n_pad * S::kRowBytes);
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_mma[0])) : "memory");
@@ -282,28 +284,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
     const unsigned sbo = static_cast<unsigned>(S::kK / 8 * 128);
     const unsigned b_base = smem_addr(sb);
     const long long tiles = (n + kTcTile - 1) / kTcTile;
-    // this warpgroup's cameras: [c_begin, c_end), c_begin even (8-column TMEM loads)
-    const int half = ((n_cams + 1) / 2 + 1) & ~1;
-    const int c_begin = wg == 0 ? 0 : min(half, n_cams), c_end = wg == 0 ? min(half, n_cams) : n_cams;
-    // this thread builds half (wg) of row `row` and finishes the same point: row = TMEM lane
+    // this warpgroup's cameras: [c_begin, c_end), boundaries even (8-column TMEM loads)
+    const int c_begin = min(((grp * n_cams / kTcGroups) + 1) & ~1, n_cams);
+    const int c_end = min((((grp + 1) * n_cams / kTcGroups) + 1) & ~1, n_cams);
+    // this thread builds part `grp` of row `row` and finishes the same point: row = TMEM lane
     const int row = quad * 32 + lane;
     float px = 0.0f, py = 0.0f, pz = 0.0f;       // the previous tile's point (LIN epilogue)
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;       // this tile's point, loaded one iteration ahead
+    {
+        const long long p = static_cast<long long>(blockIdx.x) * kTcTile + row;
+        if (p < n) {
+            nx = __ldg(xyz + p);
+            ny = __ldg(xyz + n + p);
+            nz = __ldg(xyz + 2 * n + p);
+        }
+    }
     long long prev_tile = -1;
     int k = 0;
     for (long long tile = blockIdx.x;; tile += gridDim.x, ++k) {
         const bool have = tile < tiles;
         const int buf = k & 1;
-        float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+        const float cx = nx, cy = ny, cz = nz;
         if (have && !failed) {
-            const long long p = tile * kTcTile + row;
-            if (p < n) {
-                cx = __ldg(xyz + p);
-                cy = __ldg(xyz + n + p);
-                cz = __ldg(xyz + 2 * n + p);
-            }
             unsigned char *a_tile = sa0 + buf * (kTcTile * S::kRowBytes);
-            if (wg == 0) build_a_half<LIN, 0>(a_tile, row, cx, cy, cz);
-            else build_a_half<LIN, 1>(a_tile, row, cx, cy, cz);
+            switch (grp) {
+                case 0: build_a_part<LIN, 0>(a_tile, row, cx, cy, cz); break;
+                case 1: build_a_part<LIN, 1>(a_tile, row, cx, cy, cz); break;
+                case 2: build_a_part<LIN, 2>(a_tile, row, cx, cy, cz); break;
+                default: build_a_part<LIN, 3>(a_tile, row, cx, cy, cz); break;
+            }
+            // the next tile's point, in flight during this iteration's epilogue
+            const long long p = (tile + gridDim.x) * kTcTile + row;
+            nx = ny = nz = 0.0f;
+            if (p < n) {
+                nx = __ldg(xyz + p);
+                ny = __ldg(xyz + n + p);
+                nz = __ldg(xyz + 2 * n + p);
+            }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
@@ -338,26 +355,46 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
                     for (int j = 0; j < 4; ++j)
                         if (cb + 2 * j < c_end) tmem_ld8(lane_base + 4 * (cb + 2 * j), r[j]);   // warp-uniform
                     tmem_wait();
+                    // quotients of the chunk's 8 cameras, branch-free; one warp-uniform check
+                    // sends rare operands (|den| outside [1e-30, 1e30], |num| >= 1e30) to IEEE
+                    // division
+                    float num[16], den[16], q[16];
+                    bool ok = true;
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
 #pragma unroll
                         for (int h = 0; h < 2; ++h) {
-                            const int cam = cb + 2 * j + h;
-                            if (cam < c_end && p < n) {
-                                float cn = __uint_as_float(r[j][4 * h]), cd = __uint_as_float(r[j][4 * h + 1]);
-                                float rn = __uint_as_float(r[j][4 * h + 2]), rd = __uint_as_float(r[j][4 * h + 3]);
+                            const int cam = min(cb + 2 * j + h, c_end - 1);
+#pragma unroll
+                            for (int pl = 0; pl < 2; ++pl) {
+                                float nu = __uint_as_float(r[j][4 * h + 2 * pl]);
+                                float de = __uint_as_float(r[j][4 * h + 2 * pl + 1]);
                                 if (LIN) {
-                                    const float4 *lc = slin + 4 * cam;
-                                    cn = add_linear(cn, lc[0], px, py, pz);
-                                    cd = add_linear(cd, lc[1], px, py, pz);
-                                    rn = add_linear(rn, lc[2], px, py, pz);
-                                    rd = add_linear(rd, lc[3], px, py, pz);
+                                    nu = add_linear(nu, slin[4 * cam + 2 * pl], px, py, pz);
+                                    de = add_linear(de, slin[4 * cam + 2 * pl + 1], px, py, pz);
                                 }
-                                const float2 dc = sden[2 * cam], dr = sden[2 * cam + 1];
-                                __stcs(out + (2LL * cam) * n + p, __fmaf_rn(tc_quotient(cn, cd), dc.x, dc.y));
-                                __stcs(out + (2LL * cam + 1) * n + p, __fmaf_rn(tc_quotient(rn, rd), dr.x, dr.y));
+                                const int e = 2 * (2 * j + h) + pl;
+                                num[e] = nu;
+                                den[e] = de;
+                                q[e] = quotient_fast(nu, de);
+                                ok = ok && (cb + 2 * j + h >= c_end || quotient_fast_ok(nu, de));
                             }
                         }
+                    if (__builtin_expect(!__all_sync(0xffffffffu, ok), 0)) {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e)
+                            if (!quotient_fast_ok(num[e], den[e])) q[e] = tc_quotient_ieee(num[e], den[e]);
+                    }
+                    if (p < n) {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) {
+                            const int cam = cb + (e >> 1);
+                            if (cam < c_end) {
+                                const float2 dn = sden[2 * cam + (e & 1)];
+                                __stcs(out + (2LL * cam + (e & 1)) * n + p, __fmaf_rn(q[e], dn.x, dn.y));
+                            }
+                        }
+                    }
                 }
             }
         }

@@ -277,11 +277,11 @@ __device__ __forceinline__ bool axis_contained(const FastAxis &a, long long bv, 
 }
 
 // Points per thread of the fast binning kernel.  Measured on one 4096^2 view (16.8 M points,
-// 2000^2 grid, grid of 8 CTAs of 256 per SM): 2 points per thread bin it in 0.0765 ms
-// (56 registers), 4 in 0.0814 ms, 8 in 0.098 ms; issuing the next points' loads before
-// binning the current ones (register double buffering) is slower too -- the kernel is
-// bound by the latency of its binning chain, so resident warps matter more than loads in
-// flight per thread.
+// 2000^2 grid, 2 waves of CTAs of 256): 2 points per thread bin it in 0.0765 ms, 4 in
+// 0.0814 ms, 8 in 0.098 ms; issuing the next points' loads before binning the current ones
+// (register double buffering) is slower too -- the kernel is bound by the latency of its
+// binning chain, so resident warps matter more than loads in flight per thread.  Grids
+// of 1.33 or 2.67 waves were slower than whole waves.
 constexpr int kFastPts = 2;
 
 // The kFastPts points of one thread: raw 64-bit words (x, y, z per point).
@@ -777,7 +777,19 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
         }
         // rows: a = off - v unless the origin is negative; columns: a = v - off unless negative
         const bool flip_row = !tb.row.neg, flip_col = tb.col.neg != 0;
-        gx = static_cast<unsigned>(std::max<long long>(1LL, std::min<long long>(ceil_div(ceil_div(max_points, kFastPts), threads), cap)));
+        // one wave of resident CTAs (grid-stride): a partial second wave would leave most
+        // SMs idle at the tail
+        static int resident = 0;
+        if (!resident) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bin_fast_kernel<true, false>, threads, 0) !=
+                    cudaSuccess || per_sm <= 0)
+                per_sm = 4;
+            resident = per_sm;
+        }
+        gx = static_cast<unsigned>(std::max<long long>(
+            1LL, std::min<long long>(ceil_div(ceil_div(max_points, kFastPts), threads),
+                                     static_cast<long long>(sm_count()) * resident)));
         if (flip_row && !flip_col)
             bin_fast_kernel<true, false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
         else if (flip_row && flip_col)
@@ -1800,10 +1812,13 @@ extern "C" int vs_map_points(const float *heights, int64_t row_stride, int width
     VS_REQUIRE(heights && points && width > 0 && height > 0 && row_stride >= width,
                "vs_map_points: bad arguments (%dx%d, stride %lld)", width, height, (long long)row_stride);
     const long long total = static_cast<long long>(width) * height;
-    // |e0| + (|ej| + |ei|) * 2^31 < 2^53 keeps every coordinate an exact double
-    const long long lim = 1LL << 52;
-    VS_REQUIRE(std::llabs(e0) < lim && std::llabs(n0) < lim && std::llabs(ej) < (1LL << 20) &&
-                   std::llabs(ei) < (1LL << 20) && std::llabs(nj) < (1LL << 20) && std::llabs(ni) < (1LL << 20),
+    // every coordinate integer e0 + ej (2j+1-W) + ei (2i+1-H) must stay below 2^53 (an exact
+    // double, and no 64-bit overflow): bound |e0| + |ej| W + |ei| H in FP64 with margin
+    auto bound = [&](long long c0, long long cj, long long ci) {
+        return std::fabs(static_cast<double>(c0)) + std::fabs(static_cast<double>(cj)) * width +
+               std::fabs(static_cast<double>(ci)) * height;
+    };
+    VS_REQUIRE(bound(e0, ej, ei) < 0x1p52 && bound(n0, nj, ni) < 0x1p52,
                "vs_map_points: affine map out of the exact range");
     const int threads = 256;
     const unsigned g = static_cast<unsigned>(std::min<long long>(ceil_div(total, threads), sm_count() * 16LL));
