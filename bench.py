@@ -327,6 +327,17 @@ def run_ours(args):
                                        'achieved': round(view_bytes / view_s / 1e9, 1),
                                        'frac': round(view_bytes / view_s / 1e9 / hbm_peak, 4)}}
 
+    # the camera fit alone (no concurrent rasterisation), same call as in the step
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fit()
+    torch.cuda.synchronize()
+    f0.record()
+    for _ in range(5):
+        fit()
+    f1.record()
+    torch.cuda.synchronize()
+    stages['camera_fit_alone_ms'] = f0.elapsed_time(f1) / 5
+
     result = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',

@@ -226,8 +226,12 @@ __device__ __forceinline__ void build_a_part(unsigned char *a_tile, int row, flo
     }
 }
 
+// Operands for which the fast quotient is accurate.  An RPC denominator is 1 plus small
+// terms inside the normalised cube, so the test is |den - 1| < 1/2 (rcp.approx is then
+// well inside its accurate range) and |num| < 1e30 (finite residual); anything else --
+// points far outside the cube, NaN, infinities -- takes IEEE division.
 __device__ __forceinline__ bool quotient_fast_ok(float num, float den) {
-    return fabsf(den) > 1e-30f && fabsf(den) < 1e30f && fabsf(num) < 1e30f;
+    return fabsf(den - 1.0f) < 0.5f && fabsf(num) < 1e30f;
 }
 __device__ __forceinline__ float quotient_fast(float num, float den) {
     float r;
@@ -355,43 +359,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
                     for (int j = 0; j < 4; ++j)
                         if (cb + 2 * j < c_end) tmem_ld8(lane_base + 4 * (cb + 2 * j), r[j]);   // warp-uniform
                     tmem_wait();
-                    // quotients of the chunk's 8 cameras, branch-free; one warp-uniform check
-                    // sends rare operands (|den| outside [1e-30, 1e30], |num| >= 1e30) to IEEE
-                    // division
+                    // quotients of the chunk's cameras, branch-free; one warp-uniform check
+                    // sends rare operands to IEEE division.  Columns of cameras past c_end
+                    // (an odd last pair) are computed and dropped.
+                    const int nc = min(8, c_end - cb);
                     float num[16], den[16], q[16];
                     bool ok = true;
 #pragma unroll
-                    for (int j = 0; j < 4; ++j)
-#pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const int cam = min(cb + 2 * j + h, c_end - 1);
-#pragma unroll
-                            for (int pl = 0; pl < 2; ++pl) {
-                                float nu = __uint_as_float(r[j][4 * h + 2 * pl]);
-                                float de = __uint_as_float(r[j][4 * h + 2 * pl + 1]);
-                                if (LIN) {
-                                    nu = add_linear(nu, slin[4 * cam + 2 * pl], px, py, pz);
-                                    de = add_linear(de, slin[4 * cam + 2 * pl + 1], px, py, pz);
-                                }
-                                const int e = 2 * (2 * j + h) + pl;
-                                num[e] = nu;
-                                den[e] = de;
-                                q[e] = quotient_fast(nu, de);
-                                ok = ok && (cb + 2 * j + h >= c_end || quotient_fast_ok(nu, de));
-                            }
+                    for (int e = 0; e < 16; ++e) {
+                        const int j = e >> 2, h = (e >> 1) & 1, pl = e & 1;
+                        float nu = __uint_as_float(r[j][4 * h + 2 * pl]);
+                        float de = __uint_as_float(r[j][4 * h + 2 * pl + 1]);
+                        if (LIN) {
+                            const float4 *lc = slin + 4 * (cb + (e >> 1)) + 2 * pl;   // within slin's 64 cameras
+                            nu = add_linear(nu, lc[0], px, py, pz);
+                            de = add_linear(de, lc[1], px, py, pz);
                         }
+                        num[e] = nu;
+                        den[e] = de;
+                        q[e] = quotient_fast(nu, de);
+                        if ((e >> 1) < nc) ok = ok && quotient_fast_ok(nu, de);
+                    }
                     if (__builtin_expect(!__all_sync(0xffffffffu, ok), 0)) {
 #pragma unroll
                         for (int e = 0; e < 16; ++e)
                             if (!quotient_fast_ok(num[e], den[e])) q[e] = tc_quotient_ieee(num[e], den[e]);
                     }
                     if (p < n) {
+                        float *o = out + (2LL * cb) * n + p;     // plane 2 cb, then one plane per entry
 #pragma unroll
-                        for (int e = 0; e < 16; ++e) {
-                            const int cam = cb + (e >> 1);
-                            if (cam < c_end) {
-                                const float2 dn = sden[2 * cam + (e & 1)];
-                                __stcs(out + (2LL * cam + (e & 1)) * n + p, __fmaf_rn(q[e], dn.x, dn.y));
+                        for (int e = 0; e < 16; ++e, o += n) {
+                            if ((e >> 1) < nc) {
+                                const float2 dn = sden[2 * cb + e];
+                                __stcs(o, __fmaf_rn(q[e], dn.x, dn.y));
                             }
                         }
                     }

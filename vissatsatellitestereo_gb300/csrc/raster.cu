@@ -236,9 +236,9 @@ __device__ __forceinline__ bool axis_fast(const FastAxis &a, long long bv, int &
 
 // axis_fast from the difference d itself.  For a contained grid the origin-binade test is
 // implied: d is monotone in the coordinate, and every coordinate outside the origin's
-// binade lies at least two cells outside [0, tmax).
+// binade lies at least two cells outside [0, tmax).  One unsigned compare covers d < 0.
 __device__ __forceinline__ bool axis_from_d(const FastAxis &a, long long d, int &r, bool &sure) {
-    const bool ok = (d >= 0) & (d < a.tmax);
+    const bool ok = static_cast<unsigned long long>(d) < static_cast<unsigned long long>(a.tmax);
     const unsigned u = static_cast<unsigned>(static_cast<unsigned long long>(d) >> a.shift);
     const float q = __fmul_rn(__uint2float_rn(u), a.scale);
     const float big = __fadd_rn(q, 12582912.0f);
@@ -916,7 +916,7 @@ __global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
         const MapViewDev mv = views[v];
         const AoiDev &ad = aois[mv.aoi];
         const FastAxis R = ad.row, C = ad.col;
-        const unsigned long long ncols = static_cast<unsigned>(ad.xsize);
+        const unsigned ncols32 = static_cast<unsigned>(ad.xsize);
         unsigned long long *vk = keys + mv.off;
         const int i0 = static_cast<int>(it - __ldg(item_start + v)) * rows_per_item;
         const int i1 = min(i0 + rows_per_item, mv.H);
@@ -939,8 +939,9 @@ __global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
             long long dcol = mv.dc0 + mv.dc_di * di2 + mv.dc_dj * dj0;
             long long drow = mv.dr0 + mv.dr_di * di2 + mv.dr_dj * dj0;
             const long long scol = 2 * mv.dc_dj, srow = 2 * mv.dr_dj;   // per pixel along the row
-            long long cell[4];
+            unsigned cell[4];                 // 32-bit: the plan keeps grids below 2^31 cells
             unsigned long long key[4];
+            bool okk[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k, dcol += scol, drow += srow) {
                 int r, c;
@@ -950,14 +951,14 @@ __global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
                 ok &= (hb[k] & 0x7fffffffu) <= 0x7f800000u;     // not NaN
                 if (ok && !sr) r = axis_correct(R.thr, r, drow);
                 if (ok && !sc) c = axis_correct(C.thr, c, dcol);
-                const long long cl = static_cast<long long>(static_cast<unsigned long long>(static_cast<unsigned>(r)) * ncols) + c;
                 const unsigned long long idx = static_cast<unsigned long long>(i) * static_cast<unsigned>(mv.W) + (j0 + k);
                 key[k] = ok ? map_key(hb[k], idx) : kEmptyKey;
-                cell[k] = ok ? cl : -1 - k;
+                cell[k] = static_cast<unsigned>(r) * ncols32 + static_cast<unsigned>(c);
+                okk[k] = ok;
             }
 #pragma unroll
             for (int k = 1; k < 4; ++k) {     // merge runs of consecutive pixels in one cell
-                const bool same = cell[k] == cell[k - 1];
+                const bool same = okk[k] & okk[k - 1] & (cell[k] == cell[k - 1]);
                 key[k] = same ? max(key[k], key[k - 1]) : key[k];
                 key[k - 1] = same ? kEmptyKey : key[k - 1];
             }
@@ -1439,9 +1440,12 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
     int expect_view = 0;
     for (int a = 0; a < n_aois; ++a) {
         const VsAoi &A = aois[a];
-        if (!(grid_ok(A.xsize, A.ysize) && A.xsize < (1LL << 22) && A.ysize < (1LL << 22) && A.n_views > 0 &&
-              A.first_view == expect_view && A.xoff > 0.0 && A.yoff > 0.0)) {
-            set_error("vs_aoi_batch_plan: AOI %d: bad grid or view range (views must be consecutive, origin positive)", a);
+        // cells below 2^31: the binning kernel indexes cells with 32-bit integers
+        if (!(grid_ok(A.xsize, A.ysize) && A.xsize < (1LL << 22) && A.ysize < (1LL << 22) &&
+              A.xsize * A.ysize < (1LL << 31) && A.n_views > 0 && A.first_view == expect_view && A.xoff > 0.0 &&
+              A.yoff > 0.0)) {
+            set_error("vs_aoi_batch_plan: AOI %d: bad grid (at most 2^31 - 1 cells) or view range (views must be "
+                      "consecutive, origin positive)", a);
             return fail(VS_ERR_ARG);
         }
         expect_view += A.n_views;
