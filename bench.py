@@ -685,6 +685,30 @@ def plain_serve(specs, source, metas, requests, fit_grid=(200, 20), time_limit_s
                     'copy to the host; no resident state'}
 
 
+def plain_fit_seconds(metas, fit_grid=(200, 20)):
+    """GPU time of the plain per-view camera fit of one AOI (the reference's camera loop on
+    the GPU, camera_approx.py:166-189): per view the exact RPCModel projection of the AOI's
+    grid, solve_perspective and check_perspective_error, one call each."""
+    import torch
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.check_error import perspective_error_batch
+    from vissatsatellitestereo_gb300.rpc_model import RPCModel
+    from vissatsatellitestereo_gb300.solve_perspective import solve_perspective_batch
+    g = synth.rpc_sample_grid_torch(metas[0], fit_grid[0], fit_grid[1], 'cuda')
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for meta in metas:
+        m = RPCModel(meta)
+        col, row = m.projection(g['lat'], g['lon'], g['alt'])
+        keep = (col >= 0) & (row >= 0) & (col < m.width) & (row < m.height)
+        K, R, t, st = solve_perspective_batch(g['x'], g['y'], g['z'], col.view(1, -1), row.view(1, -1),
+                                              keep.view(1, -1))
+        perspective_error_batch(g['x'], g['y'], g['z'], col.view(1, -1), row.view(1, -1), K, R, t, keep.view(1, -1))
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
 def serving_form(n_requests=400, rate=20.0, n_aois=400, budget_gb=150, pool_maps=32, seed=None, slots=3):
     """A stream of AOI fusion requests (Poisson arrivals at `rate`/s, Zipf popularity over a
     catalog of `n_aois` AOIs with config-3 size ranges drawn log-uniformly) served in real
@@ -767,26 +791,35 @@ def batched_form(n_aois=200, pool_maps=32, budget_gb=96, steps=2, warmup=1, plai
     algo = eng.pixels * 4 + eng.cell_views * (8 + 8 + 4 + 4) + eng.cells * 12
     res['algorithmic_bytes_per_step'] = algo
     res['achieved_gbs_batched'] = round(algo / modes['batched']['s_per_step'] / 1e9, 1)
-    # plain per-view GPU form on a sample of views, scaled by pixels
-    pix, plain_t, n_plain_views, k = 0, 0.0, 0, 0
+    # plain per-view GPU form on a sample of views: rasterisation + fusion scaled by pixels,
+    # the camera fits (the reference's per-view camera loop) scaled by views
+    metas = [synth.aoi_rpc_metas(s) for s in specs]
+    pix, plain_t, plain_fit_t, n_plain_views, k = 0, 0.0, 0.0, 0, 0
     for a, s in enumerate(specs):
         if n_plain_views >= plain_views:
             break
         maps = [pool[(k + v) % pool_maps] for v in range(s.n_views)]
+        if a == 0:
+            plain_aoi_seconds(s, maps, affines[a])                 # warm
+            plain_fit_seconds(metas[a][:2])
         plain_t += plain_aoi_seconds(s, maps, affines[a])
+        plain_fit_t += plain_fit_seconds(metas[a])
         pix += s.n_views * s.image * s.image
         n_plain_views += s.n_views
         k += s.n_views
     est = plain_t * eng.pixels / pix
-    res['plain_per_view'] = {'sample': f'first {n_plain_views} views (AOIs 0..), scaled by pixels',
-                             'est_s_per_step': round(est, 3), 'pixels_per_s': eng.pixels / est}
-    res['speedup_batched_vs_plain'] = round(est / modes['batched']['s_per_step'], 2)
+    est_fit = plain_fit_t * eng.n_views / n_plain_views
+    res['plain_per_view'] = {'sample': f'first {n_plain_views} views (AOIs 0..): rasterisation + fusion scaled by '
+                                       f'pixels, camera fits by views',
+                             'est_s_per_step': round(est, 3), 'pixels_per_s': eng.pixels / est,
+                             'fits_est_s_per_step': round(est_fit, 3)}
+    res['speedup_batched_vs_plain_raster_fusion'] = round(est / modes['batched']['s_per_step'], 2)
     res['speedup_graph_vs_per_view_launches'] = round(modes['per_view']['s_per_step'] / modes['graph']['s_per_step'], 3)
+    eng_cells = eng.cell_views
     eng.close()
     del eng, pool
     torch.cuda.empty_cache()
     if with_fits:
-        metas = [synth.aoi_rpc_metas(s) for s in specs]
         fits = AoiCameraFits(specs, metas)
         fits.step()
         torch.cuda.synchronize()
@@ -796,6 +829,14 @@ def batched_form(n_aois=200, pool_maps=32, budget_gb=96, steps=2, warmup=1, plai
         e1.record()
         torch.cuda.synchronize()
         ft = e0.elapsed_time(e1) / 1e3
+        batched_total = modes['batched']['s_per_step'] + ft
+        plain_total = est + est_fit
+        res['pipeline'] = {
+            'what': 'camera fits (RPC projection + perspective fit + error statistics) + rasterisation + fusion of '
+                    'all AOIs',
+            'batched_s_per_step': round(batched_total, 3), 'plain_per_view_est_s_per_step': round(plain_total, 3),
+            'speedup_batched_vs_plain': round(plain_total / batched_total, 2),
+            'rpc_pts_per_s_batched': fits.points / ft, 'dsm_cell_views_per_s_batched': eng_cells / batched_total}
         res['camera_fits'] = {'views': sum(s.n_views for s in specs), 'grid': '200x200x20 per AOI (shared by its views)',
                               's_per_step': round(ft, 4), 'rpc_pts_per_s': fits.points / ft,
                               'status_ok': fits.status_ok()}

@@ -342,6 +342,25 @@ def test_dsm_epilogue_cv2_network_shapes(H, W):
     assert same_bits(got, blur.median_blur3x3(raster.proj_to_grid(pts, *args).astype(np.float32)))
 
 
+@pytest.mark.parametrize('H,W', [(33, 70), (64, 64), (70, 33), (5, 6)])
+def test_dsm_epilogue_sorted_column_path(H, W):
+    """Tiles whose staged values hold no NaN and no zero take the sorted-column median in
+    the epilogue; with ties and infinities it must still equal OpenCV's network bit for bit."""
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    rng = np.random.default_rng(H * 7 + W)
+    xoff, yoff, res = 354000.0, 6182000.0, 1.0
+    n = 16 * H * W                                 # dense: no empty cells, so no hole fill
+    pts = np.empty((n, 3))
+    pts[:, 0] = xoff + rng.uniform(0, W, n)
+    pts[:, 1] = yoff - rng.uniform(0, H, n)
+    pts[:, 2] = rng.choice([-3.5, -1.0, 1.0, 2.5, 7.0, np.inf, -np.inf], n, p=[0.2, 0.2, 0.2, 0.2, 0.1, 0.05, 0.05])
+    args = (xoff, yoff, res, res, W, H)
+    ref = blur.median_blur3x3(raster.proj_to_grid(pts, *args).astype(np.float32))
+    assert not np.isnan(raster.proj_to_grid(pts, *args)).any()       # every cell covered: the fast path
+    got = dsm_from_points(pts, np.array([0, n]), *args).cpu().numpy()[0]
+    assert same_bits(got, ref)
+
+
 def test_median_blur_matches_oracle():
     from vissatsatellitestereo_gb300.proj_to_grid import median_blur3x3
     rng = np.random.default_rng(3)

@@ -310,18 +310,15 @@ __global__ void prepare_views_kernel(const VsRpcCamera *__restrict__ cams, int n
     wh[2 * v + 1] = f.height;
 }
 
-// Projection and moments in one pass (the fused camera path): each thread projects its
-// points through view v's RPC camera (double-float, or FP64 in the reference's order),
-// writes (col, row) as double-floats for the error pass, and accumulates the moments of
-// the in-image points -- the (col, row) never make a round trip through HBM before the
-// moments.  Same block/point partition as moments_kernel, so the partials line up.
+// Projection pass of the fused camera path: (col, row) of every grid point through view
+// v's RPC camera as double-floats.
 template <int MODE>
-__global__ void __launch_bounds__(kMomThreads, 4) project_moments_kernel(
-    const VsRpcCamera *__restrict__ cams, const RpcFast *__restrict__ fasts, const double *__restrict__ lat,
-    const double *__restrict__ lon, const double *__restrict__ alt, const double *__restrict__ x,
-    const double *__restrict__ y, const double *__restrict__ z, long long stride, long long n,
-    const Norm *__restrict__ norm, float4 *__restrict__ colrow, double *__restrict__ partial) {
-    __shared__ double red[(kMomThreads / 32) * kSlots];
+__global__ void __launch_bounds__(256) project_view_kernel(const VsRpcCamera *__restrict__ cams,
+                                                           const RpcFast *__restrict__ fasts,
+                                                           const double *__restrict__ lat,
+                                                           const double *__restrict__ lon,
+                                                           const double *__restrict__ alt, long long n,
+                                                           long long stride, float4 *__restrict__ colrow) {
     __shared__ VsRpcCamera cam;
     __shared__ RpcFast fast;
     const int v = blockIdx.y;
@@ -334,21 +331,9 @@ __global__ void __launch_bounds__(kMomThreads, 4) project_moments_kernel(
         for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
-    const NormF nf = make_normf(norm[v]);
-    const float w = MODE == VS_PROJ_EXACT ? static_cast<float>(cam.width) : fast.width;
-    const float h = MODE == VS_PROJ_EXACT ? static_cast<float>(cam.height) : fast.height;
     const long long off = v * stride;
-    float m[kMom];
-#pragma unroll
-    for (int k = 0; k < kMom; ++k) m[k] = 0.0f;
-    float count = 0.0f;
-    const long long base = static_cast<long long>(blockIdx.x) * kMomThreads * kChunk + threadIdx.x;
-#pragma unroll 1
-    for (int j = 0; j < kChunk; ++j) {
-        const long long i = base + static_cast<long long>(j) * kMomThreads;
-        if (i >= n) break;
-        // the ENU point is loaded with the geodetic one: its latency hides under the projection
-        const double X = __ldcs(x + off + i), Y = __ldcs(y + off + i), Z = __ldcs(z + off + i);
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
         df dc, dr;
         if (MODE == VS_PROJ_EXACT) {
             double cc, rr;
@@ -360,14 +345,7 @@ __global__ void __launch_bounds__(kMomThreads, 4) project_moments_kernel(
                          split_double(__ldcs(alt + off + i)), dc, dr);
         }
         colrow[static_cast<long long>(v) * n + i] = make_float4(dc.hi, dc.lo, dr.hi, dr.lo);
-        if (df_ge0(dc) && df_ge0(dr) && df_lt(dc, w) && df_lt(dr, h)) {
-            float px, py, pz, pc, pr;
-            normalised_point(nf, X, Y, Z, dc, dr, px, py, pz, pc, pr);
-            add_moments(m, px, py, pz, pc, pr);
-            count += 1.0f;
-        }
     }
-    store_block_moments(m, count, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kSlots, red);
 }
 
 // ---- 12x12 solve (one thread per view; FP64) -------------------------------------------
@@ -1172,13 +1150,19 @@ extern "C" int vs_camera_approx_perspective(const VsRpcCamera *cams, int n_views
     const int blocks = mom_blocks(n);
     prepare_views_kernel<<<static_cast<unsigned>(ceil_div(n_views, 64)), 64, 0, st>>>(cams, n_views, f.fast, f.wh);
     VS_LAUNCH_CHECK("prepare_views_kernel");
-    if (proj_mode == VS_PROJ_EXACT)
-        project_moments_kernel<VS_PROJ_EXACT><<<dim3(blocks, n_views), kMomThreads, 0, st>>>(
-            cams, f.fast, lat, lon, alt, x, y, z, point_stride, n, f.norm, f.colrow, f.partial);
-    else
-        project_moments_kernel<VS_PROJ_FAST><<<dim3(blocks, n_views), kMomThreads, 0, st>>>(
-            cams, f.fast, lat, lon, alt, x, y, z, point_stride, n, f.norm, f.colrow, f.partial);
-    VS_LAUNCH_CHECK("project_moments_kernel");
+    if (n > 0) {
+        const unsigned pg = static_cast<unsigned>(std::min<long long>(ceil_div(n, 256), sm_count() * 8LL / n_views + 8));
+        if (proj_mode == VS_PROJ_EXACT)
+            project_view_kernel<VS_PROJ_EXACT><<<dim3(pg, n_views), 256, 0, st>>>(cams, f.fast, lat, lon, alt, n,
+                                                                                  point_stride, f.colrow);
+        else
+            project_view_kernel<VS_PROJ_FAST><<<dim3(pg, n_views), 256, 0, st>>>(cams, f.fast, lat, lon, alt, n,
+                                                                                 point_stride, f.colrow);
+        VS_LAUNCH_CHECK("project_view_kernel");
+    }
+    moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, point_stride, nullptr, nullptr, f.colrow,
+                                                                   nullptr, f.wh, n, f.norm, f.partial);
+    VS_LAUNCH_CHECK("moments_kernel");
     solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, cams, K, R, t, params, f.errcam, status);
     VS_LAUNCH_CHECK("solve_kernel");
     if (!err) return VS_OK;

@@ -522,6 +522,15 @@ __device__ __forceinline__ bool cv_vector_column(long long c, long long W) {
     return c >= 1 && c < 1 + 4 * nv;
 }
 
+// Sorted triple and median of three for NaN-free values (IEEE min/max).
+__device__ __forceinline__ void sort3f(float a, float b, float c, float &lo, float &mid, float &hi) {
+    const float l = fminf(a, b), h = fmaxf(a, b);
+    lo = fminf(l, c);
+    hi = fmaxf(h, c);
+    mid = fmaxf(l, fminf(h, c));
+}
+__device__ __forceinline__ float med3f(float a, float b, float c) { return fmaxf(fminf(a, b), fminf(fmaxf(a, b), c)); }
+
 template <typename T>
 __device__ __forceinline__ float as_f32(T v) { return static_cast<float>(v); }
 template <>
@@ -582,6 +591,7 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
                                               float *__restrict__ out, unsigned long long *__restrict__ next_keys,
                                               int H, int W, int r0, int c0, EpilogueSmem &sm) {
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx, lane = tid & 31;
+    bool special = false;          // this thread staged a NaN or a zero
     if (tid == 0) sm.n_holes = 0;
     for (int i = tid; i < RAW_H * RAW_W; i += TX * TY) {
         const int ly = i / RAW_W, lx = i - ly * RAW_W;
@@ -599,7 +609,11 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
         const bool in = i < FK_H * FK_W;
         const int ly = i / FK_W, lx = i - ly * FK_W;
         const unsigned long long k = in ? sm.raw[(ly + 1) * RAW_W + lx + 1] : 1ull;
-        if (in && k != kEmptyKey) sm.fk[ly][lx] = f64_to_f32(double_from_key(k));
+        if (in && k != kEmptyKey) {
+            const float f = f64_to_f32(double_from_key(k));
+            sm.fk[ly][lx] = f;
+            special |= isnan(f) || f == 0.0f;
+        }
         // warp-aggregated append of the empty cells to the hole list
         const unsigned empty = __ballot_sync(0xffffffffu, in && k == kEmptyKey);
         if (empty) {
@@ -624,14 +638,46 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
         bool any = false;
 #pragma unroll
         for (int q = 0; q < 8; ++q) any |= s8[q] != kEmptyKey;
-        sm.fk[ly][lx] = any ? f64_to_f32(median8_keys(s8)) : __uint_as_float(0x7fffffffu);
+        const float f = any ? f64_to_f32(median8_keys(s8)) : __uint_as_float(0x7fffffffu);
+        sm.fk[ly][lx] = f;
+        special |= isnan(f) || f == 0.0f;
     }
-    __syncthreads();
+    // A tile whose staged values hold no NaN and no zero takes the sorted-column median:
+    // with no NaN and no -0/+0 pair every compare-exchange order yields the same value, so
+    // OpenCV's network and the column form agree bit for bit.
+    const bool exact_net = __syncthreads_or(special) != 0 || H == 1 || W == 1;
     const int c = c0 + tx;
-    if (c >= W) return;
     int xa = tx, xb = tx + 1, xc = tx + 2;
     if (c == 0) xa = xb;                 // replicate border: clamp the neighbours into the image
     if (c == W - 1) xc = xb;
+    if (!exact_net) {
+        // lane tx owns fk column tx + 1; lanes 0 and 31 also sort the halo columns 0 and 33
+        const int xe = tx == 0 ? 0 : (tx == TX - 1 ? TX + 1 : tx + 1);
+#pragma unroll
+        for (int j = 0; j < TILE_Y / TY; ++j) {
+            const int oy = ty + TY * j, r = r0 + oy;
+            int ya = oy, yb = oy + 1, yc = oy + 2;
+            if (r == 0) ya = yb;
+            if (r == H - 1) yc = yb;
+            float lo, mid, hi, elo, emid, ehi;
+            sort3f(sm.fk[ya][tx + 1], sm.fk[yb][tx + 1], sm.fk[yc][tx + 1], lo, mid, hi);
+            sort3f(sm.fk[ya][xe], sm.fk[yb][xe], sm.fk[yc][xe], elo, emid, ehi);
+            float llo = __shfl_up_sync(0xffffffffu, lo, 1), lmid = __shfl_up_sync(0xffffffffu, mid, 1),
+                  lhi = __shfl_up_sync(0xffffffffu, hi, 1);
+            float rlo = __shfl_down_sync(0xffffffffu, lo, 1), rmid = __shfl_down_sync(0xffffffffu, mid, 1),
+                  rhi = __shfl_down_sync(0xffffffffu, hi, 1);
+            if (tx == 0) { llo = elo; lmid = emid; lhi = ehi; }
+            if (tx == TX - 1) { rlo = elo; rmid = emid; rhi = ehi; }
+            if (c == 0) { llo = lo; lmid = mid; lhi = hi; }           // replicate border
+            if (c == W - 1) { rlo = lo; rmid = mid; rhi = hi; }
+            if (c >= W || r >= H) continue;
+            const long long cell = static_cast<long long>(r) * W + c;
+            if (next_keys) next_keys[cell] = kEmptyKey;
+            out[cell] = med3f(fmaxf(fmaxf(llo, lo), rlo), med3f(lmid, mid, rmid), fminf(fminf(lhi, hi), rhi));
+        }
+        return;
+    }
+    if (c >= W) return;
     const bool vec = cv_vector_column(c, W);
 #pragma unroll
     for (int j = 0; j < TILE_Y / TY; ++j) {
