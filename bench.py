@@ -454,9 +454,8 @@ def precision_form(metas, n_points=16 << 20, steps=10, warmup=3, sample_stride=1
            'points': n_points, 'cameras': C, 'algorithmic_bytes_per_launch': algo_bytes,
            'error_sample': f'every {sample_stride}th point x {C} cameras x (col,row) vs FP64 exact kernel',
            'variants': {}}
-    products = {'fp32': 1, 'bf16x3': 3, 'tf32x3': 3, 'bf16x6': 6, 'bf16x3_tc': 3, 'bf16x3_lin': 3, 'bf16x3_lin_tc': 3,
-                'bf16x3_lin6_tc': 3}
-    for name in ('fp32', 'bf16x3', 'tf32x3', 'bf16x6', 'bf16x3_tc', 'bf16x3_lin', 'bf16x3_lin_tc', 'bf16x3_lin6_tc'):
+    products = {'fp32': 1, 'bf16x3': 3, 'tf32x3': 3, 'bf16x6': 6, 'bf16x3_tc': 3, 'bf16x3_lin': 3, 'bf16x3_lin_tc': 3}
+    for name in ('fp32', 'bf16x3', 'tf32x3', 'bf16x6', 'bf16x3_tc', 'bf16x3_lin', 'bf16x3_lin_tc'):
         for _ in range(warmup):
             project_cube(cams, xyz, name, out=out, check=False)
         torch.cuda.synchronize()

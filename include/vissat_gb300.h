@@ -98,9 +98,6 @@ int vs_rpc_project(const VsRpcCamera *cams, int n_cams, const double *lat, const
                               * than BF16X6                                                  */
 #define VS_CUBE_BF16X3_LIN_TC 6 /* as BF16X3_LIN with the contraction on tcgen05 (TMEM
                                  * accumulators, overlapped epilogue), at most 64 cameras     */
-#define VS_CUBE_BF16X3_LIN6_TC 7 /* tcgen05: BF16X3 for the higher-order terms and six bf16
-                                  * split products for the constant and linear terms, all in
-                                  * the tensor cores, at most 64 cameras                      */
 #define VS_CUBE_MAX_CAMERAS 128
 size_t vs_rpc_project_cube_workspace_size(int n_cams);
 int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const float *xyz, int64_t n, float *colrow,

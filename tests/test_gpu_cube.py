@@ -108,8 +108,7 @@ def test_cube_empty_and_errors(cameras50):
         project_cube(too_many, np.zeros((3, 5), np.float32))
 
 
-@pytest.mark.parametrize('variant,twin', [('bf16x3_tc', 'bf16x3'), ('bf16x3_lin_tc', 'bf16x3_lin'),
-                                          ('bf16x3_lin6_tc', 'bf16x3_lin')])
+@pytest.mark.parametrize('variant,twin', [('bf16x3_tc', 'bf16x3'), ('bf16x3_lin_tc', 'bf16x3_lin')])
 @pytest.mark.parametrize('n_cams,n', [(50, 20000), (3, 37), (1, 1), (7, 300), (64, 1000), (49, 129), (63, 256)])
 def test_cube_tcgen05_variant(variant, twin, n_cams, n):
     """The tcgen05 kernels (TMEM accumulators, overlapped epilogue): within the bound of
@@ -137,7 +136,7 @@ def test_cube_tcgen05_rejects_too_many_cameras(cameras50):
         project_cube(cameras50 + cameras50[:20], np.zeros((3, 5), np.float32), variant='bf16x3_tc')
 
 
-@pytest.mark.parametrize('variant', ['bf16x3_tc', 'bf16x3_lin_tc', 'bf16x3_lin6_tc'])
+@pytest.mark.parametrize('variant', ['bf16x3_tc', 'bf16x3_lin_tc'])
 def test_cube_tcgen05_timeout_is_reported(variant):
     """A CTA whose bounded wait for the tensor cores runs out sets the error word; the call's
     status query returns VS_ERR_TIMEOUT and the context stays usable.  The wait limit is

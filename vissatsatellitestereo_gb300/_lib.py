@@ -33,7 +33,6 @@ VS_CUBE_BF16X6 = 3
 VS_CUBE_BF16X3_TC = 4
 VS_CUBE_BF16X3_LIN = 5
 VS_CUBE_BF16X3_LIN_TC = 6
-VS_CUBE_BF16X3_LIN6_TC = 7
 VS_CUBE_MAX_CAMERAS = 128
 VS_GEO_EXACT = 0
 VS_GEO_FAST = 1

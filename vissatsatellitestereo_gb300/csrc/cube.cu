@@ -498,7 +498,7 @@ int launch_mma(const VsRpcCamera *cams, int n_cams, const float *xyz, long long 
 size_t cube_tc_workspace_bytes(int n_cams);
 int cube_tc_status(const void *ws, int n_cams, cudaStream_t st);
 int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
-                   cudaStream_t st, int scheme);
+                   cudaStream_t st, bool lin);
 
 }  // namespace vs
 
@@ -517,7 +517,7 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
                "vs_rpc_project_cube: bad sizes (cameras %d, max %d; n %lld)", n_cams, VS_CUBE_MAX_CAMERAS, (long long)n);
     VS_REQUIRE(variant == VS_CUBE_FP32 || variant == VS_CUBE_BF16X3 || variant == VS_CUBE_TF32X3 ||
                    variant == VS_CUBE_BF16X6 || variant == VS_CUBE_BF16X3_TC || variant == VS_CUBE_BF16X3_LIN ||
-                   variant == VS_CUBE_BF16X3_LIN_TC || variant == VS_CUBE_BF16X3_LIN6_TC,
+                   variant == VS_CUBE_BF16X3_LIN_TC,
                "vs_rpc_project_cube: bad variant %d", variant);
     VS_REQUIRE(cams && workspace && (n == 0 || (xyz && colrow)), "vs_rpc_project_cube: null pointer");
     const size_t need = vs_rpc_project_cube_workspace_size(n_cams);
@@ -534,9 +534,8 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
         case VS_CUBE_TF32X3: return launch_mma<VS_CUBE_TF32X3>(cams, n_cams, xyz, n, colrow, w, st);
         case VS_CUBE_BF16X6: return launch_mma<VS_CUBE_BF16X6>(cams, n_cams, xyz, n, colrow, w, st);
         case VS_CUBE_BF16X3_LIN: return launch_mma<VS_CUBE_BF16X3_LIN>(cams, n_cams, xyz, n, colrow, w, st);
-        case VS_CUBE_BF16X3_TC: return launch_cube_tc(cams, n_cams, xyz, n, colrow, workspace, st, 0);
-        case VS_CUBE_BF16X3_LIN_TC: return launch_cube_tc(cams, n_cams, xyz, n, colrow, workspace, st, 1);
-        case VS_CUBE_BF16X3_LIN6_TC: return launch_cube_tc(cams, n_cams, xyz, n, colrow, workspace, st, 2);
+        case VS_CUBE_BF16X3_TC: return launch_cube_tc(cams, n_cams, xyz, n, colrow, workspace, st, false);
+        case VS_CUBE_BF16X3_LIN_TC: return launch_cube_tc(cams, n_cams, xyz, n, colrow, workspace, st, true);
         default: break;
     }
     cube_prepare_fp32_kernel<<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(kTerms) * 4 * n_cams, 256)), 256, 0,
@@ -557,7 +556,7 @@ extern "C" int vs_rpc_project_cube(const VsRpcCamera *cams, int n_cams, const fl
 
 extern "C" int vs_rpc_project_cube_status(const void *workspace, int n_cams, int variant, void *stream) {
     VS_REQUIRE(workspace && n_cams > 0 && n_cams <= VS_CUBE_MAX_CAMERAS, "vs_rpc_project_cube_status: bad arguments");
-    if (variant != VS_CUBE_BF16X3_TC && variant != VS_CUBE_BF16X3_LIN_TC && variant != VS_CUBE_BF16X3_LIN6_TC)
+    if (variant != VS_CUBE_BF16X3_TC && variant != VS_CUBE_BF16X3_LIN_TC)
         return VS_OK;                                    // the other variants have no device-side waits
     return cube_tc_status(workspace, n_cams, as_stream(stream));
 }

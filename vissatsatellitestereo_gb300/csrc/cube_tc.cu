@@ -9,9 +9,6 @@
 //   LIN  (VS_CUBE_BF16X3_LIN_TC): the 16 higher-order monomials only (K = 48); the
 //        constant and linear terms -- whose large coefficients carry the split forms'
 //        error -- are added in FP32 in the epilogue (z, x, y, then the constant).
-//   LIN6 (VS_CUBE_BF16X3_LIN6_TC): the 16 higher-order monomials as in LIN, then the
-//        constant and linear monomials with three bf16 pieces per factor and the six
-//        products of order <= 2 (K = 48 + 24, padded to 80): all on the tensor cores.
 // Monomials enter the reduction from the highest order down, so the large terms come last.
 //
 // One persistent CTA per SM, four warpgroups (512 threads).  Per tile of 128 points:
@@ -49,30 +46,16 @@ constexpr int kTcTile = 128;        // points per tile = TMEM lanes
 constexpr int kTcTmemCols = 512;    // two accumulators of up to 256 columns
 constexpr int kTcMaxN = 256;
 constexpr int kTcMaxCams = kTcMaxN / 4;
-constexpr int kTcMaxK = 80;         // reduction slots of the widest scheme
 constexpr unsigned kWaitLimit = 1u << 24;
 
-// Split schemes: 0 = X3, 1 = LIN, 2 = LIN6 (see the top of the file).
-template <int SCH>
+template <bool LIN>
 struct TcScheme {
-    static constexpr bool kEpiLinear = SCH == 1;                 // constant + linear terms in the epilogue
-    static constexpr int kSlots3 = (SCH == 0 ? 20 : 16) * 3;      // 3-product slots (highest order first)
-    static constexpr int kSlots6 = SCH == 2 ? 4 * 6 : 0;          // 6-product slots of z, x, y, 1
-    static constexpr int kUsed = kSlots3 + kSlots6;
-    static constexpr int kK = (kUsed + 15) / 16 * 16;             // whole K=16 steps: 64, 48, 80
+    static constexpr int kFirst = LIN ? 4 : 0;            // first monomial in the contraction
+    static constexpr int kMonos = 20 - kFirst;
+    static constexpr int kK = LIN ? 48 : 64;              // slots, padded to whole K=16 steps
     static constexpr int kRowBytes = kK * 2;
-    // monomial of slot k
-    static __host__ __device__ constexpr int mono(int k) { return k < kSlots3 ? 19 - k / 3 : 3 - (k - kSlots3) / 6; }
-    // A and B piece of slot k (0 = the bf16 rounding, 1 = that of the residual, 2 = the next)
-    // 3 products: hh + lh + hl; 6 products, smallest first: 11, 20, 02, 10, 01, 00
-    static __host__ __device__ constexpr int apiece(int k) {
-        return k < kSlots3 ? (k % 3 == 1 ? 1 : 0) : ((k - kSlots3) % 6 == 0 ? 1 : (k - kSlots3) % 6 == 1 ? 2
-                                                     : (k - kSlots3) % 6 == 3 ? 1 : 0);
-    }
-    static __host__ __device__ constexpr int bpiece(int k) {
-        return k < kSlots3 ? (k % 3 == 2 ? 1 : 0) : ((k - kSlots3) % 6 == 0 ? 1 : (k - kSlots3) % 6 == 2 ? 2
-                                                     : (k - kSlots3) % 6 == 4 ? 1 : 0);
-    }
+    // monomial of contraction slot group j (highest order first)
+    static __host__ __device__ constexpr int mono(int j) { return 19 - j; }
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
@@ -177,28 +160,26 @@ inline int tc_n_pad(int n_cams) { return ((4 * n_cams + 15) / 16) * 16; }
 CubeTcWs carve_cube_tc(void *ws, int n_cams) {
     Carver cv(ws);
     CubeTcWs w;
-    w.b = cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * kTcMaxK);
+    w.b = cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * 64);
     w.den = cv.take<float2>(2 * static_cast<size_t>(n_cams));
     w.lin = cv.take<float4>(4 * static_cast<size_t>(n_cams));
     w.err = cv.take<int>(1);
     return w;
 }
 
-template <int SCH>
+template <bool LIN>
 __global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int n_cams, int n_pad, CubeTcWs w) {
-    using S = TcScheme<SCH>;
+    using S = TcScheme<LIN>;
     const int total = n_pad * S::kK;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         const int col = i / S::kK, k = i - col * S::kK;
         const int cam = col >> 2, p = col & 3;
         float v = 0.0f;
-        if (cam < n_cams && k < S::kUsed) {
-            const double coef = column_poly(cams[cam], p)[S::mono(k)];
-            const float c0 = bf16_round(static_cast<float>(coef));
-            const float c1 = bf16_round(static_cast<float>(coef - static_cast<double>(c0)));
-            const float c2 = bf16_round(static_cast<float>(coef - static_cast<double>(c0) - static_cast<double>(c1)));
-            const int b = S::bpiece(k);
-            v = b == 0 ? c0 : b == 1 ? c1 : c2;
+        if (cam < n_cams && k < 3 * S::kMonos) {
+            const double coef = column_poly(cams[cam], p)[S::mono(k / 3)];
+            const float hi = bf16_round(static_cast<float>(coef));
+            const float lo = bf16_round(static_cast<float>(coef - static_cast<double>(hi)));
+            v = (k % 3 == 2) ? lo : hi;           // B pieces (hi, hi, lo)
         }
         w.b[canon_offset(col, k, S::kK) / 2] = __float2bfloat16_rn(v);
     }
@@ -215,9 +196,9 @@ __global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int
 }
 
 // Part P of a point's A row: the 16-byte chunks c (8 slots each) with c % 4 == P.
-template <int SCH, int P>
+template <bool LIN, int P>
 __device__ __forceinline__ void build_a_part(unsigned char *a_tile, int row, float x, float y, float z) {
-    using S = TcScheme<SCH>;
+    using S = TcScheme<LIN>;
     const float yx = y * x, yz = y * z, xz = x * z, yy = y * y, xx = x * x, zz = z * z;
     const float m[20] = {1.0f,   y,      x,      z,      yx,     yz,     xz,     yy,     xx,     zz,
                          yx * z, yy * y, y * xx, y * zz, yy * x, xx * x, x * zz, yy * z, xx * z, zz * z};
@@ -231,12 +212,10 @@ __device__ __forceinline__ void build_a_part(unsigned char *a_tile, int row, flo
             for (int q = 0; q < 2; ++q) {
                 const int k = 8 * c + 2 * wd + q;
                 float v = 0.0f;
-                if (k < S::kUsed) {
-                    const float mv = m[S::mono(k)];
-                    const float p0 = bf16_round(mv), r1 = mv - p0;      // residuals exact in FP32
-                    const float p1 = bf16_round(r1), p2 = bf16_round(r1 - p1);
-                    const int a = S::apiece(k);
-                    v = a == 0 ? p0 : a == 1 ? p1 : p2;
+                if (k < 3 * S::kMonos) {
+                    const float mv = m[S::mono(k / 3)];
+                    const float hi = bf16_round(mv);
+                    v = (k % 3 == 1) ? bf16_round(mv - hi) : hi;   // A pieces (hi, lo, hi)
                 }
                 e[q] = v;
             }
@@ -261,11 +240,11 @@ __device__ __forceinline__ float quotient_fast(float num, float den) {
     return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
 }
 
-template <int SCH>
+template <bool LIN>
 __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__restrict__ xyz, long long n, int n_cams,
                                                                int n_pad, CubeTcWs w, float *__restrict__ out,
                                                                unsigned wait_limit) {
-    using S = TcScheme<SCH>;
+    using S = TcScheme<LIN>;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sb = smem;                                           // B: n_pad x K
     unsigned char *sa0 = sb + kTcMaxN * S::kRowBytes;                   // A buffers: 128 x K each, adjacent
@@ -291,7 +270,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
             : "memory");
     }
     for (int i = tid; i < 2 * n_cams; i += kTcThreads) sden[i] = w.den[i];
-    if (TcScheme<SCH>::kEpiLinear)
+    if (LIN)
         for (int i = tid; i < 4 * n_cams; i += kTcThreads) slin[i] = w.lin[i];
     __syncwarp();
     if (warp == 0) {
@@ -333,10 +312,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
         if (have && !failed) {
             unsigned char *a_tile = sa0 + buf * (kTcTile * S::kRowBytes);
             switch (grp) {
-                case 0: build_a_part<SCH, 0>(a_tile, row, cx, cy, cz); break;
-                case 1: build_a_part<SCH, 1>(a_tile, row, cx, cy, cz); break;
-                case 2: build_a_part<SCH, 2>(a_tile, row, cx, cy, cz); break;
-                default: build_a_part<SCH, 3>(a_tile, row, cx, cy, cz); break;
+                case 0: build_a_part<LIN, 0>(a_tile, row, cx, cy, cz); break;
+                case 1: build_a_part<LIN, 1>(a_tile, row, cx, cy, cz); break;
+                case 2: build_a_part<LIN, 2>(a_tile, row, cx, cy, cz); break;
+                default: build_a_part<LIN, 3>(a_tile, row, cx, cy, cz); break;
             }
             // the next tile's point, in flight during this iteration's epilogue
             const long long p = (tile + gridDim.x) * kTcTile + row;
@@ -391,7 +370,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
                         const int j = e >> 2, h = (e >> 1) & 1, pl = e & 1;
                         float nu = __uint_as_float(r[j][4 * h + 2 * pl]);
                         float de = __uint_as_float(r[j][4 * h + 2 * pl + 1]);
-                        if (S::kEpiLinear) {
+                        if (LIN) {
                             const float4 *lc = slin + 4 * (cb + (e >> 1)) + 2 * pl;   // within slin's 64 cameras
                             nu = add_linear(nu, lc[0], px, py, pz);
                             de = add_linear(de, lc[1], px, py, pz);
@@ -441,9 +420,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
 }
 
-template <int SCH>
+template <bool LIN>
 size_t cube_tc_smem() {
-    using S = TcScheme<SCH>;
+    using S = TcScheme<LIN>;
     // at least half of the SM's shared memory: one CTA per SM, which owns all 512 TMEM columns
     const size_t need = static_cast<size_t>(kTcMaxN + 2 * kTcTile) * S::kRowBytes + sizeof(float2) * 2 * kTcMaxCams +
                         sizeof(float4) * 4 * kTcMaxCams + 1024;
@@ -458,7 +437,7 @@ unsigned g_tc_wait_limit = kWaitLimit;
 
 size_t cube_tc_workspace_bytes(int n_cams) {
     Carver cv(nullptr);
-    cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * kTcMaxK);
+    cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * 64);
     cv.take<float2>(2 * static_cast<size_t>(n_cams));
     cv.take<float4>(4 * static_cast<size_t>(n_cams));
     cv.take<int>(1);
@@ -482,7 +461,7 @@ int cube_tc_status(const void *ws, int n_cams, cudaStream_t st) {
     return VS_OK;
 }
 
-template <int SCH>
+template <bool LIN>
 static int launch_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
                      cudaStream_t st) {
     const int n_pad = tc_n_pad(n_cams);
@@ -495,29 +474,26 @@ static int launch_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long
         set_error("vs_rpc_project_cube: cudaMemsetAsync failed");
         return VS_ERR_CUDA;
     }
-    cube_tc_prepare_kernel<SCH><<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(n_pad) * TcScheme<SCH>::kK, 256)),
+    cube_tc_prepare_kernel<LIN><<<static_cast<unsigned>(ceil_div(static_cast<int64_t>(n_pad) * TcScheme<LIN>::kK, 256)),
                                    256, 0, st>>>(cams, n_cams, n_pad, w);
     VS_LAUNCH_CHECK("cube_tc_prepare_kernel");
-    const size_t sh = cube_tc_smem<SCH>();
-    if (cudaFuncSetAttribute(cube_tc_kernel<SCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sh)) !=
+    const size_t sh = cube_tc_smem<LIN>();
+    if (cudaFuncSetAttribute(cube_tc_kernel<LIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sh)) !=
         cudaSuccess) {
         set_error("vs_rpc_project_cube: shared memory request of %zu bytes refused", sh);
         return VS_ERR_CUDA;
     }
     const long long tiles = ceil_div(n, static_cast<long long>(kTcTile));
     const unsigned grid = static_cast<unsigned>(std::max(1LL, std::min<long long>(tiles, sm_count())));
-    cube_tc_kernel<SCH><<<grid, kTcThreads, sh, st>>>(xyz, n, n_cams, n_pad, w, colrow, g_tc_wait_limit);
+    cube_tc_kernel<LIN><<<grid, kTcThreads, sh, st>>>(xyz, n, n_cams, n_pad, w, colrow, g_tc_wait_limit);
     VS_LAUNCH_CHECK("cube_tc_kernel");
     return VS_OK;
 }
 
 int launch_cube_tc(const VsRpcCamera *cams, int n_cams, const float *xyz, long long n, float *colrow, void *ws,
-                   cudaStream_t st, int scheme) {
-    switch (scheme) {
-        case 1: return launch_tc<1>(cams, n_cams, xyz, n, colrow, ws, st);
-        case 2: return launch_tc<2>(cams, n_cams, xyz, n, colrow, ws, st);
-        default: return launch_tc<0>(cams, n_cams, xyz, n, colrow, ws, st);
-    }
+                   cudaStream_t st, bool lin) {
+    return lin ? launch_tc<true>(cams, n_cams, xyz, n, colrow, ws, st)
+               : launch_tc<false>(cams, n_cams, xyz, n, colrow, ws, st);
 }
 
 }  // namespace vs

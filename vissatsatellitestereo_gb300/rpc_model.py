@@ -117,9 +117,8 @@ def project_cameras(meta_dicts, lat, lon, alt, mode='fast', shared=True, keep=Fa
 
 CUBE_VARIANTS = {'fp32': _lib.VS_CUBE_FP32, 'bf16x3': _lib.VS_CUBE_BF16X3, 'tf32x3': _lib.VS_CUBE_TF32X3,
                  'bf16x6': _lib.VS_CUBE_BF16X6, 'bf16x3_tc': _lib.VS_CUBE_BF16X3_TC,
-                 'bf16x3_lin': _lib.VS_CUBE_BF16X3_LIN, 'bf16x3_lin_tc': _lib.VS_CUBE_BF16X3_LIN_TC,
-                 'bf16x3_lin6_tc': _lib.VS_CUBE_BF16X3_LIN6_TC}
-TC_VARIANTS = ('bf16x3_tc', 'bf16x3_lin_tc', 'bf16x3_lin6_tc')
+                 'bf16x3_lin': _lib.VS_CUBE_BF16X3_LIN, 'bf16x3_lin_tc': _lib.VS_CUBE_BF16X3_LIN_TC}
+TC_VARIANTS = ('bf16x3_tc', 'bf16x3_lin_tc')
 
 
 def project_cube(meta_dicts, xyz, variant='tf32x3', out=None, check=True):
@@ -132,8 +131,7 @@ def project_cube(meta_dicts, xyz, variant='tf32x3', out=None, check=True):
     ``variant``: 'fp32' (CUDA cores), 'bf16x3', 'tf32x3', 'bf16x6' (tensor-core split forms),
     'bf16x3_tc' (BF16X3 on tcgen05), 'bf16x3_lin' (BF16X3 for the higher-order terms, the
     constant and linear terms in FP32), 'bf16x3_lin_tc' (the same with the contraction on
-    tcgen05), 'bf16x3_lin6_tc' (tcgen05, the constant and linear terms as six bf16 split
-    products in the tensor cores).
+    tcgen05).
     ``out``: optional preallocated (C, 2, N) float32 CUDA tensor.
     ``check``: for the tcgen05 variants, read the kernel's device-side status back (synchronises the
     stream) and raise ``VsError`` (VS_ERR_TIMEOUT) if a CTA gave up waiting for the tensor
