@@ -129,12 +129,16 @@ __global__ void fuse_kernel_large(const float *__restrict__ dsm, int layout, int
 // the [H][W][V] layout) in shared memory with cp.async (the hardware tracks completion:
 // no spin waits); each thread sorts its cell into its column of a view-major scratch
 // block beside the tile (conflict-free) and reads the originals for the mean from the
-// tile.  Unaligned inputs take the same cell code with the values read from global memory.
+// tile.  Stacks whose view rows are not 16-byte aligned are staged with 4-byte copies.
 constexpr int kTileCells = 128;
 
 __device__ __forceinline__ void cp_async16(float *smem_dst, const float *gmem_src) {
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(float *smem_dst, const float *gmem_src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gmem_src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
@@ -294,7 +298,7 @@ __device__ __forceinline__ float fuse_cell_v64(const float *xs, long long si, in
 template <int N>
 __global__ void __launch_bounds__(kTileCells) fuse_tile_kernel(const float *__restrict__ dsm, int layout, int V,
                                                                long long cells, float *__restrict__ out,
-                                                               long long n_tiles) {
+                                                               long long n_tiles, int aligned) {
     extern __shared__ __align__(16) float fsm[];           // the tile: V x 128 (VHW) or 128 x V (HWV)
     float *scratch = fsm + V * kTileCells;                 // sorted columns: N x 128
     const int t = threadIdx.x;
@@ -302,15 +306,22 @@ __global__ void __launch_bounds__(kTileCells) fuse_tile_kernel(const float *__re
     for (long long tl = blockIdx.x; tl < n_tiles; tl += gridDim.x) {
         const long long c0 = tl * kTileCells;
         const int len = static_cast<int>(min(static_cast<long long>(kTileCells), cells - c0));   // multiple of 4
-        if (vhw) {
-            const int chunks = len >> 2;
-            for (int q = t; q < V * (kTileCells / 4); q += kTileCells) {
-                const int v = q / (kTileCells / 4), ch = q - v * (kTileCells / 4);
-                if (ch < chunks) cp_async16(fsm + v * kTileCells + 4 * ch, dsm + v * cells + c0 + 4 * ch);
+        if (aligned) {               // 16-byte copies: rows (VHW) or blocks (HWV) start 16-byte aligned
+            if (vhw) {
+                const int chunks = len >> 2;
+                for (int q = t; q < V * (kTileCells / 4); q += kTileCells) {
+                    const int v = q / (kTileCells / 4), ch = q - v * (kTileCells / 4);
+                    if (ch < chunks) cp_async16(fsm + v * kTileCells + 4 * ch, dsm + v * cells + c0 + 4 * ch);
+                }
+            } else {
+                const int chunks = (len * V) >> 2;
+                for (int q = t; q < chunks; q += kTileCells) cp_async16(fsm + 4 * q, dsm + c0 * V + 4 * q);
             }
+        } else if (vhw) {            // 4-byte copies otherwise (a thread per cell, so t < len)
+            if (t < len)
+                for (int v = 0; v < V; ++v) cp_async4(fsm + v * kTileCells + t, dsm + v * cells + c0 + t);
         } else {
-            const int chunks = (len * V) >> 2;
-            for (int q = t; q < chunks; q += kTileCells) cp_async16(fsm + 4 * q, dsm + c0 * V + 4 * q);
+            for (int q = t; q < len * V; q += kTileCells) cp_async4(fsm + q, dsm + c0 * V + q);
         }
         cp_async_commit();
         cp_async_wait_all();
@@ -325,25 +336,10 @@ __global__ void __launch_bounds__(kTileCells) fuse_tile_kernel(const float *__re
     }
 }
 
-// Unaligned inputs: the values straight from global memory, the sorted column in shared
-// memory (one column per thread, odd stride against bank conflicts).
-template <int N>
-__global__ void __launch_bounds__(kTileCells) fuse_direct_kernel(const float *__restrict__ dsm, int layout, int V,
-                                                                 long long cells, float *__restrict__ out) {
-    __shared__ float cols[kTileCells * (N + 1)];
-    float *col = cols + threadIdx.x * (N + 1);
-    for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < cells;
-         c += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const float *xg = layout == VS_LAYOUT_VHW ? dsm + c : dsm + c * V;
-        const long long sg = layout == VS_LAYOUT_VHW ? cells : 1;
-        out[c] = fuse_cell_v64<N>(xg, sg, V, col, 1, xg, sg);
-    }
-}
-
 size_t fuse_tile_smem(int V, int N) { return sizeof(float) * static_cast<size_t>(V + N) * kTileCells; }
 
 template <int N>
-bool launch_fuse_v64(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
+bool launch_fuse_v64(const float *dsm, int layout, int V, long long cells, float *out, bool aligned, cudaStream_t st) {
     const size_t sh = fuse_tile_smem(V, N);
     static bool configured = false;     // per instantiation: room for the largest tile (V = N)
     if (!configured) {
@@ -358,48 +354,37 @@ bool launch_fuse_v64(const float *dsm, int layout, int V, long long cells, float
         return false;
     const long long n_tiles = ceil_div(cells, static_cast<long long>(kTileCells));
     const unsigned g = static_cast<unsigned>(std::min<long long>(n_tiles, 1LL * sm_count() * per_sm));
-    fuse_tile_kernel<N><<<g, kTileCells, sh, st>>>(dsm, layout, V, cells, out, n_tiles);
+    fuse_tile_kernel<N><<<g, kTileCells, sh, st>>>(dsm, layout, V, cells, out, n_tiles, aligned ? 1 : 0);
     return true;
 }
 
-// The staged kernel needs 16-byte aligned view rows (VHW) or blocks (HWV).
-bool fuse_tile_ok(const float *dsm, int layout, int V, long long cells) {
+// 16-byte copies need 16-byte aligned view rows (VHW) or cell blocks (HWV).
+bool fuse_tile_aligned(const float *dsm, int layout, int V, long long cells) {
     (void)layout;
     (void)V;
     return (reinterpret_cast<uintptr_t>(dsm) & 15) == 0 && cells % 4 == 0;
 }
 
 int launch_fuse_small(const float *dsm, int layout, int V, long long cells, float *out, cudaStream_t st) {
-    const bool staged = fuse_tile_ok(dsm, layout, V, cells);
-    if (!staged) {   // unaligned: one 64-slot instantiation (rare inputs)
-        const int threads = kTileCells;
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fuse_direct_kernel<64>, threads, 0) != cudaSuccess ||
-            per_sm <= 0)
-            per_sm = 1;
-        const unsigned g = static_cast<unsigned>(
-            std::max(1LL, std::min<long long>(ceil_div(cells, threads), 1LL * sm_count() * per_sm)));
-        fuse_direct_kernel<64><<<g, threads, 0, st>>>(dsm, layout, V, cells, out);
-        return VS_OK;
-    }
+    const bool aligned = fuse_tile_aligned(dsm, layout, V, cells);
     bool ok = false;
     switch ((V + 3) / 4) {
-        case 0: case 1: ok = launch_fuse_v64<4>(dsm, layout, V, cells, out, st); break;
-        case 2: ok = launch_fuse_v64<8>(dsm, layout, V, cells, out, st); break;
-        case 3: ok = launch_fuse_v64<12>(dsm, layout, V, cells, out, st); break;
-        case 4: ok = launch_fuse_v64<16>(dsm, layout, V, cells, out, st); break;
-        case 5: ok = launch_fuse_v64<20>(dsm, layout, V, cells, out, st); break;
-        case 6: ok = launch_fuse_v64<24>(dsm, layout, V, cells, out, st); break;
-        case 7: ok = launch_fuse_v64<28>(dsm, layout, V, cells, out, st); break;
-        case 8: ok = launch_fuse_v64<32>(dsm, layout, V, cells, out, st); break;
-        case 9: ok = launch_fuse_v64<36>(dsm, layout, V, cells, out, st); break;
-        case 10: ok = launch_fuse_v64<40>(dsm, layout, V, cells, out, st); break;
-        case 11: ok = launch_fuse_v64<44>(dsm, layout, V, cells, out, st); break;
-        case 12: ok = launch_fuse_v64<48>(dsm, layout, V, cells, out, st); break;
-        case 13: ok = launch_fuse_v64<52>(dsm, layout, V, cells, out, st); break;
-        case 14: ok = launch_fuse_v64<56>(dsm, layout, V, cells, out, st); break;
-        case 15: ok = launch_fuse_v64<60>(dsm, layout, V, cells, out, st); break;
-        default: ok = launch_fuse_v64<64>(dsm, layout, V, cells, out, st); break;
+        case 0: case 1: ok = launch_fuse_v64<4>(dsm, layout, V, cells, out, aligned, st); break;
+        case 2: ok = launch_fuse_v64<8>(dsm, layout, V, cells, out, aligned, st); break;
+        case 3: ok = launch_fuse_v64<12>(dsm, layout, V, cells, out, aligned, st); break;
+        case 4: ok = launch_fuse_v64<16>(dsm, layout, V, cells, out, aligned, st); break;
+        case 5: ok = launch_fuse_v64<20>(dsm, layout, V, cells, out, aligned, st); break;
+        case 6: ok = launch_fuse_v64<24>(dsm, layout, V, cells, out, aligned, st); break;
+        case 7: ok = launch_fuse_v64<28>(dsm, layout, V, cells, out, aligned, st); break;
+        case 8: ok = launch_fuse_v64<32>(dsm, layout, V, cells, out, aligned, st); break;
+        case 9: ok = launch_fuse_v64<36>(dsm, layout, V, cells, out, aligned, st); break;
+        case 10: ok = launch_fuse_v64<40>(dsm, layout, V, cells, out, aligned, st); break;
+        case 11: ok = launch_fuse_v64<44>(dsm, layout, V, cells, out, aligned, st); break;
+        case 12: ok = launch_fuse_v64<48>(dsm, layout, V, cells, out, aligned, st); break;
+        case 13: ok = launch_fuse_v64<52>(dsm, layout, V, cells, out, aligned, st); break;
+        case 14: ok = launch_fuse_v64<56>(dsm, layout, V, cells, out, aligned, st); break;
+        case 15: ok = launch_fuse_v64<60>(dsm, layout, V, cells, out, aligned, st); break;
+        default: ok = launch_fuse_v64<64>(dsm, layout, V, cells, out, aligned, st); break;
     }
     if (!ok) {
         set_error("fuse_tile_kernel: launch configuration refused");

@@ -942,7 +942,7 @@ constexpr int kMapThreads = 256;
 // Persistent binning of many views: a CTA takes work items (rows_per_item map rows of one
 // view) from a device counter until none are left.  Items [item_begin, item_end) of the
 // plan's item list.
-__global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
+__global__ void __launch_bounds__(kMapThreads, 4) map_bin_kernel(
     const MapViewDev *__restrict__ views, const AoiDev *__restrict__ aois, const long long *__restrict__ item_start,
     int v_lo, int v_hi, long long item_begin, long long item_end, int rows_per_item,
     unsigned long long *__restrict__ keys, unsigned long long *__restrict__ counter) {
@@ -1021,7 +1021,7 @@ __global__ void __launch_bounds__(kMapThreads) map_bin_kernel(
 // grid-strided so that the blocks sweep the key grids in order (L2 locality of the
 // halos).  Tile indices only grow, so every thread follows the view index with a forward
 // walk (one search at the start) and needs no barrier for it.
-__global__ void __launch_bounds__(TX *TY) map_epilogue_kernel(
+__global__ void __launch_bounds__(TX *TY, 6) map_epilogue_kernel(
     const MapViewDev *__restrict__ views, const AoiDev *__restrict__ aois, const long long *__restrict__ tile_start,
     int v_lo, int v_hi, long long tile_begin, long long tile_end, const unsigned long long *__restrict__ keys,
     float *__restrict__ dsm) {
@@ -1655,7 +1655,16 @@ extern "C" int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view
         VS_LAUNCH_CHECK("map_bin_kernel");
     }
     const long long t0 = plan->tile_start[view_begin], t1 = plan->tile_start[view_end];
-    const long long eblocks = std::min<long long>(t1 - t0, 1LL * sm_count() * 8);
+    // one resident wave of the persistent epilogue
+    static int epi_resident = 0;
+    if (!epi_resident) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, map_epilogue_kernel, TX * TY, 0) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 4;
+        epi_resident = per_sm;
+    }
+    const long long eblocks = std::min<long long>(t1 - t0, 1LL * sm_count() * epi_resident);
     map_epilogue_kernel<<<static_cast<unsigned>(eblocks), dim3(TX, TY), 0, st>>>(
         plan->d_views, plan->d_aois, plan->d_tile_start, view_begin, view_end - 1, t0, t1, keys, view_dsm);
     VS_LAUNCH_CHECK("map_epilogue_kernel");
