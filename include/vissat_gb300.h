@@ -278,19 +278,21 @@ typedef struct VsMapView {
 typedef struct VsAoiBatch VsAoiBatch;
 size_t vs_aoi_batch_plan_workspace_size(const VsAoi *aois, int n_aois, int n_views);
 int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView *views, int n_views,
-                      int rows_per_item, void *workspace, size_t workspace_bytes, VsAoiBatch **plan,
+                      int tile, void *workspace, size_t workspace_bytes, VsAoiBatch **plan,
                       void *stream);
 /* Cells of all views' DSMs (view v at the sum of the cells of views < v), of all fused
- * DSMs (AOI a at the sum of the cells of AOIs < a), and the scratch a run needs. */
+ * DSMs (AOI a at the sum of the cells of AOIs < a), and the scratch the fusion needs. */
 int vs_aoi_batch_query(const VsAoiBatch *plan, int64_t *view_cells, int64_t *fused_cells,
                        size_t *scratch_bytes);
-/* Rasterises views [view_begin, view_end) into their float32 DSMs: one persistent binning
- * launch over all their pixels (work items of rows_per_item map rows, taken from a
- * device-side counter by bin_blocks_per_sm CTAs per SM) and one epilogue launch over all
- * their 32x32 tiles (nanmax decode, hole fill, blur).  A single view is the per-view form.
- * view_dsm may be NULL when every view of the plan has its own `dsm` output. */
-int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int bin_blocks_per_sm,
-                     void *scratch, size_t scratch_bytes, float *view_dsm, void *stream);
+/* Rasterises views [view_begin, view_end) into their float32 DSMs in one persistent launch:
+ * CTAs (at most blocks_per_sm per SM) take work items -- one tile x tile block of one
+ * view's DSM, tile = 32 or 64 as planned -- from a device-side counter, bin the pixels that
+ * can reach the block (plus a 2-cell halo) into shared memory and run the epilogue
+ * (nanmax, hole fill, float32, blur) from there; no key grid is written to device memory.
+ * A single view is the per-view form.  view_dsm may be NULL when every view of the plan
+ * has its own `dsm` output. */
+int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int blocks_per_sm,
+                     float *view_dsm, void *stream);
 /* Fuses AOIs [aoi_begin, aoi_end) from their views' DSMs (vs_fuse_dsms per AOI). */
 int vs_aoi_batch_fuse(const VsAoiBatch *plan, int aoi_begin, int aoi_end, const float *view_dsm,
                       float *fused, int median_blur, void *scratch, size_t scratch_bytes, void *stream);

@@ -11,7 +11,7 @@ from oracle import maps as omaps
 pytestmark = pytest.mark.gpu
 
 
-def build_batch(specs, maps, affines, rows_per_item=8, pad=0):
+def build_batch(specs, maps, affines, tile=64, pad=0):
     from vissatsatellitestereo_gb300.batch import AoiBatch, AoiGrid, MapAffine, MapView
     grids, views = [], []
     for s, ms, afs in zip(specs, maps, affines):
@@ -23,7 +23,7 @@ def build_batch(specs, maps, affines, rows_per_item=8, pad=0):
             store[:, :W] = m
             vs.append(MapView(torch.from_numpy(store).cuda(), W, H, MapAffine(**a)))
         views.append(vs)
-    return AoiBatch(grids, views, rows_per_item=rows_per_item)
+    return AoiBatch(grids, views, tile=tile)
 
 
 def oracle_results(specs, maps, affines):
@@ -43,12 +43,12 @@ def small_case():
     return specs, maps, affines, oracle_results(specs, maps, affines)
 
 
-@pytest.mark.parametrize('rows_per_item,pad', [(8, 0), (1, 3), (64, 5), (3, 1)])
-def test_batch_matches_oracle(small_case, rows_per_item, pad):
+@pytest.mark.parametrize('tile,pad,blocks', [(64, 0, 4), (32, 3, 4), (64, 5, 1), (32, 1, 8)])
+def test_batch_matches_oracle(small_case, tile, pad, blocks):
     specs, maps, affines, (ref_views, ref_fused) = small_case
-    b = build_batch(specs, maps, affines, rows_per_item=rows_per_item, pad=pad)
+    b = build_batch(specs, maps, affines, tile=tile, pad=pad)
     vd, fu, sc = b.new_view_dsm(), b.new_fused(), b.new_scratch()
-    b.run(vd, sc)
+    b.run(vd, blocks_per_sm=blocks)
     b.fuse(vd, fu, sc)
     torch.cuda.synchronize()
     v = 0
@@ -63,11 +63,10 @@ def test_batch_matches_oracle(small_case, rows_per_item, pad):
 def test_per_view_runs_equal_the_batched_run(small_case):
     specs, maps, affines, _ = small_case
     b = build_batch(specs, maps, affines)
-    sc = b.new_scratch()
     one, many = b.new_view_dsm(), b.new_view_dsm()
-    b.run(many, sc)
+    b.run(many)
     for v in range(b.n_views):
-        b.run(one, sc, views=(v, v + 1), bin_blocks_per_sm=1)
+        b.run(one, views=(v, v + 1), blocks_per_sm=1)
     torch.cuda.synchronize()
     assert same_bits(one.cpu().numpy(), many.cpu().numpy())
 
@@ -86,8 +85,8 @@ def test_points_on_cell_boundaries():
     rng = np.random.default_rng(5)
     m = rng.normal(5.0, 1.0, (H, W)).astype(np.float32)
     b = build_batch([s], [[m]], [[aff]])
-    vd, fu, sc = b.new_view_dsm(), b.new_fused(), b.new_scratch()
-    b.run(vd, sc)
+    vd = b.new_view_dsm()
+    b.run(vd)
     torch.cuda.synchronize()
     g = {'xoff': s.xoff, 'yoff': s.yoff, 'xres': s.res, 'yres': s.res, 'xsize': s.xsize, 'ysize': s.ysize}
     assert same_bits(b.view_dsm(vd, 0).cpu().numpy(), omaps.view_dsm(m, aff, g))
@@ -125,3 +124,53 @@ def test_map_points_kernel_matches_oracle(small_case):
             assert same_bits(pts.cpu().numpy(), omaps.map_points(m, aff))
             d = median_blur3x3(proj_to_grid(pts, s.xoff, s.yoff, s.res, s.res, s.xsize, s.ysize))
             assert same_bits(d.cpu().numpy() if isinstance(d, torch.Tensor) else d, ref_views[a][k])
+
+
+def _geometry_cases():
+    """Views whose pixel boxes stress the tile kernel: large rotations, a mirrored map,
+    pixels much larger and much smaller than cells, a map half off the grid, one far away
+    and a singular (rank-one) map; grids spanning several tiles."""
+    from vissatsatellitestereo_gb300 import synth
+    rng = np.random.default_rng(11)
+    cases = []
+
+    def heights(H, W):
+        m = (rng.normal(0.0, 0.3, (H, W)) + rng.choice([0.0, 10.0, 25.0], (H, W), p=[0.6, 0.3, 0.1]))
+        m = m.astype(np.float32)
+        m[rng.random((H, W)) < 0.15] = np.nan
+        zeros = rng.random((H, W)) < 0.02
+        m[zeros] = np.where(rng.random(zeros.sum()) < 0.5, np.float32(0.0), np.float32(-0.0))
+        return m
+
+    s = synth.AoiSpec(0, 354052.25, 6182702.5, 0.5, 150, 130, 1, 0, 1)
+    ce, cn = s.xoff + 37.5, s.yoff - 32.5
+    cases.append(('rotated', s, heights(200, 180), synth.map_affine(ce, cn, 0.4, 0.7)))
+    mir = synth.map_affine(ce + 3.0, cn - 2.0, 0.45, 2.5)
+    mir['ej'], mir['nj'] = -mir['ej'], -mir['nj']
+    cases.append(('mirrored', s, heights(170, 190), mir))
+    cases.append(('sparse', s, heights(60, 70), synth.map_affine(ce, cn, 1.7, 0.2)))
+    cases.append(('half_off_grid', s, heights(150, 160), synth.map_affine(s.xoff + 5.0, cn, 0.45, -0.1)))
+    cases.append(('far_away', s, heights(40, 40), synth.map_affine(ce + 5000.0, cn, 0.5, 0.0)))
+    sing = synth.map_affine(ce, cn, 0.4, 0.0)
+    sing['ei'], sing['ni'] = sing['ej'], sing['nj']
+    cases.append(('singular', s, heights(90, 90), sing))
+    d = synth.AoiSpec(0, 300001.0, 4300123.75, 1.0, 70, 66, 1, 0, 1)
+    cases.append(('dense', d, heights(700, 640), synth.map_affine(d.xoff + 33.0, d.yoff - 31.0, 0.1, 0.3)))
+    return cases
+
+
+@pytest.mark.parametrize('tile', [32, 64])
+def test_tile_pixel_boxes_cover_every_geometry(tile):
+    """Each view's DSM equals the oracle bit for bit: every pixel that reaches a tile (and
+    its halo) lies inside the tile's pixel box, whatever the map's rotation, mirroring,
+    scale or rank."""
+    cases = _geometry_cases()
+    specs = [c[1] for c in cases]
+    b = build_batch(specs, [[c[2]] for c in cases], [[c[3]] for c in cases], tile=tile, pad=1)
+    vd = b.new_view_dsm()
+    b.run(vd)
+    torch.cuda.synchronize()
+    for v, (name, s, m, aff) in enumerate(cases):
+        g = {'xoff': s.xoff, 'yoff': s.yoff, 'xres': s.res, 'yres': s.res, 'xsize': s.xsize, 'ysize': s.ysize}
+        assert same_bits(b.view_dsm(vd, v).cpu().numpy(), omaps.view_dsm(m, aff, g)), name
+    b.close()

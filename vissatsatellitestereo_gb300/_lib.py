@@ -82,7 +82,7 @@ SIGNATURES = {
     'vs_aoi_batch_plan_workspace_size': (_sz, [_vp, _int, _int]),
     'vs_aoi_batch_plan': (_int, [_vp, _int, _vp, _int, _int, _vp, _sz, _vp, _vp]),
     'vs_aoi_batch_query': (_int, [_vp, _vp, _vp, _vp]),
-    'vs_aoi_batch_run': (_int, [_vp, _int, _int, _int, _vp, _sz, _vp, _vp]),
+    'vs_aoi_batch_run': (_int, [_vp, _int, _int, _int, _vp, _vp]),
     'vs_aoi_batch_fuse': (_int, [_vp, _int, _int, _vp, _vp, _int, _vp, _sz, _vp]),
     'vs_aoi_batch_destroy': (None, [_vp]),
     'vs_dsm_from_points_overlap_workspace_size': (_sz, [_int, _i64, _i64]),

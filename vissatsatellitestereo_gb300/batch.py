@@ -4,8 +4,9 @@ The reference produces one AOI at a time: per view, the depth map's pixels becom
 points (aggregate_2p5d_util.py:75-98), ``produce_dsm_from_points`` rasterises them
 (produce_dsm.py:46-58: proj_to_grid + the float32 3x3 median blur), and ``run_fuse``
 fuses the AOI's views (aggregate_2p5d.py:65-81).  ``AoiBatch`` plans many AOIs at once:
-the rasterisation of all their views is one persistent binning launch and one epilogue
-launch (``run``), and the fusion follows per AOI (``fuse``).  A view's points are its
+the rasterisation of all their views is one persistent launch over tiles of their DSMs,
+each binned and finished in shared memory (``run``), and the fusion follows per AOI
+(``fuse``).  A view's points are its
 height-map pixels placed by a fixed-point affine pixel -> UTM map (``MapAffine``), whose
 coordinates are exact doubles, so every DSM is bit-identical to materialising the FP64
 point list and running the per-view reference path.
@@ -83,13 +84,15 @@ class AoiBatch:
     ``fuse()`` fuses each AOI's views into the fused buffer.  ``view_dsm(v)`` and
     ``fused_dsm(a)`` return the (H, W) slices."""
 
-    def __init__(self, grids, views, rows_per_item=8):
+    def __init__(self, grids, views, tile=64):
         require_cuda()
         self.grids = list(grids)
         self.views = [list(vs) for vs in views]
         if len(self.grids) != len(self.views):
             raise ValueError('one view list per AOI grid')
-        self.rows_per_item = int(rows_per_item)
+        self.tile = int(tile)
+        if self.tile not in (32, 64):
+            raise ValueError('tile must be 32 or 64')
         n_aois = len(self.grids)
         flat = [(a, v) for a, vs in enumerate(self.views) for v in vs]
         self.n_views = len(flat)
@@ -122,7 +125,7 @@ class AoiBatch:
         nbytes = lib.vs_aoi_batch_plan_workspace_size(self.aoi_arr, n_aois, self.n_views)
         self._plan_ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device='cuda')
         self._plan = ctypes.c_void_p()
-        _lib.call('vs_aoi_batch_plan', self.aoi_arr, n_aois, self.view_arr, self.n_views, self.rows_per_item,
+        _lib.call('vs_aoi_batch_plan', self.aoi_arr, n_aois, self.view_arr, self.n_views, self.tile,
                   self._plan_ws.data_ptr(), self._plan_ws.numel(), ctypes.byref(self._plan), stream_handle())
         vc, fc, sb = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_size_t()
         _lib.call('vs_aoi_batch_query', self._plan, ctypes.byref(vc), ctypes.byref(fc), ctypes.byref(sb))
@@ -157,12 +160,12 @@ class AoiBatch:
     def new_scratch(self):
         return torch.empty(self.scratch_bytes, dtype=torch.uint8, device='cuda')
 
-    def run(self, view_dsm, scratch, views=None, bin_blocks_per_sm=4):
+    def run(self, view_dsm, views=None, blocks_per_sm=4):
         """Rasterise views[0]..views[1]-1 (all by default) into ``view_dsm`` (views with
         their own ``dsm`` output write there; ``view_dsm`` may then be None)."""
         v0, v1 = (0, self.n_views) if views is None else views
-        _lib.call('vs_aoi_batch_run', self._plan, v0, v1, int(bin_blocks_per_sm), scratch.data_ptr(),
-                  scratch.numel(), None if view_dsm is None else view_dsm.data_ptr(), stream_handle())
+        _lib.call('vs_aoi_batch_run', self._plan, v0, v1, int(blocks_per_sm),
+                  None if view_dsm is None else view_dsm.data_ptr(), stream_handle())
         return view_dsm
 
     def fuse(self, view_dsm, fused, scratch, aois=None, median_blur=True):

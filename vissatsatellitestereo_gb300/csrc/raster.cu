@@ -234,21 +234,6 @@ __device__ __forceinline__ bool axis_fast(const FastAxis &a, long long bv, int &
     return ok;
 }
 
-// axis_fast from the difference d itself.  For a contained grid the origin-binade test is
-// implied: d is monotone in the coordinate, and every coordinate outside the origin's
-// binade lies at least two cells outside [0, tmax).  One unsigned compare covers d < 0.
-__device__ __forceinline__ bool axis_from_d(const FastAxis &a, long long d, int &r, bool &sure) {
-    const bool ok = static_cast<unsigned long long>(d) < static_cast<unsigned long long>(a.tmax);
-    const unsigned u = static_cast<unsigned>(static_cast<unsigned long long>(d) >> a.shift);
-    const float q = __fmul_rn(__uint2float_rn(u), a.scale);
-    const float big = __fadd_rn(q, 12582912.0f);
-    const float fr = __fsub_rn(q, __fsub_rn(big, 12582912.0f));
-    const int rn = static_cast<int>(static_cast<unsigned>(__float_as_int(big)) - 0x4b400000u);
-    r = min(max(rn - (fr < 0.0f ? 1 : 0), 0), a.nm1);
-    sure = fabsf(fr) > __fmaf_rn(a.err_rel, q, a.err_abs);
-    return ok;
-}
-
 __device__ __noinline__ int axis_correct(const long long *thr, int r, long long d) {
     for (int it = 0; it < 8 && __ldg(thr + r) > d; ++it) --r;
     for (int it = 0; it < 8 && __ldg(thr + r + 1) <= d; ++it) ++r;
@@ -408,6 +393,15 @@ __device__ __forceinline__ unsigned long long select8(const unsigned long long (
     return b2 ? c1 : c0;
 }
 
+// numpy's median from the middle keys of n sorted values (n odd: lo == hi's slot).
+__device__ __forceinline__ double median_from_middle(unsigned long long lo, unsigned long long hi, int n) {
+    if (n & 1) {
+        if (hi == 0x7fffffffffffffffull) hi = kZeroKey;   // -0 + 0 = +0
+        return double_from_key(hi);
+    }
+    return rare_dmul(rare_dadd(rare_dadd(0.0, double_from_key(lo)), double_from_key(hi)), 0.5);
+}
+
 __device__ __forceinline__ double median8_keys(unsigned long long (&s)[8]) {
     int n = 0;
 #pragma unroll
@@ -422,13 +416,7 @@ __device__ __forceinline__ double median8_keys(unsigned long long (&s)[8]) {
     cswap(s[0], s[4]); cswap(s[1], s[5]); cswap(s[2], s[6]); cswap(s[3], s[7]);
     cswap(s[2], s[4]); cswap(s[3], s[5]);
     cswap(s[1], s[2]); cswap(s[3], s[4]); cswap(s[5], s[6]);
-    const unsigned long long lo = select8(s, (n - 1) >> 1);
-    unsigned long long hi = select8(s, n >> 1);
-    if (n & 1) {
-        if (hi == 0x7fffffffffffffffull) hi = kZeroKey;   // -0 + 0 = +0
-        return double_from_key(hi);
-    }
-    return rare_dmul(rare_dadd(rare_dadd(0.0, double_from_key(lo)), double_from_key(hi)), 0.5);
+    return median_from_middle(select8(s, (n - 1) >> 1), select8(s, n >> 1), n);
 }
 
 __device__ __forceinline__ bool nan_double(double v) {
@@ -859,7 +847,6 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
 // exponent field, which the axis test rejects (off-grid, as the containment guarantees).
 // So each pixel is binned with integer and FP32 operations only, reading 4 bytes.
 constexpr unsigned long long kMapIdxLimit = 1ull << 28;   // pixels per view
-constexpr unsigned long long kMapZeroSpan = kMapIdxLimit << 1;
 
 // FP64 point list of one height map in pixel order (the plain per-view form's input):
 // pixel (i, j) -> (easting, northing, height) with easting = (e0 + ej (2j+1-W) + ei (2i+1-H))
@@ -888,12 +875,17 @@ struct MapViewDev {
     int W, H;
     int aoi;
     int vec;                  // rows are 16-byte aligned: float4 loads
-    long long off;            // cell offset of the view's key grid (and default DSM slot)
+    long long off;            // cell offset of the view's DSM in the run's buffer
     float *out;               // the view's DSM, or null: the run's buffer at `off`
     // the axes' differences from the grid origin (in ulps of the origin's binade) are
     // affine in the pixel indices: d = d0 + d_di * (2i+1-H) + d_dj * (2j+1-W)
     long long dc0, dc_di, dc_dj;   // columns: bits(x) - bits(xoff)
     long long dr0, dr_di, dr_dj;   // rows:    bits(yoff) - bits(y)
+    // pixel box of a cell region: pixel (i, j) as an affine function of the cell
+    // coordinates (s_col, s_row) = (d_col, d_row) * ulp / res (cell r spans [r, r + 1))
+    double bi0, bic, bir, bj0, bjc, bjr;
+    double bmarg;             // pixels added on each side of a box (rounding of the map)
+    int box_all;              // singular map: every tile reads the whole map
 };
 
 struct AoiDev {
@@ -901,30 +893,6 @@ struct AoiDev {
     long long bx, by;         // bit-pattern bases of the origins' binades
     int shx, shy;
     int xsize, ysize;
-};
-
-// 64-bit key of double(h) from the float's bits; zeros carry their complemented pixel index
-// and sign in the low bits (kZeroKey + 2*(limit-1-idx) + sign), so the largest zero key is
-// the first zero and no per-cell "first zero" word is needed.  Non-zero FP32 values have
-// keys at least 2^61 away from kZeroKey.
-__device__ __noinline__ unsigned long long map_key_rare(unsigned hb) {
-    return key_from_double(f32_to_f64(__uint_as_float(hb)));
-}
-
-__device__ __forceinline__ unsigned long long map_key(unsigned hb, unsigned long long idx) {
-    const unsigned mag = hb & 0x7fffffffu;
-    if (mag == 0u) return kZeroKey + (((kMapIdxLimit - 1ull - idx) << 1) | (hb >> 31));
-    if ((mag >> 23) - 1u >= 254u) return map_key_rare(hb);     // subnormal or infinite
-    const unsigned long long db = (static_cast<unsigned long long>(mag) << 29) + (896ull << 52);
-    return (hb >> 31) ? (0x7fffffffffffffffull - db) : (db | 0x8000000000000000ull);
-}
-
-// Resolves the zero keys of a map-fed key grid to the keys of +0.0 / -0.0.
-struct MapZeroDecoder {
-    __device__ __forceinline__ unsigned long long operator()(unsigned long long k, long long) const {
-        if (k - kZeroKey < kMapZeroSpan) return (k & 1ull) ? 0x7fffffffffffffffull : kZeroKey;
-        return k;
-    }
 };
 
 // Largest index i in [lo, hi] with starts[i] <= x (starts ascending, starts[lo] <= x).
@@ -938,109 +906,367 @@ __device__ __forceinline__ int find_range(const long long *starts, int lo, int h
 }
 
 constexpr int kMapThreads = 256;
+constexpr unsigned kMapKeyZero = 0x80000000u;   // key of +0.0f; any zero while binning
+constexpr int kMapUnitPx = 8;                   // consecutive pixels of a row per thread step
 
-// Persistent binning of many views: a CTA takes work items (rows_per_item map rows of one
-// view) from a device counter until none are left.  Items [item_begin, item_end) of the
-// plan's item list.
-__global__ void __launch_bounds__(kMapThreads, 4) map_bin_kernel(
-    const MapViewDev *__restrict__ views, const AoiDev *__restrict__ aois, const long long *__restrict__ item_start,
-    int v_lo, int v_hi, long long item_begin, long long item_end, int rows_per_item,
-    unsigned long long *__restrict__ keys, unsigned long long *__restrict__ counter) {
-    __shared__ long long s_item;
-    __shared__ int s_view;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const long long it = item_begin + static_cast<long long>(atomicAdd(counter, 1ull));
-            s_item = it;
-            s_view = it < item_end ? find_range(item_start, v_lo, v_hi, it) : -1;
+// Shared-memory tile of one work item: an OW x OH block of one view's DSM.  The key tile
+// carries a 2-cell halo (the hole fill of the blur's 1-cell halo needs its neighbours);
+// its keys are 32-bit order keys of the float32 heights (0: no point), enough for the
+// nanmax because the heights are float32.  The "first zero" words, needed only when a
+// cell's maximum is a zero, share storage with the epilogue's arrays.
+template <int OW, int OH>
+struct MapTileSmem {
+    static constexpr int KW = OW + 4, KH = OH + 4, FW = OW + 2, FH = OH + 2;
+    static constexpr int NK = KW * KH, NF = FW * FH;
+    unsigned keys[NK];
+    union {
+        unsigned zw[NK];                    // (2^28 - 1 - first zero's pixel) << 1 | its sign
+        struct {
+            float fk[FH][FW];               // hole-filled values: the blur's input
+            unsigned short holes[NF];       // empty in-grid cells of the blur input
+        } e;
+    } u;
+    long long item;
+    int view, r0, c0, ia, ib, ja, jb;
+    int n_holes, has_zero;
+    unsigned char specrow[FH];              // a NaN or a zero in this row of the blur input
+};
+
+// Row/column estimate from the difference d (contained grid: the origin-binade test is
+// implied, since d is monotone in the coordinate and every coordinate outside the
+// origin's binade lies at least two cells outside [0, tmax); one unsigned compare covers
+// d < 0).  The estimate is not clamped into the grid: the key tile's own bounds test
+// drops any row or column outside it, and the rare correction clamps first.
+__device__ __forceinline__ bool axis_tile(const FastAxis &a, long long d, int &r, bool &sure) {
+    const bool ok = static_cast<unsigned long long>(d) < static_cast<unsigned long long>(a.tmax);
+    const unsigned u = static_cast<unsigned>(static_cast<unsigned long long>(d) >> a.shift);
+    const float q = __fmul_rn(__uint2float_rn(u), a.scale);
+    const float big = __fadd_rn(q, 12582912.0f);
+    const float fr = __fsub_rn(q, __fsub_rn(big, 12582912.0f));
+    r = static_cast<int>(static_cast<unsigned>(__float_as_int(big)) - 0x4b400000u) - (fr < 0.0f ? 1 : 0);
+    sure = fabsf(fr) > __fmaf_rn(a.err_rel, q, a.err_abs);
+    return ok;
+}
+
+// One pass over the item's pixel box [ia, ib] x [ja, jb] (ja a multiple of 4 for float4
+// rows).  Every pixel is binned exactly as the per-view path bins its FP64 point (the
+// integer/FP32 axis test and the threshold correction); pixels whose cell lies outside
+// the key tile are dropped.  ZERO = false: the nanmax keys, zeros as kMapKeyZero;
+// ZERO = true: for cells whose maximum is a zero, the first zero pixel and its sign.
+template <int OW, int OH, bool ZERO>
+__device__ __forceinline__ void map_tile_pass(const MapViewDev &mv, const FastAxis &R, const FastAxis &C, int rbase,
+                                              int cbase, int ia, int ib, int ja, int jb, MapTileSmem<OW, OH> &sm) {
+    using S = MapTileSmem<OW, OH>;
+    constexpr int P = kMapUnitPx;
+    const int G = (jb - ja) / P + 1;                    // P-pixel groups per box row
+    const int units = (ib - ia + 1) * G;
+    int row = threadIdx.x / G, g = threadIdx.x - row * G;
+    const int rstep = kMapThreads / G, gstep = kMapThreads - rstep * G;
+    const long long scol = 2 * mv.dc_dj, srow = 2 * mv.dr_dj;   // per pixel along a row
+    bool zero_seen = false;
+    for (int unit = threadIdx.x; unit < units; unit += kMapThreads) {
+        const int i = ia + row, j0 = ja + g * P;
+        const float *src = mv.map + static_cast<long long>(i) * mv.stride + j0;
+        unsigned hb[P];
+        if (mv.vec && j0 + P <= mv.W) {
+#pragma unroll
+            for (int q = 0; q < P / 4; ++q) {
+                const float4 v4 = __ldg(reinterpret_cast<const float4 *>(src) + q);
+                hb[4 * q] = __float_as_uint(v4.x); hb[4 * q + 1] = __float_as_uint(v4.y);
+                hb[4 * q + 2] = __float_as_uint(v4.z); hb[4 * q + 3] = __float_as_uint(v4.w);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < P; ++k) hb[k] = j0 + k < mv.W ? __float_as_uint(__ldg(src + k)) : 0x7fc00000u;
         }
-        __syncthreads();
-        const long long it = s_item;
-        const int v = s_view;
-        __syncthreads();
-        if (it >= item_end) return;
-        const MapViewDev mv = views[v];
-        const AoiDev &ad = aois[mv.aoi];
-        const FastAxis R = ad.row, C = ad.col;
-        const unsigned ncols32 = static_cast<unsigned>(ad.xsize);
-        unsigned long long *vk = keys + mv.off;
-        const int i0 = static_cast<int>(it - __ldg(item_start + v)) * rows_per_item;
-        const int i1 = min(i0 + rows_per_item, mv.H);
-        const int groups = (mv.W + 3) >> 2;          // 4-pixel groups per row
-        int i = i0, g = threadIdx.x;
-        while (g >= groups && i < i1) { g -= groups; ++i; }
-        for (; i < i1;) {
-            const int j0 = g << 2;
-            const float *row = mv.map + static_cast<long long>(i) * mv.stride;
-            unsigned hb[4];
-            if (mv.vec && j0 + 4 <= mv.W) {
-                const float4 q = __ldcs(reinterpret_cast<const float4 *>(row + j0));
-                hb[0] = __float_as_uint(q.x); hb[1] = __float_as_uint(q.y);
-                hb[2] = __float_as_uint(q.z); hb[3] = __float_as_uint(q.w);
+        const int di2 = 2 * i + 1 - mv.H, dj0 = 2 * j0 + 1 - mv.W;
+        long long dcol = mv.dc0 + mv.dc_di * di2 + mv.dc_dj * dj0;
+        long long drow = mv.dr0 + mv.dr_di * di2 + mv.dr_dj * dj0;
+        // rows: d is affine along the unit, and the exact row monotone in d, so when the
+        // first and the last pixel fall in the same row with sure estimates, all do
+        int ra, rb;
+        bool sa, sb;
+        const bool oka = axis_tile(R, drow, ra, sa), okb = axis_tile(R, drow + (P - 1) * srow, rb, sb);
+        const bool row_fixed = oka & okb & sa & sb & (ra == rb);
+        const unsigned lr_fixed = static_cast<unsigned>(ra - rbase);
+        int cell[P];
+        unsigned key[P];
+#pragma unroll
+        for (int k = 0; k < P; ++k, dcol += scol, drow += srow) {
+            const unsigned mag = hb[k] & 0x7fffffffu;
+            int c;
+            bool sc;
+            bool ok = ZERO ? mag == 0u : mag <= 0x7f800000u;    // not NaN
+            unsigned lr = lr_fixed;
+            if (!row_fixed) {
+                int r;
+                bool sr;
+                ok &= axis_tile(R, drow, r, sr);
+                if (ok && !sr) r = axis_correct(R.thr, min(max(r, 0), R.nm1), drow);
+                lr = static_cast<unsigned>(r - rbase);
+            }
+            ok &= axis_tile(C, dcol, c, sc);
+            if (ok && !sc) c = axis_correct(C.thr, min(max(c, 0), C.nm1), dcol);
+            const unsigned lc = static_cast<unsigned>(c - cbase);
+            ok &= (lr < static_cast<unsigned>(S::KH)) & (lc < static_cast<unsigned>(S::KW));
+            cell[k] = ok ? static_cast<int>(lr) * S::KW + static_cast<int>(lc) : -1;
+            if (ZERO) {
+                const unsigned idx = static_cast<unsigned>(i) * static_cast<unsigned>(mv.W) + static_cast<unsigned>(j0 + k);
+                key[k] = ((static_cast<unsigned>(kMapIdxLimit) - 1u - idx) << 1) | (hb[k] >> 31);
             } else {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) hb[k] = j0 + k < mv.W ? __float_as_uint(__ldcs(row + j0 + k)) : 0x7fc00000u;
+                zero_seen |= ok & (mag == 0u);
+                key[k] = mag == 0u ? kMapKeyZero : ((hb[k] >> 31) ? ~hb[k] : (hb[k] | 0x80000000u));
             }
-            const int di2 = 2 * i + 1 - mv.H, dj0 = 2 * j0 + 1 - mv.W;
-            long long dcol = mv.dc0 + mv.dc_di * di2 + mv.dc_dj * dj0;
-            long long drow = mv.dr0 + mv.dr_di * di2 + mv.dr_dj * dj0;
-            const long long scol = 2 * mv.dc_dj, srow = 2 * mv.dr_dj;   // per pixel along the row
-            unsigned cell[4];                 // 32-bit: the plan keeps grids below 2^31 cells
-            unsigned long long key[4];
-            bool okk[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k, dcol += scol, drow += srow) {
-                int r, c;
-                bool sr, sc;
-                bool ok = axis_from_d(R, drow, r, sr);
-                ok &= axis_from_d(C, dcol, c, sc);
-                ok &= (hb[k] & 0x7fffffffu) <= 0x7f800000u;     // not NaN
-                if (ok && !sr) r = axis_correct(R.thr, r, drow);
-                if (ok && !sc) c = axis_correct(C.thr, c, dcol);
-                const unsigned long long idx = static_cast<unsigned long long>(i) * static_cast<unsigned>(mv.W) + (j0 + k);
-                key[k] = ok ? map_key(hb[k], idx) : kEmptyKey;
-                cell[k] = static_cast<unsigned>(r) * ncols32 + static_cast<unsigned>(c);
-                okk[k] = ok;
-            }
-#pragma unroll
-            for (int k = 1; k < 4; ++k) {     // merge runs of consecutive pixels in one cell
-                const bool same = okk[k] & okk[k - 1] & (cell[k] == cell[k - 1]);
-                key[k] = same ? max(key[k], key[k - 1]) : key[k];
-                key[k - 1] = same ? kEmptyKey : key[k - 1];
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (key[k] != kEmptyKey) atomicMax(vk + cell[k], key[k]);
-            g += kMapThreads;
-            while (g >= groups && i < i1) { g -= groups; ++i; }
         }
+        if (ZERO) {
+#pragma unroll
+            for (int k = 0; k < P; ++k)
+                if (cell[k] >= 0 && sm.keys[cell[k]] == kMapKeyZero) atomicMax(&sm.u.zw[cell[k]], key[k]);
+        } else {
+#pragma unroll
+            for (int k = 1; k < P; ++k) {     // merge runs of consecutive pixels in one cell
+                const bool same = (cell[k] >= 0) & (cell[k] == cell[k - 1]);
+                key[k] = same ? max(key[k], key[k - 1]) : key[k];
+                cell[k - 1] = same ? -1 : cell[k - 1];
+            }
+#pragma unroll
+            for (int k = 0; k < P; ++k)
+                if (cell[k] >= 0) atomicMax(&sm.keys[cell[k]], key[k]);
+        }
+        g += gstep;
+        row += rstep;
+        if (g >= G) {
+            g -= G;
+            ++row;
+        }
+    }
+    if (!ZERO && zero_seen) sm.has_zero = 1;
+}
+
+// cswap on 32-bit keys.
+__device__ __forceinline__ void cswap32(unsigned &a, unsigned &b) {
+    const unsigned lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+__device__ __forceinline__ unsigned select8_32(const unsigned (&s)[8], int idx) {
+    const bool b0 = idx & 1, b1 = idx & 2, b2 = idx & 4;
+    const unsigned a0 = b0 ? s[1] : s[0], a1 = b0 ? s[3] : s[2];
+    const unsigned a2 = b0 ? s[5] : s[4], a3 = b0 ? s[7] : s[6];
+    const unsigned c0 = b1 ? a1 : a0, c1 = b1 ? a3 : a2;
+    return b2 ? c1 : c0;
+}
+
+// 64-bit double order key of a non-zero 32-bit float order key.
+__device__ __forceinline__ unsigned long long key64_of_key32(unsigned k) {
+    return key_from_double(f32_to_f64(float_from_key(k)));
+}
+
+// numpy's median of the non-empty 32-bit keys among 8 (at least one), as float32: the
+// float keys order like the double keys of the same values, so the 8-input network runs
+// on 32-bit keys and only the middle ones are widened for the FP64 mean.
+__device__ __forceinline__ float median8_keys32(unsigned (&s)[8]) {
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        n += s[i] != 0u;
+        s[i] = s[i] ? s[i] : ~0u;                      // empty sorts last
+    }
+    cswap32(s[0], s[1]); cswap32(s[2], s[3]); cswap32(s[4], s[5]); cswap32(s[6], s[7]);
+    cswap32(s[0], s[2]); cswap32(s[1], s[3]); cswap32(s[4], s[6]); cswap32(s[5], s[7]);
+    cswap32(s[1], s[2]); cswap32(s[5], s[6]);
+    cswap32(s[0], s[4]); cswap32(s[1], s[5]); cswap32(s[2], s[6]); cswap32(s[3], s[7]);
+    cswap32(s[2], s[4]); cswap32(s[3], s[5]);
+    cswap32(s[1], s[2]); cswap32(s[3], s[4]); cswap32(s[5], s[6]);
+    const unsigned lo = select8_32(s, (n - 1) >> 1), hi = select8_32(s, n >> 1);
+    if (n & 1) return float_from_key(hi == 0x7fffffffu ? kMapKeyZero : hi);   // -0 + 0 = +0
+    return f64_to_f32(median_from_middle(key64_of_key32(lo), key64_of_key32(hi), n));
+}
+
+// The tile's epilogue from shared memory: nanmax keys -> hole fill (non-propagating,
+// median of the non-empty 3x3 neighbours) -> float32 -> 3x3 median blur, written to the
+// view's DSM; the same arithmetic as epilogue_tile.  Output rows whose 3x3 windows hold
+// no NaN and no zero take the sorted-column median (bit-identical there); the others run
+// OpenCV's network per cell.  Clears the key tile for the next item.
+template <int OW, int OH>
+__device__ __forceinline__ void map_tile_finish(MapTileSmem<OW, OH> &sm, float *__restrict__ out, int H, int W,
+                                                int r0, int c0) {
+    using S = MapTileSmem<OW, OH>;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const float qnan = __uint_as_float(0x7fffffffu);
+    for (int base = 0; base < S::NF; base += kMapThreads) {
+        const int idx = base + tid;
+        const bool in = idx < S::NF;
+        const int ly = idx / S::FW, lx = idx - ly * S::FW;
+        const bool grid = in && static_cast<unsigned>(r0 - 1 + ly) < static_cast<unsigned>(H) &&
+                          static_cast<unsigned>(c0 - 1 + lx) < static_cast<unsigned>(W);
+        const unsigned k = in ? sm.keys[(ly + 1) * S::KW + lx + 1] : 1u;
+        if (in) {
+            const float f = k ? float_from_key(k) : qnan;
+            sm.u.e.fk[ly][lx] = f;
+            if (grid && k && f == 0.0f) sm.specrow[ly] = 1;
+        }
+        const unsigned empty = __ballot_sync(0xffffffffu, grid && k == 0u);
+        if (empty) {
+            int slot = 0;
+            if (lane == __ffs(empty) - 1) slot = atomicAdd(&sm.n_holes, __popc(empty));
+            slot = __shfl_sync(0xffffffffu, slot, __ffs(empty) - 1);
+            if (grid && k == 0u) sm.u.e.holes[slot + __popc(empty & ((1u << lane) - 1u))] = static_cast<unsigned short>(idx);
+        }
+    }
+    __syncthreads();
+    for (int h = tid; h < sm.n_holes; h += kMapThreads) {
+        const int idx = sm.u.e.holes[h];
+        const int ly = idx / S::FW, lx = idx - ly * S::FW;
+        unsigned s8[8];
+        int m = 0;
+#pragma unroll
+        for (int dj = 0; dj < 3; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 3; ++dk)
+                if (dj != 1 || dk != 1) s8[m++] = sm.keys[(ly + dj) * S::KW + lx + dk];
+        const unsigned any = s8[0] | s8[1] | s8[2] | s8[3] | s8[4] | s8[5] | s8[6] | s8[7];
+        const float f = any ? median8_keys32(s8) : qnan;
+        sm.u.e.fk[ly][lx] = f;
+        if (isnan(f) || f == 0.0f) sm.specrow[ly] = 1;
+    }
+    __syncthreads();
+    for (int i = tid; i < S::NK; i += kMapThreads) sm.keys[i] = 0u;   // dead until the next item
+    const bool line = H == 1 || W == 1;
+    constexpr int HALVES = OW / 32;
+    const float(&fk)[S::FH][S::FW] = sm.u.e.fk;
+    for (int p = tid >> 5; p < OH * HALVES; p += kMapThreads / 32) {
+        const int oy = p / HALVES, h = p - oy * HALVES;
+        const int r = r0 + oy, c = c0 + 32 * h + lane;
+        const int fx = 32 * h + lane + 1;
+        int ya = oy, yb = oy + 1, yc = oy + 2;
+        if (r == 0) ya = yb;
+        if (r == H - 1) yc = yb;
+        if (!line && !(sm.specrow[oy] | sm.specrow[oy + 1] | sm.specrow[oy + 2])) {
+            // sorted-column median: lane owns one column of a 32-column half row; lanes 0
+            // and 31 also sort the halo columns
+            const int xe = lane == 0 ? 32 * h : (lane == 31 ? 32 * h + 33 : fx);
+            float lo, mid, hi, elo, emid, ehi;
+            sort3f(fk[ya][fx], fk[yb][fx], fk[yc][fx], lo, mid, hi);
+            sort3f(fk[ya][xe], fk[yb][xe], fk[yc][xe], elo, emid, ehi);
+            float llo = __shfl_up_sync(0xffffffffu, lo, 1), lmid = __shfl_up_sync(0xffffffffu, mid, 1),
+                  lhi = __shfl_up_sync(0xffffffffu, hi, 1);
+            float rlo = __shfl_down_sync(0xffffffffu, lo, 1), rmid = __shfl_down_sync(0xffffffffu, mid, 1),
+                  rhi = __shfl_down_sync(0xffffffffu, hi, 1);
+            if (lane == 0) { llo = elo; lmid = emid; lhi = ehi; }
+            if (lane == 31) { rlo = elo; rmid = emid; rhi = ehi; }
+            if (c == 0) { llo = lo; lmid = mid; lhi = hi; }           // replicate border
+            if (c == W - 1) { rlo = lo; rmid = mid; rhi = hi; }
+            if (c < W && r < H)
+                out[static_cast<long long>(r) * W + c] =
+                    med3f(fmaxf(fmaxf(llo, lo), rlo), med3f(lmid, mid, rmid), fminf(fminf(lhi, hi), rhi));
+            continue;
+        }
+        if (r >= H || c >= W) continue;
+        int xa = fx - 1, xb = fx, xc = fx + 1;
+        if (c == 0) xa = xb;
+        if (c == W - 1) xc = xb;
+        float v;
+        if (H == 1) {
+            v = cv_median3_line(fk[yb][xa], fk[yb][xb], fk[yb][xc]);
+        } else if (W == 1) {
+            v = cv_median3_line(fk[ya][xb], fk[yb][xb], fk[yc][xb]);
+        } else {
+            const float p0 = fk[ya][xa], p1 = fk[ya][xb], p2 = fk[ya][xc], p3 = fk[yb][xa], p4 = fk[yb][xb],
+                        p5 = fk[yb][xc], p6 = fk[yc][xa], p7 = fk[yc][xb], p8 = fk[yc][xc];
+            // all nine NaN (the epilogue's own NaN): every exchange moves equal bits
+            const bool all_nan = isnan(p0) & isnan(p1) & isnan(p2) & isnan(p3) & isnan(p4) & isnan(p5) & isnan(p6) &
+                                 isnan(p7) & isnan(p8);
+            v = all_nan ? qnan : cv_median9(cv_vector_column(c, W), p0, p1, p2, p3, p4, p5, p6, p7, p8);
+        }
+        out[static_cast<long long>(r) * W + c] = v;
     }
 }
 
-// Persistent epilogue over the 32x32 tiles of many views: tiles [tile_begin, tile_end),
-// grid-strided so that the blocks sweep the key grids in order (L2 locality of the
-// halos).  Tile indices only grow, so every thread follows the view index with a forward
-// walk (one search at the start) and needs no barrier for it.
-__global__ void __launch_bounds__(TX *TY, 6) map_epilogue_kernel(
+// Pixel box [ia, ib] x [ja, jb] of the pixels whose cells can fall in rows [rlo, rhi) and
+// columns [clo, chi) of the grid: the affine pixel <- cell map at the region's corners,
+// widened by a quarter cell and by bmarg pixels (one pixel plus a bound of the FP64
+// rounding of the map), clipped to the map.  ja is rounded down to a multiple of 4 for float4 rows.
+__device__ __forceinline__ void map_pixel_box(const MapViewDev &mv, int rlo, int rhi, int clo, int chi, int &ia, int &ib,
+                                              int &ja, int &jb) {
+    if (mv.box_all) {
+        ia = 0; ib = mv.H - 1; ja = 0; jb = mv.W - 1;
+    } else {
+        const double sr[2] = {rlo - 0.25, rhi + 0.25}, sc[2] = {clo - 0.25, chi + 0.25};
+        double imin = 1e300, imax = -1e300, jmin = 1e300, jmax = -1e300;
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                const double pi = __fma_rn(mv.bir, sr[a], __fma_rn(mv.bic, sc[b], mv.bi0));
+                const double pj = __fma_rn(mv.bjr, sr[a], __fma_rn(mv.bjc, sc[b], mv.bj0));
+                imin = fmin(imin, pi); imax = fmax(imax, pi);
+                jmin = fmin(jmin, pj); jmax = fmax(jmax, pj);
+            }
+        // clamp before converting (a far-away tile maps far outside the map)
+        ia = static_cast<int>(fmin(fmax(floor(imin - mv.bmarg), 0.0), mv.H));
+        ib = static_cast<int>(fmax(fmin(ceil(imax + mv.bmarg), mv.H - 1.0), -1.0));
+        ja = static_cast<int>(fmin(fmax(floor(jmin - mv.bmarg), 0.0), mv.W));
+        jb = static_cast<int>(fmax(fmin(ceil(jmax + mv.bmarg), mv.W - 1.0), -1.0));
+        if (!(imin <= imax && jmin <= jmax)) { ia = 1; ib = 0; }    // NaN: nothing
+    }
+    if (mv.vec) ja &= ~3;      // float4 rows: groups start 16-byte aligned
+}
+
+// The batched rasterisation of many views, one fused kernel: a CTA takes work items (one
+// OW x OH tile of one view's DSM) from a device counter, bins the pixels of the tile's
+// pixel box into its shared-memory key tile, and runs the epilogue from shared memory, so
+// no key grid exists in device memory.  Items [item_begin, item_end) of the plan's item
+// list (views in order, tiles row-major within a view).
+template <int OW, int OH>
+__global__ void __launch_bounds__(kMapThreads, 4) map_tile_kernel(
     const MapViewDev *__restrict__ views, const AoiDev *__restrict__ aois, const long long *__restrict__ tile_start,
-    int v_lo, int v_hi, long long tile_begin, long long tile_end, const unsigned long long *__restrict__ keys,
-    float *__restrict__ dsm) {
-    __shared__ EpilogueSmem sm;
-    const long long t0 = tile_begin + blockIdx.x;
-    if (t0 >= tile_end) return;
-    int v = find_range(tile_start, v_lo, v_hi, t0);
-    long long next = __ldg(tile_start + v + 1);
-    for (long long t = t0; t < tile_end; t += gridDim.x) {
-        while (t >= next) next = __ldg(tile_start + (++v) + 1);
+    int v_lo, int v_hi, long long item_begin, long long item_end, float *__restrict__ dsm,
+    unsigned long long *__restrict__ counter) {
+    using S = MapTileSmem<OW, OH>;
+    __shared__ S sm;
+    for (int i = threadIdx.x; i < S::NK; i += kMapThreads) sm.keys[i] = 0u;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long it = item_begin + static_cast<long long>(atomicAdd(counter, 1ull));
+            sm.item = it;
+            sm.n_holes = 0;
+            sm.has_zero = 0;
+            if (it < item_end) {
+                const int v = find_range(tile_start, v_lo, v_hi, it);
+                const MapViewDev &mv = views[v];
+                const AoiDev &ad = aois[mv.aoi];
+                const int tiles_x = (ad.xsize + OW - 1) / OW;
+                const int local = static_cast<int>(it - __ldg(tile_start + v));
+                const int ty = local / tiles_x, tx = local - ty * tiles_x;
+                const int r0 = ty * OH, c0 = tx * OW;
+                int ia, ib, ja, jb;
+                map_pixel_box(mv, max(r0 - 2, 0), min(r0 + OH + 2, ad.ysize), max(c0 - 2, 0),
+                              min(c0 + OW + 2, ad.xsize), ia, ib, ja, jb);
+                sm.view = v; sm.r0 = r0; sm.c0 = c0;
+                sm.ia = ia; sm.ib = ib; sm.ja = ja; sm.jb = jb;
+            }
+        }
+        __syncthreads();
+        if (sm.item >= item_end) return;
+        const int v = sm.view, r0 = sm.r0, c0 = sm.c0, ia = sm.ia, ib = sm.ib, ja = sm.ja, jb = sm.jb;
+        for (int i = threadIdx.x; i < S::FH; i += kMapThreads) sm.specrow[i] = 0;
         const MapViewDev &mv = views[v];
         const AoiDev &ad = aois[mv.aoi];
-        const int W = ad.xsize, H = ad.ysize;
-        const int tiles_x = (W + TX - 1) / TX;
-        const long long local = t - __ldg(tile_start + v);
-        const int ty = static_cast<int>(local / tiles_x), tx = static_cast<int>(local - static_cast<long long>(ty) * tiles_x);
-        float *out = mv.out ? mv.out : dsm + mv.off;
-        epilogue_tile(keys + mv.off, MapZeroDecoder{}, out, nullptr, H, W, ty * TILE_Y, tx * TX, sm);
+        const FastAxis R = ad.row, C = ad.col;
+        if (ia <= ib && ja <= jb) map_tile_pass<OW, OH, false>(mv, R, C, r0 - 2, c0 - 2, ia, ib, ja, jb, sm);
         __syncthreads();
+        if (sm.has_zero) {       // rare: resolve the sign of cells whose maximum is a zero
+            for (int i = threadIdx.x; i < S::NK; i += kMapThreads) sm.u.zw[i] = 0u;
+            __syncthreads();
+            map_tile_pass<OW, OH, true>(mv, R, C, r0 - 2, c0 - 2, ia, ib, ja, jb, sm);
+            __syncthreads();
+            for (int i = threadIdx.x; i < S::NK; i += kMapThreads)
+                if (sm.keys[i] == kMapKeyZero) sm.keys[i] = (sm.u.zw[i] & 1u) ? 0x7fffffffu : kMapKeyZero;
+            __syncthreads();
+        }
+        map_tile_finish<OW, OH>(sm, mv.out ? mv.out : dsm + mv.off, ad.ysize, ad.xsize, r0, c0);
     }
 }
 
@@ -1386,14 +1612,14 @@ extern "C" int vs_median_blur3x3_f64(const double *in, float *out, int64_t h, in
 
 // ---- batched form: plan and run ------------------------------------------------------------
 struct VsAoiBatch {
-    int n_aois = 0, n_views = 0, rows_per_item = 0;
+    int n_aois = 0, n_views = 0, tile = 0;
     std::vector<VsAoi> aois;
-    std::vector<long long> view_off, fused_off, item_start, tile_start;
+    std::vector<long long> view_off, fused_off, tile_start;
     long long view_cells = 0, fused_cells = 0, max_fuse_cells = 0;
     bool all_direct = true;                // every view has its own DSM output
     vs::MapViewDev *d_views = nullptr;
     vs::AoiDev *d_aois = nullptr;
-    long long *d_item_start = nullptr, *d_tile_start = nullptr;
+    long long *d_tile_start = nullptr;
     unsigned long long *d_counter = nullptr;
     std::vector<vs::MapViewDev> h_views;   // host copies, alive while their upload runs
     std::vector<vs::AoiDev> h_aois;
@@ -1405,7 +1631,7 @@ namespace {
 struct PlanLayout {
     MapViewDev *views;
     AoiDev *aois;
-    long long *item_start, *tile_start;
+    long long *tile_start;
     unsigned long long *counter;
     long long *thr;
     size_t bytes;
@@ -1416,7 +1642,6 @@ PlanLayout carve_plan(void *ws, const VsAoi *aois, int n_aois, int n_views) {
     PlanLayout p;
     p.views = cv.take<MapViewDev>(n_views);
     p.aois = cv.take<AoiDev>(n_aois);
-    p.item_start = cv.take<long long>(n_views + 1);
     p.tile_start = cv.take<long long>(n_views + 1);
     p.counter = cv.take<unsigned long long>(2);
     size_t thr = 0;
@@ -1452,11 +1677,11 @@ extern "C" size_t vs_aoi_batch_plan_workspace_size(const VsAoi *aois, int n_aois
 }
 
 extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView *views, int n_views,
-                                 int rows_per_item, void *workspace, size_t workspace_bytes, VsAoiBatch **plan,
+                                 int tile, void *workspace, size_t workspace_bytes, VsAoiBatch **plan,
                                  void *stream) {
     VS_REQUIRE(aois && views && plan && workspace && n_aois > 0 && n_views > 0 && n_views < (1 << 30) &&
-                   rows_per_item > 0 && rows_per_item <= 65536,
-               "vs_aoi_batch_plan: bad arguments");
+                   (tile == 32 || tile == 64),
+               "vs_aoi_batch_plan: bad arguments (tile must be 32 or 64)");
     *plan = nullptr;
     const size_t need = vs_aoi_batch_plan_workspace_size(aois, n_aois, n_views);
     VS_REQUIRE(need > 0, "vs_aoi_batch_plan: empty grid");
@@ -1469,12 +1694,11 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
     VsAoiBatch *p = new VsAoiBatch();
     p->n_aois = n_aois;
     p->n_views = n_views;
-    p->rows_per_item = rows_per_item;
+    p->tile = tile;
     p->aois.assign(aois, aois + n_aois);
     p->h_aois.resize(n_aois);
     p->h_views.resize(n_views);
     p->view_off.resize(n_views + 1);
-    p->item_start.resize(n_views + 1);
     p->tile_start.resize(n_views + 1);
     p->fused_off.resize(n_aois + 1);
     auto fail = [&](int code) {
@@ -1482,6 +1706,7 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
         return code;
     };
     long long *thr = L.thr;
+    std::vector<double> sig_c(n_aois), sig_r(n_aois);   // cell coordinate per ulp of difference
     p->fused_off[0] = 0;
     int expect_view = 0;
     for (int a = 0; a < n_aois; ++a) {
@@ -1530,6 +1755,8 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
         }
         ad.shx = 24 - ex;
         ad.shy = 24 - ey;
+        sig_c[a] = ldexp(1.0, ex - 52) / A.yres;    // columns divide by yres, rows by xres
+        sig_r[a] = ldexp(1.0, ey - 52) / A.xres;    // (lib/proj_to_grid.py's own pairing)
         ad.bx = (static_cast<long long>(ex + 1023) << 52) - (1LL << 52);
         ad.by = (static_cast<long long>(ey + 1023) << 52) - (1LL << 52);
         ad.xsize = static_cast<int>(A.xsize);
@@ -1542,7 +1769,7 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
         set_error("vs_aoi_batch_plan: the AOIs cover %d views, %d given", expect_view, n_views);
         return fail(VS_ERR_ARG);
     }
-    p->view_off[0] = p->item_start[0] = p->tile_start[0] = 0;
+    p->view_off[0] = p->tile_start[0] = 0;
     for (int v = 0; v < n_views; ++v) {
         const VsMapView &V = views[v];
         const bool aoi_ok = V.aoi >= 0 && V.aoi < n_aois && v >= aois[V.aoi].first_view &&
@@ -1584,24 +1811,44 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
             d.dr_di = -(static_cast<long long>(V.ni) << ad.shy);
             d.dr_dj = -(static_cast<long long>(V.nj) << ad.shy);
         }
+        // pixel <- cell map for the tiles' pixel boxes: (s_col, s_row) = sig * (d_col, d_row)
+        // with d = d0 + M (u, w), u = 2i+1-H, w = 2j+1-W; inverted in FP64, with a margin for
+        // its rounding; a singular (or numerically hopeless) map reads the whole map per tile
+        {
+            const double a = static_cast<double>(d.dc_di), b = static_cast<double>(d.dc_dj);
+            const double c = static_cast<double>(d.dr_di), e = static_cast<double>(d.dr_dj);
+            const double dc0 = static_cast<double>(d.dc0), dr0 = static_cast<double>(d.dr0);
+            const double det = a * e - b * c;
+            const double sc = sig_c[V.aoi], sr = sig_r[V.aoi];
+            d.bic = e / (sc * det) * 0.5;
+            d.bir = -b / (sr * det) * 0.5;
+            d.bi0 = ((b * dr0 - e * dc0) / det + (V.height - 1)) * 0.5;
+            d.bjc = -c / (sc * det) * 0.5;
+            d.bjr = a / (sr * det) * 0.5;
+            d.bj0 = ((c * dc0 - a * dr0) / det + (V.width - 1)) * 0.5;
+            const double span = fabs(d.bic) * (static_cast<double>(aois[V.aoi].xsize) + 4.0) + fabs(d.bir) * (static_cast<double>(aois[V.aoi].ysize) + 4.0) +
+                                fabs(d.bjc) * (static_cast<double>(aois[V.aoi].xsize) + 4.0) + fabs(d.bjr) * (static_cast<double>(aois[V.aoi].ysize) + 4.0);
+            const double big = (fabs(e * dc0) + fabs(b * dr0) + fabs(c * dc0) + fabs(a * dr0)) / fabs(det);
+            d.bmarg = 1.0 + 1e-12 * (big + span + fabs(d.bi0) + fabs(d.bj0));
+            const bool finite = std::isfinite(d.bic) && std::isfinite(d.bir) && std::isfinite(d.bi0) &&
+                                std::isfinite(d.bjc) && std::isfinite(d.bjr) && std::isfinite(d.bj0) &&
+                                std::isfinite(d.bmarg);
+            d.box_all = !(det != 0.0 && finite && d.bmarg < 64.0);
+        }
         if (!V.dsm) p->all_direct = false;
         const VsAoi &A = aois[V.aoi];
         const long long cells = A.xsize * A.ysize;
         p->view_off[v + 1] = p->view_off[v] + cells;
-        p->item_start[v + 1] = p->item_start[v] + ceil_div(V.height, rows_per_item);
-        p->tile_start[v + 1] = p->tile_start[v] + ceil_div(A.xsize, TX) * ceil_div(A.ysize, TILE_Y);
+        p->tile_start[v + 1] = p->tile_start[v] + ceil_div(A.xsize, tile) * ceil_div(A.ysize, tile);
     }
     p->view_cells = p->view_off[n_views];
     p->fused_cells = p->fused_off[n_aois];
     p->d_views = L.views;
     p->d_aois = L.aois;
-    p->d_item_start = L.item_start;
     p->d_tile_start = L.tile_start;
     p->d_counter = L.counter;
     bool ok = cudaMemcpyAsync(L.views, p->h_views.data(), sizeof(MapViewDev) * n_views, cudaMemcpyHostToDevice, st) == cudaSuccess;
     ok = ok && cudaMemcpyAsync(L.aois, p->h_aois.data(), sizeof(AoiDev) * n_aois, cudaMemcpyHostToDevice, st) == cudaSuccess;
-    ok = ok && cudaMemcpyAsync(L.item_start, p->item_start.data(), sizeof(long long) * (n_views + 1),
-                               cudaMemcpyHostToDevice, st) == cudaSuccess;
     ok = ok && cudaMemcpyAsync(L.tile_start, p->tile_start.data(), sizeof(long long) * (n_views + 1),
                                cudaMemcpyHostToDevice, st) == cudaSuccess;
     ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
@@ -1618,57 +1865,48 @@ extern "C" int vs_aoi_batch_query(const VsAoiBatch *plan, int64_t *view_cells, i
     VS_REQUIRE(plan, "vs_aoi_batch_query: null plan");
     if (view_cells) *view_cells = plan->view_cells;
     if (fused_cells) *fused_cells = plan->fused_cells;
-    if (scratch_bytes) {
-        const size_t keys = sizeof(unsigned long long) * static_cast<size_t>(plan->view_cells);
-        const size_t fuse = vs_fuse_dsms_workspace_size(1, plan->max_fuse_cells);
-        *scratch_bytes = std::max(keys, fuse) + 256;
-    }
+    if (scratch_bytes) *scratch_bytes = vs_fuse_dsms_workspace_size(1, plan->max_fuse_cells) + 256;
     return VS_OK;
 }
 
-extern "C" int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int bin_blocks_per_sm,
-                                void *scratch, size_t scratch_bytes, float *view_dsm, void *stream) {
-    VS_REQUIRE(plan && scratch && (view_dsm || plan->all_direct), "vs_aoi_batch_run: null pointer");
-    VS_REQUIRE(0 <= view_begin && view_begin < view_end && view_end <= plan->n_views && bin_blocks_per_sm > 0 &&
-                   bin_blocks_per_sm <= 64,
-               "vs_aoi_batch_run: bad view range [%d, %d) or blocks per SM %d", view_begin, view_end, bin_blocks_per_sm);
-    size_t need = 0;
-    vs_aoi_batch_query(plan, nullptr, nullptr, &need);
-    if (scratch_bytes < need) {
-        set_error("vs_aoi_batch_run: scratch %zu < %zu bytes", scratch_bytes, need);
-        return VS_ERR_WORKSPACE;
+namespace vs {
+namespace {
+
+template <int T>
+int launch_map_tiles(const VsAoiBatch *plan, int view_begin, int view_end, int blocks_per_sm, float *view_dsm,
+                     cudaStream_t st) {
+    static int resident = 0;       // CTAs per SM the kernel fits (registers, shared memory)
+    if (!resident) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, map_tile_kernel<T, T>, kMapThreads, 0) !=
+                cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 1;
+        resident = per_sm;
     }
+    const long long t0 = plan->tile_start[view_begin], t1 = plan->tile_start[view_end];
+    const long long blocks = std::min<long long>(t1 - t0, 1LL * sm_count() * std::min(blocks_per_sm, resident));
+    map_tile_kernel<T, T><<<static_cast<unsigned>(blocks), kMapThreads, 0, st>>>(
+        plan->d_views, plan->d_aois, plan->d_tile_start, view_begin, view_end - 1, t0, t1, view_dsm, plan->d_counter);
+    return check_launch("map_tile_kernel");
+}
+
+}  // namespace
+}  // namespace vs
+
+extern "C" int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int blocks_per_sm,
+                                float *view_dsm, void *stream) {
+    VS_REQUIRE(plan && (view_dsm || plan->all_direct), "vs_aoi_batch_run: null pointer");
+    VS_REQUIRE(0 <= view_begin && view_begin < view_end && view_end <= plan->n_views && blocks_per_sm > 0 &&
+                   blocks_per_sm <= 64,
+               "vs_aoi_batch_run: bad view range [%d, %d) or blocks per SM %d", view_begin, view_end, blocks_per_sm);
     cudaStream_t st = as_stream(stream);
-    unsigned long long *keys = static_cast<unsigned long long *>(scratch);
-    const long long c0 = plan->view_off[view_begin], c1 = plan->view_off[view_end];
-    if (cudaMemsetAsync(keys + c0, 0, sizeof(unsigned long long) * (c1 - c0), st) != cudaSuccess ||
-        cudaMemsetAsync(plan->d_counter, 0, sizeof(unsigned long long), st) != cudaSuccess) {
+    if (cudaMemsetAsync(plan->d_counter, 0, sizeof(unsigned long long), st) != cudaSuccess) {
         set_error("vs_aoi_batch_run: cudaMemsetAsync failed");
         return VS_ERR_CUDA;
     }
-    const long long i0 = plan->item_start[view_begin], i1 = plan->item_start[view_end];
-    if (i1 > i0) {
-        const long long blocks = std::min<long long>(i1 - i0, 1LL * sm_count() * bin_blocks_per_sm);
-        map_bin_kernel<<<static_cast<unsigned>(blocks), kMapThreads, 0, st>>>(
-            plan->d_views, plan->d_aois, plan->d_item_start, view_begin, view_end - 1, i0, i1, plan->rows_per_item, keys,
-            plan->d_counter);
-        VS_LAUNCH_CHECK("map_bin_kernel");
-    }
-    const long long t0 = plan->tile_start[view_begin], t1 = plan->tile_start[view_end];
-    // one resident wave of the persistent epilogue
-    static int epi_resident = 0;
-    if (!epi_resident) {
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, map_epilogue_kernel, TX * TY, 0) != cudaSuccess ||
-            per_sm <= 0)
-            per_sm = 4;
-        epi_resident = per_sm;
-    }
-    const long long eblocks = std::min<long long>(t1 - t0, 1LL * sm_count() * epi_resident);
-    map_epilogue_kernel<<<static_cast<unsigned>(eblocks), dim3(TX, TY), 0, st>>>(
-        plan->d_views, plan->d_aois, plan->d_tile_start, view_begin, view_end - 1, t0, t1, keys, view_dsm);
-    VS_LAUNCH_CHECK("map_epilogue_kernel");
-    return VS_OK;
+    return plan->tile == 64 ? launch_map_tiles<64>(plan, view_begin, view_end, blocks_per_sm, view_dsm, st)
+                            : launch_map_tiles<32>(plan, view_begin, view_end, blocks_per_sm, view_dsm, st);
 }
 
 extern "C" int vs_aoi_batch_fuse(const VsAoiBatch *plan, int aoi_begin, int aoi_end, const float *view_dsm,

@@ -5,11 +5,11 @@ An ``AoiSetEngine`` owns the device data of a set of AOIs (per-view FP32 height 
 windows of a resident map pool, fixed-point pixel -> UTM maps, DSM grids) and runs the
 reference's per-AOI chain -- per-view DSMs (produce_dsm.py:46-58) and their fusion
 (aggregate_2p5d.py:65-81) -- for all of them.  AOIs are grouped into consecutive waves
-whose per-view DSMs and key grids (12 bytes per cell-view) fit ``budget_bytes``; each wave
-is one ``AoiBatch`` plan.  ``step('batched')`` issues per wave one binning launch and one
-epilogue launch over all its views, then the per-AOI fusions; ``step('per_view')`` issues
-the same kernels one view at a time (the per-view form).  Fused DSMs of all AOIs land in
-one resident buffer.
+whose per-view DSMs (4 bytes per cell-view) fit ``budget_bytes``; each wave is one
+``AoiBatch`` plan.  ``step('batched')`` issues per wave one rasterisation launch over all
+its views' DSM tiles, then the per-AOI fusions; ``step('per_view')`` issues the same kernel
+one view at a time (the per-view form).  Fused DSMs of all AOIs land in one resident
+buffer.
 """
 import torch
 
@@ -17,7 +17,7 @@ from .batch import AoiBatch, AoiGrid, MapAffine, MapView
 
 
 class AoiSetEngine:
-    def __init__(self, specs, pool, affines, budget_bytes=96 << 30, rows_per_item=8, bin_blocks_per_sm=4):
+    def __init__(self, specs, pool, affines, budget_bytes=96 << 30, tile=64, blocks_per_sm=4):
         """specs: AOI specs (``synth.AoiSpec``); pool: (P, S, S) CUDA float32 map pool (view
         k of the set reads pool map k % P, window [:image, :image]); affines: per AOI, the
         per-view fixed-point maps (dicts)."""
@@ -25,8 +25,8 @@ class AoiSetEngine:
         self.pool = pool
         self.affines = affines
         self.budget = int(budget_bytes)
-        self.rows_per_item = int(rows_per_item)
-        self.bin_blocks_per_sm = int(bin_blocks_per_sm)
+        self.tile = int(tile)
+        self.blocks_per_sm = int(blocks_per_sm)
         self._build()
 
     # ---- plans ------------------------------------------------------------------------
@@ -44,7 +44,7 @@ class AoiSetEngine:
         cur, cur_bytes, k = [], 0, 0
         groups = []
         for a, s in enumerate(self.specs):
-            need = 12 * s.cells * s.n_views
+            need = 4 * s.cells * s.n_views
             if cur and cur_bytes + need > self.budget:
                 groups.append(cur)
                 cur, cur_bytes = [], 0
@@ -57,7 +57,7 @@ class AoiSetEngine:
             grids = [AoiGrid(self.specs[a].xoff, self.specs[a].yoff, self.specs[a].res, self.specs[a].res,
                              self.specs[a].xsize, self.specs[a].ysize) for a, _ in g]
             views = [self._views_of(a, k0) for a, k0 in g]
-            self.waves.append(AoiBatch(grids, views, rows_per_item=self.rows_per_item))
+            self.waves.append(AoiBatch(grids, views, tile=self.tile))
             self.wave_aois.append([a for a, _ in g])
         self.view_dsm = torch.empty(max(w.view_cells for w in self.waves), dtype=torch.float32, device='cuda')
         self.scratch = torch.empty(max(w.scratch_bytes for w in self.waves), dtype=torch.uint8, device='cuda')
@@ -81,10 +81,10 @@ class AoiSetEngine:
         w = self.waves[i]
         fused = self.fused[self.fused_off[i]:self.fused_off[i + 1]]
         if mode == 'batched':
-            w.run(self.view_dsm, self.scratch, bin_blocks_per_sm=self.bin_blocks_per_sm)
+            w.run(self.view_dsm, blocks_per_sm=self.blocks_per_sm)
         else:
             for v in range(w.n_views):
-                w.run(self.view_dsm, self.scratch, views=(v, v + 1), bin_blocks_per_sm=self.bin_blocks_per_sm)
+                w.run(self.view_dsm, views=(v, v + 1), blocks_per_sm=self.blocks_per_sm)
         w.fuse(self.view_dsm, fused, self.scratch)
 
     def step(self, mode='batched'):
@@ -130,31 +130,32 @@ class AoiSetEngine:
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 1e3 / reps
 
-    def autotune(self, rows=(4, 8, 16, 32), blocks=(2, 4, 8), wave=0):
-        """Pick rows_per_item and bin CTAs per SM by timing the batched rasterisation of one
-        wave for every pair; re-plans all waves with the winner.  Returns the timings."""
+    def autotune(self, tiles=(32, 64), blocks=(2, 3, 4, 6, 8), wave=0):
+        """Pick the DSM tile edge and the CTAs per SM (capped by what fits) by timing the
+        batched rasterisation of one wave for every pair; re-plans all waves with the winner.
+        Returns the timings."""
         w0 = self.waves[wave]
         grids = w0.grids
         views = w0.views
         timings = {}
-        for r in rows:
-            b = AoiBatch(grids, views, rows_per_item=r)
+        for t in tiles:
+            b = AoiBatch(grids, views, tile=t)
             for bl in blocks:
-                b.run(self.view_dsm, self.scratch, bin_blocks_per_sm=bl)       # warm
+                b.run(self.view_dsm, blocks_per_sm=bl)       # warm
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 torch.cuda.synchronize()
                 e0.record()
-                b.run(self.view_dsm, self.scratch, bin_blocks_per_sm=bl)
+                b.run(self.view_dsm, blocks_per_sm=bl)
                 e1.record()
                 torch.cuda.synchronize()
-                timings[(r, bl)] = e0.elapsed_time(e1) / 1e3
+                timings[(t, bl)] = e0.elapsed_time(e1) / 1e3
             b.close()
-        (r, bl) = min(timings, key=timings.get)
-        if r != self.rows_per_item or bl != self.bin_blocks_per_sm:
+        (t, bl) = min(timings, key=timings.get)
+        if t != self.tile or bl != self.blocks_per_sm:
             self.close()
-            self.rows_per_item, self.bin_blocks_per_sm = r, bl
+            self.tile, self.blocks_per_sm = t, bl
             self._build()
-        return {f'rows{k[0]}_blocks{k[1]}': round(v * 1e3, 3) for k, v in timings.items()}
+        return {f'tile{k[0]}_blocks{k[1]}': round(v * 1e3, 3) for k, v in timings.items()}
 
 
 class AoiCameraFits:

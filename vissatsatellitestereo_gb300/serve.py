@@ -128,8 +128,8 @@ class _InFlight:
 
 
 class FusionServer:
-    def __init__(self, specs, view_source, metas=None, budget_bytes=150 << 30, max_batch=64, rows_per_item=32,
-                 bin_blocks_per_sm=8, scratch_cap_bytes=16 << 30, fit_grid=(200, 20), slots=3):
+    def __init__(self, specs, view_source, metas=None, budget_bytes=150 << 30, max_batch=64, tile=64,
+                 blocks_per_sm=4, fit_grid=(200, 20), slots=3):
         """specs: the AOI catalog (``synth.AoiSpec``: grid and view count); view_source(a):
         the AOI's views as (CUDA float32 heights, width, height, fixed-point affine dict);
         metas: per AOI the views' RPC meta_dicts (None: no camera fits); slots: batches that
@@ -139,13 +139,11 @@ class FusionServer:
         self.metas = metas
         self.store = ResidentStore(budget_bytes)
         self.max_batch = int(max_batch)
-        self.rows_per_item = rows_per_item
-        self.bin_blocks_per_sm = bin_blocks_per_sm
-        self.scratch_cap = int(scratch_cap_bytes)
+        self.tile = tile
+        self.blocks_per_sm = blocks_per_sm
         self.fit_grid = fit_grid
         self.slots = max(1, int(slots))
         self.streams = [torch.cuda.Stream() for _ in range(self.slots)]
-        self.scratch = {}             # stream -> rasterisation scratch
         self.inflight = []
         self.max_inflight = 0
         self.pixels = 0               # height-map pixels rasterised
@@ -162,13 +160,8 @@ class FusionServer:
     def _rasterise(self, aois, stacks):
         grids = [AoiGrid(self.specs[a].xoff, self.specs[a].yoff, self.specs[a].res, self.specs[a].res,
                          self.specs[a].xsize, self.specs[a].ysize) for a in aois]
-        plan = AoiBatch(grids, [self._views(a, stacks[a]) for a in aois], rows_per_item=self.rows_per_item)
-        st = torch.cuda.current_stream()
-        scratch = self.scratch.get(st)
-        if scratch is None or scratch.numel() < plan.scratch_bytes:
-            scratch = torch.empty(plan.scratch_bytes, dtype=torch.uint8, device='cuda')
-            self.scratch[st] = scratch
-        plan.run(None, scratch, bin_blocks_per_sm=self.bin_blocks_per_sm)
+        plan = AoiBatch(grids, [self._views(a, stacks[a]) for a in aois], tile=self.tile)
+        plan.run(None, blocks_per_sm=self.blocks_per_sm)
         self.pixels += plan.pixels
         self.cell_views += plan.view_cells
         return plan
@@ -183,27 +176,20 @@ class FusionServer:
         return params, err, status
 
     def _materialise(self, misses, pinned):
-        """Admit, rasterise and fit the missing AOIs on the current stream (rasterisation
-        batched in groups whose key-grid scratch stays under the cap).  Returns the plans,
+        """Admit, rasterise (all missing AOIs' views in one launch, straight into their
+        resident stacks) and fit the missing AOIs on the current stream.  Returns the plans,
         which must outlive the work."""
-        stacks, group, group_bytes, plans, states = {}, [], 0, [], []
+        stacks, plans, states = {}, [], []
         for a in misses:
             s = self.specs[a]
             self.store.admit(state_bytes(s), pinned)
             stack = torch.empty((s.n_views, s.ysize, s.xsize), dtype=torch.float32, device='cuda')
             stacks[a] = stack
-            need = 8 * s.cells * s.n_views
-            if group and group_bytes + need > self.scratch_cap:
-                plans.append(self._rasterise(group, stacks))
-                group, group_bytes = [], 0
-            group.append(a)
-            group_bytes += need
             cams = self._fit(a) if self.metas is not None else None
             state = {'stack': stack, 'cameras': cams, 'stream': torch.cuda.current_stream(), 'ready': None}
             states.append(state)
             self.store.put(a, state, state_bytes(s))
-        if group:
-            plans.append(self._rasterise(group, stacks))
+        plans.append(self._rasterise(misses, stacks))
         ready = torch.cuda.Event()
         ready.record()
         for st in states:
