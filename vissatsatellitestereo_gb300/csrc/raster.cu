@@ -926,7 +926,6 @@ struct MapTileSmem {
             unsigned short holes[NF];       // empty in-grid cells of the blur input
         } e;
     } u;
-    long long tcol[KW + 1], trow[KH + 1];   // thresholds of the key tile's columns and rows
     long long item;
     int view, r0, c0, ia, ib, ja, jb;
     int n_holes, has_zero;
@@ -954,54 +953,16 @@ __device__ __forceinline__ bool axis_tile(const FastAxis &a, long long d, int &r
 // integer/FP32 axis test and the threshold correction); pixels whose cell lies outside
 // the key tile are dropped.  ZERO = false: the nanmax keys, zeros as kMapKeyZero;
 // ZERO = true: for cells whose maximum is a zero, the first zero pixel and its sign.
-// Exact local index of difference d on one axis of the key tile: the cell from the FP32
-// estimate (corrected against the thresholds when not sure), -1 / the grid size for
-// differences below / beyond the grid, then relative to the tile's first cell `base`
-// and clamped to [-1, span] (-1: before the tile, span: after it).
-__device__ __forceinline__ int tile_local(const FastAxis &a, long long d, int base, int span) {
-    int r;
-    bool sure;
-    const bool ok = axis_tile(a, d, r, sure);
-    if (ok && !sure) r = axis_correct(a.thr, min(max(r, 0), a.nm1), d);
-    if (!ok) r = d < 0 ? -1 : a.nm1 + 1;
-    return min(max(r - base, -1), span);
-}
-
-// One step of the walk along a row of pixels: d moved by a step of known sign; the local
-// index l keeps t[l] <= d < t[l + 1] (t[-1] = -inf, t[span + 1] = +inf), so that it is the
-// exact cell as long as it lies inside the tile.
-__device__ __forceinline__ void tile_walk(const long long *t, long long d, bool up, int span, int &l) {
-    if (up) {
-        while (l < span && d >= t[l + 1]) ++l;
-    } else {
-        while (l >= 0 && d < t[l]) --l;
-    }
-}
-
-// One pass over the item's pixel box [ia, ib] x [ja, jb] (ja a multiple of 4 for float4
-// rows).  A thread takes kMapUnitPx consecutive pixels of a box row: the first pixel's
-// cell comes from the FP32 estimate and the threshold correction (exactly as the
-// per-view path bins its FP64 point), the next ones walk the tile's threshold tables in
-// shared memory -- along a row the differences move by a constant step, so the cell
-// changes only when a threshold is crossed -- and runs of pixels in one cell merge
-// before their shared-memory atomicMax.  Pixels whose cell lies outside the grid or the
-// key tile are dropped.  ZERO = false: the nanmax keys, zeros as kMapKeyZero; ZERO = true:
-// for cells whose maximum is a zero, the first zero pixel and its sign.
 template <int OW, int OH, bool ZERO>
 __device__ __forceinline__ void map_tile_pass(const MapViewDev &mv, const FastAxis &R, const FastAxis &C, int rbase,
                                               int cbase, int ia, int ib, int ja, int jb, MapTileSmem<OW, OH> &sm) {
     using S = MapTileSmem<OW, OH>;
     constexpr int P = kMapUnitPx;
-    const int G = (jb - ja) / P + 1;                    // P-pixel units per box row
+    const int G = (jb - ja) / P + 1;                    // P-pixel groups per box row
     const int units = (ib - ia + 1) * G;
     int row = threadIdx.x / G, g = threadIdx.x - row * G;
     const int rstep = kMapThreads / G, gstep = kMapThreads - rstep * G;
     const long long scol = 2 * mv.dc_dj, srow = 2 * mv.dr_dj;   // per pixel along a row
-    const bool col_up = scol >= 0, row_up = srow >= 0;
-    // local cells that are grid cells: [lc_lo, lc_hi) x [lr_lo, lr_hi)
-    const int lc_lo = max(0, -cbase), lc_hi = min(S::KW, C.nm1 + 1 - cbase);
-    const int lr_lo = max(0, -rbase), lr_hi = min(S::KH, R.nm1 + 1 - rbase);
-    const unsigned lc_n = static_cast<unsigned>(lc_hi - lc_lo), lr_n = static_cast<unsigned>(lr_hi - lr_lo);
     bool zero_seen = false;
     for (int unit = threadIdx.x; unit < units; unit += kMapThreads) {
         const int i = ia + row, j0 = ja + g * P;
@@ -1021,44 +982,56 @@ __device__ __forceinline__ void map_tile_pass(const MapViewDev &mv, const FastAx
         const int di2 = 2 * i + 1 - mv.H, dj0 = 2 * j0 + 1 - mv.W;
         long long dcol = mv.dc0 + mv.dc_di * di2 + mv.dc_dj * dj0;
         long long drow = mv.dr0 + mv.dr_di * di2 + mv.dr_dj * dj0;
-        int lc = tile_local(C, dcol, cbase, S::KW), lr = tile_local(R, drow, rbase, S::KH);
-        int run = -1;                                  // cell of the open run (-1: none)
-        unsigned run_key = 0u;
+        // rows: d is affine along the unit, and the exact row monotone in d, so when the
+        // first and the last pixel fall in the same row with sure estimates, all do
+        int ra, rb;
+        bool sa, sb;
+        const bool oka = axis_tile(R, drow, ra, sa), okb = axis_tile(R, drow + (P - 1) * srow, rb, sb);
+        const bool row_fixed = oka & okb & sa & sb & (ra == rb);
+        const unsigned lr_fixed = static_cast<unsigned>(ra - rbase);
+        int cell[P];
+        unsigned key[P];
 #pragma unroll
-        for (int k = 0; k < P; ++k) {
-            if (k > 0) {
-                dcol += scol;
-                drow += srow;
-                tile_walk(sm.tcol, dcol, col_up, S::KW, lc);
-                tile_walk(sm.trow, drow, row_up, S::KH, lr);
-            }
+        for (int k = 0; k < P; ++k, dcol += scol, drow += srow) {
             const unsigned mag = hb[k] & 0x7fffffffu;
-            const bool ok = (ZERO ? mag == 0u : mag <= 0x7f800000u) &&                 // not NaN
-                            static_cast<unsigned>(lc - lc_lo) < lc_n && static_cast<unsigned>(lr - lr_lo) < lr_n;
-            if (!ok) continue;
-            const int cell = lr * S::KW + lc;
-            unsigned key;
+            int c;
+            bool sc;
+            bool ok = ZERO ? mag == 0u : mag <= 0x7f800000u;    // not NaN
+            unsigned lr = lr_fixed;
+            if (!row_fixed) {
+                int r;
+                bool sr;
+                ok &= axis_tile(R, drow, r, sr);
+                if (ok && !sr) r = axis_correct(R.thr, min(max(r, 0), R.nm1), drow);
+                lr = static_cast<unsigned>(r - rbase);
+            }
+            ok &= axis_tile(C, dcol, c, sc);
+            if (ok && !sc) c = axis_correct(C.thr, min(max(c, 0), C.nm1), dcol);
+            const unsigned lc = static_cast<unsigned>(c - cbase);
+            ok &= (lr < static_cast<unsigned>(S::KH)) & (lc < static_cast<unsigned>(S::KW));
+            cell[k] = ok ? static_cast<int>(lr) * S::KW + static_cast<int>(lc) : -1;
             if (ZERO) {
                 const unsigned idx = static_cast<unsigned>(i) * static_cast<unsigned>(mv.W) + static_cast<unsigned>(j0 + k);
-                key = ((static_cast<unsigned>(kMapIdxLimit) - 1u - idx) << 1) | (hb[k] >> 31);
+                key[k] = ((static_cast<unsigned>(kMapIdxLimit) - 1u - idx) << 1) | (hb[k] >> 31);
             } else {
-                zero_seen |= mag == 0u;
-                key = mag == 0u ? kMapKeyZero : ((hb[k] >> 31) ? ~hb[k] : (hb[k] | 0x80000000u));
-            }
-            if (cell == run) {
-                run_key = max(run_key, key);
-            } else {
-                if (run >= 0) {
-                    if (!ZERO) atomicMax(&sm.keys[run], run_key);
-                    else if (sm.keys[run] == kMapKeyZero) atomicMax(&sm.u.zw[run], run_key);
-                }
-                run = cell;
-                run_key = key;
+                zero_seen |= ok & (mag == 0u);
+                key[k] = mag == 0u ? kMapKeyZero : ((hb[k] >> 31) ? ~hb[k] : (hb[k] | 0x80000000u));
             }
         }
-        if (run >= 0) {
-            if (!ZERO) atomicMax(&sm.keys[run], run_key);
-            else if (sm.keys[run] == kMapKeyZero) atomicMax(&sm.u.zw[run], run_key);
+        if (ZERO) {
+#pragma unroll
+            for (int k = 0; k < P; ++k)
+                if (cell[k] >= 0 && sm.keys[cell[k]] == kMapKeyZero) atomicMax(&sm.u.zw[cell[k]], key[k]);
+        } else {
+#pragma unroll
+            for (int k = 1; k < P; ++k) {     // merge runs of consecutive pixels in one cell
+                const bool same = (cell[k] >= 0) & (cell[k] == cell[k - 1]);
+                key[k] = same ? max(key[k], key[k - 1]) : key[k];
+                cell[k - 1] = same ? -1 : cell[k - 1];
+            }
+#pragma unroll
+            for (int k = 0; k < P; ++k)
+                if (cell[k] >= 0) atomicMax(&sm.keys[cell[k]], key[k]);
         }
         g += gstep;
         row += rstep;
@@ -1282,16 +1255,6 @@ __global__ void __launch_bounds__(kMapThreads, 4) map_tile_kernel(
         const MapViewDev &mv = views[v];
         const AoiDev &ad = aois[mv.aoi];
         const FastAxis R = ad.row, C = ad.col;
-        // the thresholds of the key tile's columns and rows (-inf / +inf outside the grid)
-        for (int m = threadIdx.x; m < S::KW + 1 + S::KH + 1; m += kMapThreads) {
-            const bool col = m <= S::KW;
-            const FastAxis &A = col ? C : R;
-            const int gi = col ? c0 - 2 + m : r0 - 2 + (m - S::KW - 1);
-            const long long t = gi < 0 ? LLONG_MIN : (gi > A.nm1 + 1 ? LLONG_MAX : __ldg(A.thr + gi));
-            if (col) sm.tcol[m] = t;
-            else sm.trow[m - S::KW - 1] = t;
-        }
-        __syncthreads();
         if (ia <= ib && ja <= jb) map_tile_pass<OW, OH, false>(mv, R, C, r0 - 2, c0 - 2, ia, ib, ja, jb, sm);
         __syncthreads();
         if (sm.has_zero) {       // rare: resolve the sign of cells whose maximum is a zero
