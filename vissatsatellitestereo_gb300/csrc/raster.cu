@@ -1227,6 +1227,7 @@ __global__ void __launch_bounds__(kMapThreads, 4) map_tile_kernel(
     using S = MapTileSmem<OW, OH>;
     __shared__ S sm;
     for (int i = threadIdx.x; i < S::NK; i += kMapThreads) sm.keys[i] = 0u;
+    int vlast = v_lo;      // thread 0: the view of this CTA's previous item (items only grow)
     for (;;) {
         if (threadIdx.x == 0) {
             const long long it = item_begin + static_cast<long long>(atomicAdd(counter, 1ull));
@@ -1234,7 +1235,10 @@ __global__ void __launch_bounds__(kMapThreads, 4) map_tile_kernel(
             sm.n_holes = 0;
             sm.has_zero = 0;
             if (it < item_end) {
-                const int v = find_range(tile_start, v_lo, v_hi, it);
+                int v = vlast;
+                for (int step = 0; step < 8 && v < v_hi && __ldg(tile_start + v + 1) <= it; ++step) ++v;
+                if (v < v_hi && __ldg(tile_start + v + 1) <= it) v = find_range(tile_start, v, v_hi, it);
+                vlast = v;
                 const MapViewDev &mv = views[v];
                 const AoiDev &ad = aois[mv.aoi];
                 const int tiles_x = (ad.xsize + OW - 1) / OW;
