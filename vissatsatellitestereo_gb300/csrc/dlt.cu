@@ -228,9 +228,10 @@ __device__ __forceinline__ void store_block_moments(float (&m)[kMom], float coun
 
 // Normalised coordinates of one kept point from FP64 ENU and double-float pixels (FP32 is
 // enough here: the rounding acts like data noise of ~1e-4 px that the fit averages out).
-__device__ __forceinline__ void normalised_point(const NormF &nf, double X, double Y, double Z, df c, df r,
+__device__ __forceinline__ void normalised_point(const NormF &nf, long long X, long long Y, long long Z, df c, df r,
                                                  float &px, float &py, float &pz, float &pc, float &pr) {
-    const df x = split_double(X), y = split_double(Y), z = split_double(Z);
+    const df x = split_double(__longlong_as_double(X)), y = split_double(__longlong_as_double(Y)),
+             z = split_double(__longlong_as_double(Z));
     px = ((x.hi - nf.cx.hi) + (x.lo - nf.cx.lo)) * nf.inv_s.hi;
     py = ((y.hi - nf.cy.hi) + (y.lo - nf.cy.lo)) * nf.inv_s.hi;
     pz = ((z.hi - nf.cz.hi) + (z.lo - nf.cz.lo)) * nf.inv_s.hi;
@@ -260,19 +261,21 @@ __global__ void __launch_bounds__(kMomThreads, 6) moments_kernel(
     constexpr int kAhead = 2;
 #pragma unroll 1
     for (int j0 = 0; j0 < kChunk; j0 += kAhead) {
-        double X[kAhead], Y[kAhead], Z[kAhead];
+        // coordinates as raw 64-bit patterns: double-typed registers would be moved and
+        // selected by FP64 instructions, which GB300 runs on a narrow pipe
+        long long X[kAhead], Y[kAhead], Z[kAhead];
         df c[kAhead], r[kAhead];
         bool ok[kAhead];
 #pragma unroll
         for (int u = 0; u < kAhead; ++u) {
             const long long i = base + static_cast<long long>(j0 + u) * kMomThreads;
             ok[u] = i < n;
-            X[u] = Y[u] = Z[u] = 0.0;
+            X[u] = Y[u] = Z[u] = 0;
             c[u] = r[u] = df{0.0f, 0.0f};
             if (ok[u]) {
-                X[u] = xv[i];
-                Y[u] = yv[i];
-                Z[u] = zv[i];
+                X[u] = __ldg(reinterpret_cast<const long long *>(xv) + i);
+                Y[u] = __ldg(reinterpret_cast<const long long *>(yv) + i);
+                Z[u] = __ldg(reinterpret_cast<const long long *>(zv) + i);
                 if (colrow) {
                     const float4 cr = colrow[static_cast<long long>(v) * n + i];
                     c[u] = {cr.x, cr.y};
@@ -745,7 +748,9 @@ __global__ void __launch_bounds__(kErrThreads, 4) error_points_kernel(
         unsigned pk = 0xffffffffu, ik = 0xffffffffu;
         if (k && ec.ok) {
             float X, Y, Z, cf_, rf_;
-            normalised_point(ec.nf, xv[i], yv[i], zv[i], c, r, X, Y, Z, cf_, rf_);
+            normalised_point(ec.nf, __ldg(reinterpret_cast<const long long *>(xv) + i),
+                             __ldg(reinterpret_cast<const long long *>(yv) + i),
+                             __ldg(reinterpret_cast<const long long *>(zv) + i), c, r, X, Y, Z, cf_, rf_);
             const df h0 = dot2(ec.q, X, Y, Z), h1 = dot2(ec.q + 4, X, Y, Z), h2 = dot2(ec.q + 8, X, Y, Z);
             // observation in the normalised frame as a double-float: (c - c0) / sp
             const df cn = df_mul(df_add(c, {-ec.nf.c0.hi, -ec.nf.c0.lo}), ec.nf.inv_sp);
