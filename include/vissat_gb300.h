@@ -297,6 +297,12 @@ int vs_aoi_batch_run(const VsAoiBatch *plan, int view_begin, int view_end, int b
 int vs_aoi_batch_fuse(const VsAoiBatch *plan, int aoi_begin, int aoi_end, const float *view_dsm,
                       float *fused, int median_blur, void *scratch, size_t scratch_bytes, void *stream);
 void vs_aoi_batch_destroy(VsAoiBatch *plan);
+/* Copies the width x height window of a height map in host memory (pinned for an
+ * asynchronous copy; row stride host_row_stride floats) into device memory (row stride
+ * row_stride floats) on `stream`: how a request's views reach the device when they are
+ * not resident (the serving form's misses). */
+int vs_map_upload(const float *host_heights, int64_t host_row_stride, int width, int height, float *heights,
+                  int64_t row_stride, void *stream);
 
 /* ---- (d) fusion ----------------------------------------------------------------------- */
 

@@ -89,3 +89,31 @@ def test_overlapping_batches_match_alone_and_the_oracle(catalog):
         got = outs[r.rid].numpy()
         assert same_bits(got, alone[r.rid])
         assert same_bits(got, ref[r.aoi])
+
+
+def test_host_held_maps_give_the_same_bits(catalog):
+    """Requests whose height maps live in pinned host memory (copied to the device by the
+    misses, windows of a larger map) serve the same fused DSMs as device-held maps."""
+    from vissatsatellitestereo_gb300 import synth
+    from vissatsatellitestereo_gb300.batch import upload_map
+    specs, views_of, ref = catalog
+    _, maps, affines = synth.small_aoi_case()
+    host = []
+    for ms in maps:
+        hs = []
+        for m in ms:
+            big = torch.full((m.shape[0] + 3, m.shape[1] + 5), 7.0, dtype=torch.float32).pin_memory()
+            big[:m.shape[0], :m.shape[1]] = torch.from_numpy(m)
+            hs.append(big)
+        host.append(hs)
+
+    def host_views(a):
+        return [(h, m.shape[1], m.shape[0], aff) for h, m, aff in zip(host[a], maps[a], affines[a])]
+    up = upload_map(host[0][0], maps[0][0].shape[1], maps[0][0].shape[0])
+    torch.cuda.synchronize()
+    assert same_bits(up.cpu().numpy(), maps[0][0])
+    aois = [0, 1, 2, 0, 2]
+    srv, reqs, outs = serve(specs, host_views, aois, batched=True)
+    assert srv.h2d_bytes == sum(4 * m.size for a in (0, 1, 2) for m in maps[a])
+    for r in reqs:
+        assert same_bits(outs[r.rid], ref[r.aoi])

@@ -202,3 +202,23 @@ def map_points(heights, affine, width=None, height=None, out=None):
     _lib.call('vs_map_points', heights.data_ptr(), heights.stride(0), width, height, m.e0, m.n0, m.ej, m.ei, m.nj,
               m.ni, out.data_ptr(), stream_handle())
     return out
+
+
+def upload_map(heights, width=None, height=None, out=None):
+    """The (height, width) window of a height map held in host memory (CPU float32, 2-D,
+    unit column stride; pinned for the copy to be asynchronous) as a contiguous CUDA
+    tensor, copied on the current stream (``vs_map_upload``)."""
+    require_cuda()
+    if heights.is_cuda or heights.dtype != torch.float32 or heights.dim() != 2 or heights.stride(1) != 1:
+        raise ValueError('heights must be a 2-D CPU float32 tensor with unit column stride')
+    height = heights.shape[0] if height is None else int(height)
+    width = heights.shape[1] if width is None else int(width)
+    if height > heights.shape[0] or width > heights.shape[1]:
+        raise ValueError('window larger than the map')
+    if out is None:
+        out = torch.empty((height, width), dtype=torch.float32, device='cuda')
+    elif not (out.is_cuda and out.dtype == torch.float32 and out.shape == (height, width) and out.is_contiguous()):
+        raise ValueError('out must be a contiguous (height, width) float32 CUDA tensor')
+    _lib.call('vs_map_upload', heights.data_ptr(), heights.stride(0), width, height, out.data_ptr(), width,
+              stream_handle())
+    return out

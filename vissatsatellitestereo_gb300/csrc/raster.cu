@@ -2108,6 +2108,21 @@ extern "C" int vs_dsm_from_depth_maps(const float *const *depths, const int64_t 
     return VS_OK;
 }
 
+extern "C" int vs_map_upload(const float *host_heights, int64_t host_row_stride, int width, int height, float *heights,
+                             int64_t row_stride, void *stream) {
+    VS_REQUIRE(host_heights && heights && width > 0 && height > 0 && host_row_stride >= width && row_stride >= width,
+               "vs_map_upload: bad arguments (%dx%d, strides %lld / %lld)", width, height, (long long)host_row_stride,
+               (long long)row_stride);
+    const size_t f = sizeof(float);
+    if (cudaMemcpy2DAsync(heights, static_cast<size_t>(row_stride) * f, host_heights,
+                          static_cast<size_t>(host_row_stride) * f, static_cast<size_t>(width) * f,
+                          static_cast<size_t>(height), cudaMemcpyHostToDevice, as_stream(stream)) != cudaSuccess) {
+        set_error("vs_map_upload: cudaMemcpy2DAsync failed: %s", cudaGetErrorString(cudaGetLastError()));
+        return VS_ERR_CUDA;
+    }
+    return VS_OK;
+}
+
 extern "C" int vs_map_points(const float *heights, int64_t row_stride, int width, int height, int64_t e0, int64_t n0,
                              int64_t ej, int64_t ei, int64_t nj, int64_t ni, double *points, void *stream) {
     VS_REQUIRE(heights && points && width > 0 && height > 0 && row_stride >= width,

@@ -5,9 +5,10 @@ the AOI's per-view DSMs of produce_dsm.py:46-58).  The server keeps, per AOI, it
 set (the perspective fits of camera_approx.py:150-204) and its partial DSMs (one float32
 DSM per view) resident in HBM under an admission budget, evicting the least recently used
 AOIs that no batch on the device still needs.  A request for a resident AOI costs one
-fusion; a miss first rasterises all of the AOI's views (one persistent binning launch and
-one epilogue launch for all misses of the batch, straight into the resident stacks) and
-fits its cameras.
+fusion; a miss first brings the AOI's height maps to the device when they are held in
+host memory (the request's inputs: one copy per view on the batch's stream), rasterises
+all of its views (one persistent tile launch for all misses of the batch, straight into
+the resident stacks) and fits its cameras.
 
 Continuous batching with overlap on the device: every iteration takes all requests that
 have arrived (up to ``max_batch``) as one batch and issues its work -- misses, fits,
@@ -27,7 +28,7 @@ import numpy as np
 import torch
 
 from .aggregate_2p5d import fuse_dsms
-from .batch import AoiBatch, AoiGrid, MapAffine, MapView
+from .batch import AoiBatch, AoiGrid, MapAffine, MapView, upload_map
 
 
 @dataclass
@@ -107,7 +108,8 @@ def state_bytes(spec):
 
 
 def pool_view_source(specs, pool, affines):
-    """View source over a resident height-map pool: view k of AOI a reads pool map
+    """View source over a height-map pool (on the device, or in pinned host memory, from
+    where a miss copies the windows it needs): view k of AOI a reads pool map
     (first view index of a + k) mod P, window [:image, :image]."""
     first = np.concatenate([[0], np.cumsum([s.n_views for s in specs])]).tolist()
     P = pool.shape[0]
@@ -151,11 +153,19 @@ class FusionServer:
         self.fused_cell_views = 0     # cell-views read by fusions
         self.fit_points = 0
         self.batches = 0
+        self.h2d_bytes = 0            # height maps copied from host memory for misses
 
     # ---- misses -----------------------------------------------------------------------
     def _views(self, a, stack):
-        return [MapView(h, w, hh, MapAffine(**aff), dsm=stack[v])
-                for v, (h, w, hh, aff) in enumerate(self.view_source(a))]
+        """The AOI's views as device maps: maps held in host memory (the request's inputs)
+        are copied to the device on the current stream first."""
+        out = []
+        for v, (h, w, hh, aff) in enumerate(self.view_source(a)):
+            if not h.is_cuda:
+                h = upload_map(h, w, hh)
+                self.h2d_bytes += 4 * w * hh
+            out.append(MapView(h, w, hh, MapAffine(**aff), dsm=stack[v]))
+        return out
 
     def _rasterise(self, aois, stacks):
         grids = [AoiGrid(self.specs[a].xoff, self.specs[a].yoff, self.specs[a].res, self.specs[a].res,
@@ -319,6 +329,7 @@ class FusionServer:
             'dsm_cells_per_s_busy': self.cell_views / busy if busy else None,
             'fused_cell_views_per_s_busy': self.fused_cell_views / busy if busy else None,
             'rpc_fit_pts_per_s_busy': self.fit_points / busy if busy else None,
+            'h2d_map_gb': round(self.h2d_bytes / 1e9, 2),
             'latency': 'arrival to the fused DSM in host memory (pinned), polled completion events',
             'busy': 'wall time during which at least one batch was on the device',
         }
