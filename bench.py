@@ -167,13 +167,15 @@ def run_ours(args):
     main = torch.cuda.current_stream()
     s_fit, s_epi = torch.cuda.Stream(), torch.cuda.Stream()
     s_hi, s_epi_hi = torch.cuda.Stream(priority=-1), torch.cuda.Stream(priority=-1)   # high priority
+    s_fit_hi = torch.cuda.Stream(priority=-1)
     # schedules: the rasterisation's stream, its epilogue stream (None: the same, serial), and
     # whether the fit starts with the rasterisation or after it (then overlapping the fusion)
     SCHEDULES = {
-        'fit_concurrent': dict(ras=main, epi=s_epi, late=False),
-        'fit_concurrent_raster_high_priority': dict(ras=s_hi, epi=s_epi_hi, late=False),
-        'fit_concurrent_raster_high_priority_serial_epilogues': dict(ras=s_hi, epi=None, late=False),
-        'fit_after_raster_with_fusion': dict(ras=main, epi=s_epi, late=True),
+        'fit_concurrent': dict(ras=main, epi=s_epi, late=False, fit=s_fit),
+        'fit_concurrent_raster_high_priority': dict(ras=s_hi, epi=s_epi_hi, late=False, fit=s_fit),
+        'fit_concurrent_raster_high_priority_serial_epilogues': dict(ras=s_hi, epi=None, late=False, fit=s_fit),
+        'fit_concurrent_fit_high_priority': dict(ras=main, epi=s_epi, late=False, fit=s_fit_hi),
+        'fit_after_raster_with_fusion': dict(ras=main, epi=s_epi, late=True, fit=s_fit),
     }
     sched = [SCHEDULES['fit_concurrent']]
     cams_t = torch.from_numpy(_lib.camera_array(wl.metas)).to(dev)
@@ -182,8 +184,8 @@ def run_ours(args):
         return approx_perspective_enu(cams_t, grid_t['lat'], grid_t['lon'], grid_t['alt'], grid_t['x'],
                                       grid_t['y'], grid_t['z'], mode='fast', shared_points=False)
 
-    def run_fit(ev):
-        with torch.cuda.stream(s_fit):
+    def run_fit(ev, fs):
+        with torch.cuda.stream(fs):
             if ev: ev['f0'].record()
             out = fit()
             if ev: ev['f1'].record()
@@ -191,24 +193,24 @@ def run_ours(args):
 
     def step(ev=None):
         cfg = sched[0]
-        ras = cfg['ras']
+        ras, fs = cfg['ras'], cfg['fit']
         if ev: ev['t0'].record()
-        s_fit.wait_stream(main)
+        fs.wait_stream(main)
         if ras is not main:
             ras.wait_stream(main)
-        out = None if cfg['late'] else run_fit(ev)
+        out = None if cfg['late'] else run_fit(ev, fs)
         with torch.cuda.stream(ras):
             dsm_from_points(points, offsets, *gargs, out=dsms, epilogue_stream=cfg['epi'] or ras,
                             bin_events=ev['bins'] if ev else None)
             if ev: ev['r1'].record()
             if cfg['late']:
-                s_fit.wait_stream(ras)
-                out = run_fit(ev)
+                fs.wait_stream(ras)
+                out = run_fit(ev, fs)
             fuse_dsms(dsms, median_blur=True, layout='vhw', out=fused)
             if ev: ev['u1'].record()
         if ras is not main:
             main.wait_stream(ras)
-        main.wait_stream(s_fit)
+        main.wait_stream(fs)
         if ev: ev['t1'].record()
         return out
 
