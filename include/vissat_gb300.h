@@ -112,6 +112,11 @@ int vs_rpc_project_cube_status(const void *workspace, int n_cams, int variant, v
  * far beyond any real completion time); 0 gives up at once, so tests can drive the
  * timeout path without a faulty device.  Process-wide; not thread-safe. */
 void vs_set_tc_wait_limit(unsigned polls);
+/* Caps the CTAs per SM of the point-binning launches of vs_proj_to_grid and
+ * vs_dsm_from_points* (0, the default: as many as fit).  A cap leaves room on every SM for
+ * kernels of other streams (the camera fit running concurrently with the rasterisation);
+ * process-wide, read at each launch. */
+void vs_set_binning_ctas_per_sm(int ctas);
 
 /* Replaces RPCModel.inverse_projection (lib/rpc_model.py:170-249) for n_cams cameras:
  * (lon, lat) of image points (col, row) at altitudes alt, by the reference's iteration

@@ -788,6 +788,10 @@ int make_tables(double xoff, double yoff, double xres, double yres, long long xs
     return make_axis(tb.col, xoff, yres, xsize, +1, w.col_thr, st);
 }
 
+// CTAs per SM of the point-binning launches (0: as many as fit); set through
+// vs_set_binning_ctas_per_sm.
+int g_bin_ctas_per_sm = 0;
+
 int bin_launch(const double *points, const long long *offsets, int v, long long single_n, long long max_points,
                const Tables &tb, unsigned long long *keys, unsigned long long *first, cudaStream_t st) {
     if (max_points <= 0) return VS_OK;
@@ -821,9 +825,10 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
                 per_sm = 4;
             resident = per_sm;
         }
+        const int per_sm = g_bin_ctas_per_sm > 0 ? std::min(g_bin_ctas_per_sm, resident) : resident;
         gx = static_cast<unsigned>(std::max<long long>(
             1LL, std::min<long long>(ceil_div(ceil_div(max_points, kFastPts), threads),
-                                     static_cast<long long>(sm_count()) * resident)));
+                                     static_cast<long long>(sm_count()) * per_sm)));
         if (flip_row && !flip_col)
             bin_fast_kernel<true, false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
         else if (flip_row && flip_col)
@@ -2107,6 +2112,8 @@ extern "C" int vs_dsm_from_depth_maps(const float *const *depths, const int64_t 
     }
     return VS_OK;
 }
+
+extern "C" void vs_set_binning_ctas_per_sm(int ctas) { vs::g_bin_ctas_per_sm = ctas > 0 ? ctas : 0; }
 
 extern "C" int vs_map_upload(const float *host_heights, int64_t host_row_stride, int width, int height, float *heights,
                              int64_t row_stride, void *stream) {
