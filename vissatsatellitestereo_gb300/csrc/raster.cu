@@ -581,35 +581,36 @@ __device__ __forceinline__ void epilogue_tile(const unsigned long long *__restri
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx, lane = tid & 31;
     bool special = false;          // this thread staged a NaN or a zero
     if (tid == 0) sm.n_holes = 0;
-    for (int i = tid; i < RAW_H * RAW_W; i += TX * TY) {
+    __syncthreads();
+    // one pass over the key block: stage the keys (the hole fill reads the neighbours) and,
+    // for the blur input's cells, the float32 values and the list of empty cells
+    for (int base = 0; base < RAW_H * RAW_W; base += TX * TY) {
+        const int i = base + tid;
+        const bool in = i < RAW_H * RAW_W;
         const int ly = i / RAW_W, lx = i - ly * RAW_W;
         const int r = r0 + ly - 2, c = c0 + lx - 2;
         unsigned long long k = kEmptyKey;
-        if (static_cast<unsigned>(r) < static_cast<unsigned>(H) && static_cast<unsigned>(c) < static_cast<unsigned>(W)) {
+        if (in && static_cast<unsigned>(r) < static_cast<unsigned>(H) && static_cast<unsigned>(c) < static_cast<unsigned>(W)) {
             const long long cell = static_cast<long long>(r) * W + c;
             k = dec(vk[cell], cell);
         }
-        sm.raw[i] = k;
-    }
-    __syncthreads();
-    for (int base = 0; base < FK_H * FK_W; base += TX * TY) {
-        const int i = base + tid;
-        const bool in = i < FK_H * FK_W;
-        const int ly = i / FK_W, lx = i - ly * FK_W;
-        const unsigned long long k = in ? sm.raw[(ly + 1) * RAW_W + lx + 1] : 1ull;
-        if (in && k != kEmptyKey) {
+        if (in) sm.raw[i] = k;
+        const bool inner = in && ly >= 1 && ly <= RAW_H - 2 && lx >= 1 && lx <= RAW_W - 2;
+        if (inner && k != kEmptyKey) {
             const float f = f64_to_f32(double_from_key(k));
-            sm.fk[ly][lx] = f;
+            sm.fk[ly - 1][lx - 1] = f;
             special |= isnan(f) || f == 0.0f;
         }
         // warp-aggregated append of the empty cells to the hole list
-        const unsigned empty = __ballot_sync(0xffffffffu, in && k == kEmptyKey);
+        const bool hole = inner && k == kEmptyKey;
+        const unsigned empty = __ballot_sync(0xffffffffu, hole);
         if (empty) {
             int slot = 0;
             if (lane == __ffs(empty) - 1) slot = atomicAdd(&sm.n_holes, __popc(empty));
             slot = __shfl_sync(0xffffffffu, slot, __ffs(empty) - 1);
-            if (in && k == kEmptyKey)
-                sm.holes[slot + __popc(empty & ((1u << lane) - 1u))] = static_cast<unsigned short>(i);
+            if (hole)
+                sm.holes[slot + __popc(empty & ((1u << lane) - 1u))] =
+                    static_cast<unsigned short>((ly - 1) * FK_W + (lx - 1));
         }
     }
     __syncthreads();
