@@ -122,11 +122,17 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------
 # our arm
 # ------------------------------------------------------------------------------------
-def launches_per_step(views):
+# DRAM bytes (read + write) of raster_pipe_kernel per point binned and per DSM cell of the
+# epilogue, from an ncu capture (None: not captured)
+PIPE_TRAFFIC = None
+
+
+def launches_per_step(views, piped=False):
     # kernels only (memsets are not kernels); checked against the ncu launch list
     camera = 15        # bbox init, bbox, norm, prepare, project, moments, solve, error points, error count,
     #                    select step x3, select histogram x2, error final
-    raster = 2 + views * 2   # thresholds x2; per view: bin, epilogue
+    # thresholds x2; per view: bin, epilogue -- or, pipelined, views + 1 launches
+    raster = 2 + (views + 1 if piped else views * 2)
     fusion = 2               # fuse + blur
     return camera + raster + fusion
 
@@ -179,6 +185,10 @@ def run_ours(args):
         **{f'fit_concurrent_raster_high_priority_binning_{c}_ctas': dict(ras=s_hi, epi=s_epi_hi, late=False, fit=s_fit,
                                                                          bin_ctas=c) for c in (3, 4, 5)},
         'fit_after_raster_with_fusion': dict(ras=main, epi=s_epi, late=True, fit=s_fit),
+        # one launch per view binning it while its other CTAs run the previous view's epilogue
+        'fit_concurrent_raster_high_priority_pipelined': dict(ras=s_hi, epi=None, late=False, fit=s_fit, pipe=True),
+        **{f'fit_concurrent_raster_high_priority_pipelined_{c}_ctas': dict(ras=s_hi, epi=None, late=False, fit=s_fit,
+                                                                           pipe=True, bin_ctas=c) for c in (4, 5)},
     }
     sched = [SCHEDULES['fit_concurrent']]
     cams_t = torch.from_numpy(_lib.camera_array(wl.metas)).to(dev)
@@ -204,8 +214,12 @@ def run_ours(args):
             ras.wait_stream(main)
         out = None if cfg['late'] else run_fit(ev, fs)
         with torch.cuda.stream(ras):
-            dsm_from_points(points, offsets, *gargs, out=dsms, epilogue_stream=cfg['epi'] or ras,
-                            bin_events=ev['bins'] if ev else None)
+            if cfg.get('pipe'):
+                dsm_from_points(points, offsets, *gargs, out=dsms, pipelined=True,
+                                launch_events=ev['pipe'] if ev else None)
+            else:
+                dsm_from_points(points, offsets, *gargs, out=dsms, epilogue_stream=cfg['epi'] or ras,
+                                bin_events=ev['bins'] if ev else None)
             if ev: ev['r1'].record()
             if cfg['late']:
                 fs.wait_stream(ras)
@@ -248,9 +262,10 @@ def run_ours(args):
     clocks.start()
     names = ('t0', 'f0', 'f1', 'r1', 'u1', 't1')
     stage_ev = [{k: torch.cuda.Event(enable_timing=True) for k in names} for _ in range(args.steps)]
-    for ev in stage_ev:     # events around every view's bin_fast_kernel launch (roofline)
+    for ev in stage_ev:     # events around every view's bin_fast_kernel / raster_pipe_kernel launch (roofline)
         ev['bins'] = [torch.cuda.Event(enable_timing=True) for _ in range(2 * wl.views)]
-        for e in ev['bins']:
+        ev['pipe'] = [torch.cuda.Event(enable_timing=True) for _ in range(2 * (wl.views + 1))]
+        for e in ev['bins'] + ev['pipe']:
             e.record()
     torch.cuda.synchronize()
     t0 = torch.cuda.Event(enable_timing=True)
@@ -285,23 +300,26 @@ def run_ours(args):
     status_np = status.cpu().numpy()
     value = wl.cells_per_step * args.steps * world / elapsed
 
-    # ---- roofline of the dominant kernel: bin_fast_kernel (one launch per view, ~40% of the
-    # step's kernel time in the ncu launch list).  Per launch the algorithmic bytes are the
-    # view's FP64 points (24 B each; the key grid it updates stays in L2).  Its duration is
-    # measured live inside the timed steps by CUDA events recorded on the launching stream
-    # around every launch.  The rasterisation stage as a whole (binning + the overlapped
-    # epilogue, algorithmic bytes + the 4 B per cell DSM) is timed alone beside it.
+    # ---- roofline of the dominant kernel.  With the pipelined rasterisation (the schedule
+    # normally chosen) that is raster_pipe_kernel: launch v bins view v (24 B per FP64 point
+    # read; the key grid it updates stays in L2) while its other CTAs run view v-1's
+    # epilogue (4 B per DSM cell written; its keys are read from L2), so one call's V + 1
+    # launches move V x (24 B x points + 4 B x cells) algorithmic bytes.  Otherwise it is
+    # bin_fast_kernel (one launch per view, 24 B per point).  Durations are CUDA events
+    # recorded on the launching stream around every launch, inside the timed steps and in
+    # rasterisations timed alone (no concurrent fit) after them.
     import json as _json
     peaks = {}
     pk_path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
     if os.path.exists(pk_path):
         peaks = _json.load(open(pk_path))
     hbm_peak = float(peaks.get('hbm_gbs', 6800.0))
-    step_bin_ms = [ev['bins'][2 * v].elapsed_time(ev['bins'][2 * v + 1]) for ev in stage_ev for v in range(wl.views)]
+    peak_source = 'of measured (MEASURED_PEAKS.json hbm_gbs)' if 'hbm_gbs' in peaks else 'of fallback 6800 GB/s'
+    piped = bool(SCHEDULES[best].get('pipe'))
     view_bytes = n_pts * 24 + G.xsize * G.ysize * 4
     bin_bytes = n_pts * 24
-    # the rasterisation alone (no concurrent camera fit), with the same per-launch events
     alone_reps = max(3, min(args.steps, 10))
+    # bin_fast_kernel alone: the serial two-kernel rasterisation with events around each binning
     alone_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2 * wl.views)] for _ in range(alone_reps)]
     r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     dsm_from_points(points, offsets, *gargs, out=dsms, epilogue_stream=s_epi)
@@ -315,25 +333,75 @@ def run_ours(args):
     bin_ms = [ev[2 * v].elapsed_time(ev[2 * v + 1]) for ev in alone_ev for v in range(wl.views)]
     bin_s = statistics.mean(bin_ms) / 1e3
     bin_gbs = bin_bytes / bin_s / 1e9
-    step_bin_s = statistics.mean(step_bin_ms) / 1e3
-    # DRAM traffic per launch from ncu (bin_fast_kernel on 4.19 M points: 112.1 MB read +
-    # write, i.e. 26.7 B per point, scaled by points)
-    traffic = int(26.73 * n_pts)
-    roofline = {'bound': 'hbm', 'kernel': 'bin_fast_kernel (max-height binning of one view)',
-                'achieved': round(bin_gbs, 1), 'peak': hbm_peak, 'unit': 'GB/s',
-                'frac': round(bin_gbs / hbm_peak, 4),
-                'peak_source': 'of measured (MEASURED_PEAKS.json hbm_gbs)' if 'hbm_gbs' in peaks else 'of fallback 6800 GB/s',
-                'algorithmic_bytes_per_launch': bin_bytes, 'launch_ms': round(bin_s * 1e3, 4),
-                'timing': f'CUDA events on the launching stream around each of {len(bin_ms)} launches '
-                          f'({alone_reps} rasterisations of all {wl.views} views on one stream, no concurrent work)',
-                'traffic': traffic, 'traffic_source': 'ncu dram__bytes_read+write, 2048^2-point capture scaled',
-                'in_step': {'launch_ms': round(step_bin_s * 1e3, 4),
-                            'achieved': round(bin_bytes / step_bin_s / 1e9, 1),
-                            'frac': round(bin_bytes / step_bin_s / 1e9 / hbm_peak, 4),
-                            'note': 'inside the timed steps, sharing the GPU with the concurrent camera fit'},
-                'raster_stage_alone_serial': {'view_ms': round(view_s * 1e3, 4), 'algorithmic_bytes': view_bytes,
-                                       'achieved': round(view_bytes / view_s / 1e9, 1),
-                                       'frac': round(view_bytes / view_s / 1e9 / hbm_peak, 4)}}
+    # raster_pipe_kernel alone: the pipelined rasterisation with events around each launch
+    n_launch = wl.views + 1
+    pipe_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2 * n_launch)] for _ in range(alone_reps)]
+    dsm_from_points(points, offsets, *gargs, out=dsms, pipelined=True)
+    torch.cuda.synchronize()
+    r0.record()
+    for k in range(alone_reps):
+        dsm_from_points(points, offsets, *gargs, out=dsms, pipelined=True, launch_events=pipe_ev[k])
+    r1.record()
+    torch.cuda.synchronize()
+    pipe_view_s = r0.elapsed_time(r1) / 1e3 / alone_reps / wl.views
+    pipe_ms = [ev[2 * i].elapsed_time(ev[2 * i + 1]) for ev in pipe_ev for i in range(n_launch)]
+    pipe_call_s = sum(pipe_ms) / 1e3 / alone_reps               # kernel time of one call
+    pipe_bytes = wl.views * view_bytes                          # algorithmic bytes of one call
+    pipe_gbs = pipe_bytes / pipe_call_s / 1e9
+    # DRAM traffic per launch from ncu: bin_fast_kernel on 4.19 M points moved 112.1 MB
+    # (read + write), i.e. 26.7 B per point, scaled by points; raster_pipe_kernel from its
+    # own capture (PIPE_TRAFFIC: bytes per point and per cell), scaled the same way
+    bin_traffic = int(26.73 * n_pts)
+    timing = (f'CUDA events on the launching stream around each launch ({alone_reps} rasterisations of all '
+              f'{wl.views} views on one stream, no concurrent work)')
+    bin_alone = {'kernel': 'bin_fast_kernel (max-height binning of one view)', 'launch_ms': round(bin_s * 1e3, 4),
+                 'algorithmic_bytes_per_launch': bin_bytes, 'achieved': round(bin_gbs, 1),
+                 'frac': round(bin_gbs / hbm_peak, 4), 'traffic': bin_traffic}
+    if piped:
+        step_ms = [ev['pipe'][2 * i].elapsed_time(ev['pipe'][2 * i + 1]) for ev in stage_ev for i in range(n_launch)]
+        step_call_s = sum(step_ms) / 1e3 / len(stage_ev)
+        pt = PIPE_TRAFFIC
+        roofline = {'bound': 'hbm',
+                    'kernel': 'raster_pipe_kernel (launch v: view v binning + view v-1 decode/hole fill/blur)',
+                    'achieved': round(pipe_gbs, 1), 'peak': hbm_peak, 'unit': 'GB/s',
+                    'frac': round(pipe_gbs / hbm_peak, 4), 'peak_source': peak_source,
+                    'algorithmic_bytes_per_launch': pipe_bytes // n_launch,
+                    'algorithmic_bytes': '24 B per point of view v + 4 B per DSM cell of view v-1 per launch; '
+                                         f'{wl.views} x {view_bytes} B over the {n_launch} launches of one call',
+                    'launch_ms': round(pipe_call_s * 1e3 / n_launch, 4), 'timing': timing,
+                    'traffic': None if pt is None else int((pt[0] * n_pts + pt[1] * G.xsize * G.ysize) * wl.views
+                                                           / n_launch),
+                    'traffic_source': 'ncu dram__bytes_read+write of a 2-view 2048^2 capture, scaled by points and '
+                                      'cells',
+                    'in_step': {'launch_ms': round(step_call_s * 1e3 / n_launch, 4),
+                                'achieved': round(pipe_bytes / step_call_s / 1e9, 1),
+                                'frac': round(pipe_bytes / step_call_s / 1e9 / hbm_peak, 4),
+                                'note': 'inside the timed steps, sharing the GPU with the concurrent camera fit'},
+                    'bin_fast_kernel_alone': bin_alone,
+                    'raster_stage_alone': {'view_ms': round(pipe_view_s * 1e3, 4), 'algorithmic_bytes': view_bytes,
+                                           'achieved': round(view_bytes / pipe_view_s / 1e9, 1),
+                                           'frac': round(view_bytes / pipe_view_s / 1e9 / hbm_peak, 4)},
+                    'raster_stage_alone_two_kernels_serial': {'view_ms': round(view_s * 1e3, 4)}}
+    else:
+        step_bin_ms = [ev['bins'][2 * v].elapsed_time(ev['bins'][2 * v + 1]) for ev in stage_ev
+                       for v in range(wl.views)]
+        step_bin_s = statistics.mean(step_bin_ms) / 1e3
+        roofline = {'bound': 'hbm', 'kernel': bin_alone['kernel'],
+                    'achieved': round(bin_gbs, 1), 'peak': hbm_peak, 'unit': 'GB/s',
+                    'frac': round(bin_gbs / hbm_peak, 4), 'peak_source': peak_source,
+                    'algorithmic_bytes_per_launch': bin_bytes, 'launch_ms': round(bin_s * 1e3, 4),
+                    'timing': timing, 'traffic': bin_traffic,
+                    'traffic_source': 'ncu dram__bytes_read+write, 2048^2-point capture scaled',
+                    'in_step': {'launch_ms': round(step_bin_s * 1e3, 4),
+                                'achieved': round(bin_bytes / step_bin_s / 1e9, 1),
+                                'frac': round(bin_bytes / step_bin_s / 1e9 / hbm_peak, 4),
+                                'note': 'inside the timed steps, sharing the GPU with the concurrent camera fit'},
+                    'raster_stage_alone_serial': {'view_ms': round(view_s * 1e3, 4), 'algorithmic_bytes': view_bytes,
+                                                  'achieved': round(view_bytes / view_s / 1e9, 1),
+                                                  'frac': round(view_bytes / view_s / 1e9 / hbm_peak, 4)},
+                    'raster_pipe_kernel_alone': {'view_ms': round(pipe_view_s * 1e3, 4),
+                                                 'achieved': round(pipe_gbs, 1),
+                                                 'frac': round(pipe_gbs / hbm_peak, 4)}}
 
     # the camera fit alone (no concurrent rasterisation), same call as in the step
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -357,7 +425,7 @@ def run_ours(args):
         'schedule': best + ' (the fastest of the schedules timed before the timed steps)',
         'schedule_ms': {k: round(v, 3) for k, v in sched_ms.items()},
         'serial_ms_per_step': serial_ms,
-        'roofline': roofline, 'clocks': clock_info, 'gpu_launches': launches_per_step(wl.views) * args.steps,
+        'roofline': roofline, 'clocks': clock_info, 'gpu_launches': launches_per_step(wl.views, piped) * args.steps,
     }
 
     if rank == 0 and not args.skip_extra:

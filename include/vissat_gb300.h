@@ -235,6 +235,19 @@ int vs_dsm_from_points_overlap(const double *points, const int64_t *offsets, int
                                int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
                                void *stream, void *epilogue_stream, void *const *bin_events);
 
+/* vs_dsm_from_points as n_views + 1 launches on one stream, launch v binning view v while
+ * its other CTAs run view v-1's decode / hole fill / blur (work items handed out by a
+ * device counter), so the HBM-bound binning and the issue-bound epilogue share every SM.
+ * Same arguments and results as vs_dsm_from_points (produce_dsm.py:46-58 per view).  Grids
+ * outside the fast binning's precondition run the two kernels view by view.  launch_events
+ * (nullable): 2 * (n_views + 1) cudaEvent_t created by the caller; on the fast path events
+ * 2v and 2v+1 are recorded on `stream` just before and after launch v (kernel timing). */
+size_t vs_dsm_from_points_pipelined_workspace_size(int n_views, int64_t xsize, int64_t ysize);
+int vs_dsm_from_points_pipelined(const double *points, const int64_t *offsets, int n_views, double xoff,
+                                 double yoff, double xresolution, double yresolution, int64_t xsize,
+                                 int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
+                                 void *stream, void *const *launch_events);
+
 /* vs_dsm_from_points with the points in HOST memory (the reference's numpy arrays; pinned
  * memory lets the copies overlap the binning): view v's points are copied into staging
  * buffer v % ring (ring 1..8, device buffers in the workspace) on `copy_stream` while the

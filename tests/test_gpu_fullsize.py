@@ -48,8 +48,10 @@ def test_full_size_raster_schedules_and_batch_independence(aoi50):
     pts, offsets, args, n = aoi50
     serial = dsm_from_points(pts, offsets, *args)
     over = dsm_from_points(pts, offsets, *args, epilogue_stream=torch.cuda.Stream())
+    pipe = dsm_from_points(pts, offsets, *args, pipelined=True)
     torch.cuda.synchronize()
     assert torch.equal(serial.view(torch.int32), over.view(torch.int32))
+    assert torch.equal(serial.view(torch.int32), pipe.view(torch.int32))
     for v in (0, 17, 49):
         alone = dsm_from_points(pts[v * n:(v + 1) * n], torch.tensor([0, n]), *args)
         assert torch.equal(alone[0].view(torch.int32), serial[v].view(torch.int32)), v

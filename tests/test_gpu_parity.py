@@ -268,6 +268,80 @@ def test_dsm_from_points_overlap_matches_serial_and_oracle():
         assert (over[v] == 0).any()
 
 
+@pytest.mark.parametrize('ctas', [0, 3, 5])
+def test_dsm_from_points_pipelined_matches_serial_and_oracle(ctas):
+    """One launch per view bins view v while its other CTAs run view v-1's epilogue
+    (vs_dsm_from_points_pipelined): identical to the serial call and the oracle, with signed
+    zeros alternating view by view, an empty view, a one-point view, odd view offsets and
+    more views than key grids; at full occupancy and with the CTAs per SM capped (the
+    48-register build at 5 or fewer)."""
+    from vissatsatellitestereo_gb300 import _lib, synth
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    grid = synth.DsmGrid(synth.EXPLORER_UL_EASTING, synth.EXPLORER_UL_NORTHING, 0.3, 0.3, 230, 170)
+    scene = synth.make_scene(83, grid, 30, 3.0, 80.0)
+    views = synth.make_views(84, scene, 8, 260, 300, 0.1, 0.3, 0.5)
+    clouds = [synth.view_points(scene, v) for v in views]
+    for v, c in enumerate(clouds):
+        c[:6000, 2] = -np.abs(c[:6000, 2]) - 1.0
+        c[:6000:2, 2] = -0.0 if v % 2 else 0.0
+        c[1:6000:4, 2] = 0.0 if v % 2 else -0.0
+    clouds[2] = clouds[2][:0]
+    clouds[3] = clouds[3][:1]
+    clouds[5] = clouds[5][:-13]
+    offsets = np.cumsum([0] + [len(c) for c in clouds])
+    pts = torch.from_numpy(np.concatenate(clouds)).cuda()
+    offs = torch.from_numpy(offsets).cuda()
+    args = (grid.xoff, grid.yoff, grid.xres, grid.yres, grid.xsize, grid.ysize)
+    serial = dsm_from_points(pts, offs, *args).cpu().numpy()
+    _lib.lib().vs_set_binning_ctas_per_sm(ctas)
+    try:
+        pipe = dsm_from_points(pts, offs, *args, pipelined=True)
+        again = dsm_from_points(pts, offs, *args, pipelined=True)     # the counters start from zero per call
+        torch.cuda.synchronize()
+    finally:
+        _lib.lib().vs_set_binning_ctas_per_sm(0)
+    pipe = pipe.cpu().numpy()
+    assert same_bits(pipe, serial)
+    assert same_bits(again.cpu().numpy(), serial)
+    assert np.isnan(pipe[2]).all()
+    for v, c in enumerate(clouds):
+        ref = blur.median_blur3x3(raster.proj_to_grid(c, *args).astype(np.float32))
+        assert same_bits(pipe[v], ref), v
+
+
+@pytest.mark.parametrize('case', ['straddle', 'local_origin', 'single_view'])
+def test_dsm_from_points_pipelined_other_grids(case):
+    """Grids outside the fast binning's precondition (a northing axis across 2^22, an origin
+    at 0) take the per-view kernels inside the pipelined call; a single view has one
+    binning-only and one epilogue-only launch.  All equal the oracle."""
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    rng = np.random.default_rng(12)
+    if case == 'straddle':
+        n = 120000
+        mk = lambda: np.stack([rng.uniform(1000.0, 1300.0, n), rng.uniform(4194304.0 - 150, 4194304.0 + 150, n),
+                               rng.normal(0, 10, n)], 1)
+        args = (1000.0, 4194304.0 + 140, 0.37, 0.37, 700, 700)
+        clouds = [mk(), mk()]
+    elif case == 'local_origin':
+        n = 80000
+        mk = lambda: np.stack([rng.uniform(-5, 120, n), rng.uniform(-120, 5, n), rng.normal(0, 10, n)], 1)
+        args = (0.0, 0.0, 0.5, 0.5, 230, 230)
+        clouds = [mk(), mk(), mk()]
+    else:
+        n = 150001
+        clouds = [np.stack([rng.uniform(354052.0, 354112.0, n), rng.uniform(6182640.0, 6182702.0, n),
+                            rng.normal(20, 10, n)], 1)]
+        args = (354052.25, 6182702.5, 0.3, 0.3, 197, 205)
+    for c in clouds:
+        c[rng.random(len(c)) < 0.05, 2] = np.nan
+    offsets = np.cumsum([0] + [len(c) for c in clouds])
+    pts = torch.from_numpy(np.concatenate(clouds)).cuda()
+    got = dsm_from_points(pts, torch.from_numpy(offsets).cuda(), *args, pipelined=True).cpu().numpy()
+    for v, c in enumerate(clouds):
+        ref = blur.median_blur3x3(raster.proj_to_grid(c, *args).astype(np.float32))
+        assert same_bits(got[v], ref), v
+
+
 def test_dsm_from_points_host_pipeline_equals_device_path():
     """Host points copied view by view into a 3-buffer device ring on a second stream
     (vs_dsm_from_points_host): bit-identical to the device-input call, with an empty view, a

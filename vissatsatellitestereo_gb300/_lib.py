@@ -90,6 +90,9 @@ SIGNATURES = {
     'vs_dsm_from_points_overlap_workspace_size': (_sz, [_int, _i64, _i64]),
     'vs_dsm_from_points_overlap': (_int, [_vp, _vp, _int, _dbl, _dbl, _dbl, _dbl, _i64, _i64, _vp, _vp, _sz, _vp, _vp,
                                           _vp]),
+    'vs_dsm_from_points_pipelined_workspace_size': (_sz, [_int, _i64, _i64]),
+    'vs_dsm_from_points_pipelined': (_int, [_vp, _vp, _int, _dbl, _dbl, _dbl, _dbl, _i64, _i64, _vp, _vp, _sz,
+                                            _vp, _vp]),
     'vs_fuse_dsms_workspace_size': (_sz, [_i64, _i64]),
     'vs_fuse_dsms': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp, _sz, _vp]),
     'vs_fuse_dsms_static': (_int, [_vp, _int, _i64, _i64, _i64, _vp, _int, _vp]),

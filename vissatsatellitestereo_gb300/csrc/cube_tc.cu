@@ -11,26 +11,29 @@
 //        error -- are added in FP32 in the epilogue (z, x, y, then the constant).
 // Monomials enter the reduction from the highest order down, so the large terms come last.
 //
-// One persistent CTA per SM, four warpgroups (512 threads).  Per tile of 128 points:
-//   1. four threads build a point's A row (bf16 pieces) into shared memory (two A
-//      buffers, canonical no-swizzle K-major layout);
-//   2. one thread issues the K/16 MMAs (M = 128, N = 4C rounded up to 16) into one of two
-//      TMEM accumulators and commits them to that accumulator's mbarrier;
-//   3. meanwhile all threads finish the PREVIOUS tile from the other accumulator: each
-//      warp reads its 32 lanes (points) with tcgen05.ld -- warpgroup g a quarter of the
-//      cameras -- forms the quotients (the fast form for a chunk of 8 cameras at once, one
-//      warp-uniform check for rare operands), denormalises and streams the col/row planes
-//      out (a warp writes 32 consecutive points of a plane).
-// The coefficient tile B (all cameras' pieces, prepared once per call) is copied into
-// shared memory once per CTA by the bulk-copy (TMA) engine.
+// One persistent CTA per SM, warp-specialised, tiles of 128 points (the TMEM lanes):
+//   * 2 producer warps: each thread builds two points' A rows (bf16 pieces, canonical
+//     no-swizzle K-major layout) into a 4-stage shared-memory ring;
+//   * 1 MMA warp: its lane 0 issues the K/16 MMAs (M = 128, N = 4C rounded up to 16) of
+//     a tile into one of two TMEM accumulators and commits them to the stage's "empty" and
+//     the accumulator's "full" mbarriers;
+//   * 28 epilogue warps (seven warpgroups, each a seventh of the cameras): a warp reads its
+//     32 lanes (points) with tcgen05.ld, forms the quotients (the fast form for a chunk of
+//     4 cameras at once, one warp-uniform check for rare operands), denormalises, streams
+//     the col/row planes out (32 consecutive points of a plane per store) and releases the
+//     accumulator.
+// No CTA-wide barrier inside the tile loop: the producers run up to four tiles ahead, the
+// tensor cores work on tile k+1 while the epilogue finishes tile k.  The coefficient tile
+// B (all cameras' pieces, prepared once per call) is copied into shared memory once per
+// CTA by the bulk-copy (TMA) engine.
 //
 // Operand layout (no swizzle, K-major): 8-row x 16-byte core matrices; cores adjacent along
 // K are 128 bytes apart (leading byte offset), along M/N K/8 * 128 bytes (stride offset).
 //
-// Every wait is bounded.  A thread that gives up sets the error word and the CTA stops at
-// its next barrier; before freeing its tensor memory the CTA waits (bounded) for the
-// coefficient copy and for every MMA it committed.  vs_rpc_project_cube_status reads the
-// word back.
+// Every wait is bounded.  A warp that gives up sets the error word and a shared abort flag
+// that ends the other roles' waits; before freeing its tensor memory the CTA waits
+// (bounded) for the coefficient copy and for every MMA it committed.
+// vs_rpc_project_cube_status reads the word back.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -40,8 +43,12 @@
 namespace vs {
 namespace {
 
-constexpr int kTcThreads = 512;     // four warpgroups
-constexpr int kTcGroups = kTcThreads / 128;
+constexpr int kTcProducerWarps = 2;                 // two point rows of A per thread
+constexpr int kTcMmaWarp = kTcProducerWarps;        // allocates TMEM; its lane 0 issues the MMAs
+constexpr int kTcEpiWarps = 28;                     // seven epilogue warpgroups
+constexpr int kTcGroups = kTcEpiWarps / 4;          // camera groups of the epilogue
+constexpr int kTcThreads = 32 * (kTcProducerWarps + 1 + kTcEpiWarps);
+constexpr int kTcStages = 4;                        // A ring
 constexpr int kTcTile = 128;        // points per tile = TMEM lanes
 constexpr int kTcTmemCols = 512;    // two accumulators of up to 256 columns
 constexpr int kTcMaxN = 256;
@@ -91,6 +98,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned phase, 
     for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
+}
+
+// Bounded wait that also gives up once another warp of the CTA has raised `abort`.
+__device__ __forceinline__ bool mbar_wait_abortable(unsigned bar, unsigned phase, unsigned limit,
+                                                    const volatile int *abort) {
+    for (unsigned it = 0; it < limit; ++it) {
+        if (mbar_try_wait(bar, phase)) return true;
+        if ((it & 63u) == 63u && *abort) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -195,15 +216,15 @@ __global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int
     }
 }
 
-// Part P of a point's A row: the 16-byte chunks c (8 slots each) with c % 4 == P.
-template <bool LIN, int P>
-__device__ __forceinline__ void build_a_part(unsigned char *a_tile, int row, float x, float y, float z) {
+// A point's A row: all K/8 16-byte chunks (8 slots each).
+template <bool LIN>
+__device__ __forceinline__ void build_a_row(unsigned char *a_tile, int row, float x, float y, float z) {
     using S = TcScheme<LIN>;
     const float yx = y * x, yz = y * z, xz = x * z, yy = y * y, xx = x * x, zz = z * z;
     const float m[20] = {1.0f,   y,      x,      z,      yx,     yz,     xz,     yy,     xx,     zz,
                          yx * z, yy * y, y * xx, y * zz, yy * x, xx * x, x * zz, yy * z, xx * z, zz * z};
 #pragma unroll
-    for (int c = P; c < S::kK / 8; c += kTcGroups) {
+    for (int c = 0; c < S::kK / 8; ++c) {
         unsigned words[4];
 #pragma unroll
         for (int wd = 0; wd < 4; ++wd) {
@@ -240,40 +261,107 @@ __device__ __forceinline__ float quotient_fast(float num, float den) {
     return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
 }
 
+// The epilogue of one tile for one warp: its lanes are 32 points of the tile (the TMEM
+// lanes of the warp's quarter), its cameras [c_begin, c_end) those of its warpgroup, taken
+// CH at a time (CH even: a tcgen05.ld of 8 columns covers two cameras).
+template <bool LIN, int CH>
+__device__ __forceinline__ void tc_epilogue(unsigned lane_base, int c_begin, int c_end, long long p, long long n,
+                                            float px, float py, float pz, const float2 *sden, const float4 *slin,
+                                            float *__restrict__ out) {
+    constexpr int kE = 2 * CH;                     // (camera, plane) entries of a chunk
+    for (int cb = c_begin; cb < c_end; cb += CH) {
+        unsigned r[CH / 2][8];
+#pragma unroll
+        for (int j = 0; j < CH / 2; ++j)
+            if (cb + 2 * j < c_end) tmem_ld8(lane_base + 4 * (cb + 2 * j), r[j]);   // warp-uniform
+        tmem_wait();
+        // quotients of the chunk's cameras, branch-free; one warp-uniform check sends rare
+        // operands to IEEE division.  Columns of cameras past c_end (an odd last pair) are
+        // computed and dropped.
+        const int nc = min(CH, c_end - cb);
+        float num[kE], den[kE], q[kE];
+        bool ok = true;
+#pragma unroll
+        for (int e = 0; e < kE; ++e) {
+            const int j = e >> 2, h = (e >> 1) & 1, pl = e & 1;
+            float nu = __uint_as_float(r[j][4 * h + 2 * pl]);
+            float de = __uint_as_float(r[j][4 * h + 2 * pl + 1]);
+            if (LIN) {
+                const float4 *lc = slin + 4 * (cb + (e >> 1)) + 2 * pl;   // within slin's 64 cameras
+                nu = add_linear(nu, lc[0], px, py, pz);
+                de = add_linear(de, lc[1], px, py, pz);
+            }
+            num[e] = nu;
+            den[e] = de;
+            q[e] = quotient_fast(nu, de);
+            if ((e >> 1) < nc) ok = ok && quotient_fast_ok(nu, de);
+        }
+        if (__builtin_expect(!__all_sync(0xffffffffu, ok), 0)) {
+#pragma unroll
+            for (int e = 0; e < kE; ++e)
+                if (!quotient_fast_ok(num[e], den[e])) q[e] = tc_quotient_ieee(num[e], den[e]);
+        }
+        if (p < n) {
+            float *o = out + (2LL * cb) * n + p;     // plane 2 cb, then one plane per entry
+#pragma unroll
+            for (int e = 0; e < kE; ++e, o += n) {
+                if ((e >> 1) < nc) {
+                    const float2 dn = sden[2 * cb + e];
+                    __stcs(o, __fmaf_rn(q[e], dn.x, dn.y));
+                }
+            }
+        }
+    }
+}
+
 template <bool LIN>
 __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__restrict__ xyz, long long n, int n_cams,
                                                                int n_pad, CubeTcWs w, float *__restrict__ out,
                                                                unsigned wait_limit) {
     using S = TcScheme<LIN>;
+    constexpr unsigned kStageBytes = kTcTile * S::kRowBytes;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sb = smem;                                           // B: n_pad x K
-    unsigned char *sa0 = sb + kTcMaxN * S::kRowBytes;                   // A buffers: 128 x K each, adjacent
-    float2 *sden = reinterpret_cast<float2 *>(sb + (kTcMaxN + 2 * kTcTile) * S::kRowBytes);
+    unsigned char *sa = sb + kTcMaxN * S::kRowBytes;                    // A ring: kTcStages x 128 x K
+    float2 *sden = reinterpret_cast<float2 *>(sa + kTcStages * kStageBytes);
     float4 *slin = reinterpret_cast<float4 *>(sden + 2 * kTcMaxCams);
-    __shared__ __align__(8) unsigned long long bar_mma[2], bar_b, bar_drain;
+    // mbarriers: A full / empty per stage, accumulator full / empty, B landed, final drain
+    __shared__ __align__(8) unsigned long long bars[2 * kTcStages + 6];
     __shared__ unsigned tmem_base;
-    const int tid = threadIdx.x, warp = tid >> 5, quad = warp & 3, lane = tid & 31, grp = tid >> 7;
+    __shared__ volatile int abort_flag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned bar0 = smem_addr(&bars[0]);
+    auto a_full = [&](int st) { return bar0 + 8u * st; };
+    auto a_empty = [&](int st) { return bar0 + 8u * (kTcStages + st); };
+    auto acc_full = [&](int a) { return bar0 + 8u * (2 * kTcStages + a); };
+    auto acc_empty = [&](int a) { return bar0 + 8u * (2 * kTcStages + 2 + a); };
+    const unsigned bar_b = bar0 + 8u * (2 * kTcStages + 4), bar_drain = bar0 + 8u * (2 * kTcStages + 5);
     const unsigned b_bytes = static_cast<unsigned>(n_pad * S::kRowBytes);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_mma[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_mma[1])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_b)) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar_drain)) : "memory");
+        for (int st = 0; st < kTcStages; ++st) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a_full(st)), "r"(kTcProducerWarps * 32) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a_empty(st)) : "memory");
+        }
+        for (int a = 0; a < 2; ++a) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(acc_full(a)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(acc_empty(a)), "r"(kTcEpiWarps) : "memory");
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_b) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_drain) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        abort_flag = 0;
         // B into shared memory by the bulk-copy engine (16-byte aligned, size a multiple of 16)
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&bar_b)), "r"(b_bytes)
-                     : "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_b), "r"(b_bytes) : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                 smem_addr(sb)),
-            "l"(w.b), "r"(b_bytes), "r"(smem_addr(&bar_b))
+            "l"(w.b), "r"(b_bytes), "r"(bar_b)
             : "memory");
     }
     for (int i = tid; i < 2 * n_cams; i += kTcThreads) sden[i] = w.den[i];
     if (LIN)
         for (int i = tid; i < 4 * n_cams; i += kTcThreads) slin[i] = w.lin[i];
-    __syncwarp();
-    if (warp == 0) {
+    if (warp == kTcMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
                      "r"(kTcTmemCols)
                      : "memory");
@@ -283,140 +371,136 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = tmem_base;
-    bool failed = !mbar_wait_bounded(smem_addr(&bar_b), 0, wait_limit);
-    const unsigned idesc = umma_idesc_bf16(n_pad);
-    const unsigned sbo = static_cast<unsigned>(S::kK / 8 * 128);
-    const unsigned b_base = smem_addr(sb);
     const long long tiles = (n + kTcTile - 1) / kTcTile;
-    // this warpgroup's cameras: [c_begin, c_end), boundaries even (8-column TMEM loads)
-    const int c_begin = min(((grp * n_cams / kTcGroups) + 1) & ~1, n_cams);
-    const int c_end = min((((grp + 1) * n_cams / kTcGroups) + 1) & ~1, n_cams);
-    // this thread builds part `grp` of row `row` and finishes the same point: row = TMEM lane
-    const int row = quad * 32 + lane;
-    float px = 0.0f, py = 0.0f, pz = 0.0f;       // the previous tile's point (LIN epilogue)
-    float nx = 0.0f, ny = 0.0f, nz = 0.0f;       // this tile's point, loaded one iteration ahead
-    {
-        const long long p = static_cast<long long>(blockIdx.x) * kTcTile + row;
-        if (p < n) {
-            nx = __ldg(xyz + p);
-            ny = __ldg(xyz + n + p);
-            nz = __ldg(xyz + 2 * n + p);
-        }
-    }
-    long long prev_tile = -1;
-    int k = 0;
-    for (long long tile = blockIdx.x;; tile += gridDim.x, ++k) {
-        const bool have = tile < tiles;
-        const int buf = k & 1;
-        const float cx = nx, cy = ny, cz = nz;
-        if (have && !failed) {
-            unsigned char *a_tile = sa0 + buf * (kTcTile * S::kRowBytes);
-            switch (grp) {
-                case 0: build_a_part<LIN, 0>(a_tile, row, cx, cy, cz); break;
-                case 1: build_a_part<LIN, 1>(a_tile, row, cx, cy, cz); break;
-                case 2: build_a_part<LIN, 2>(a_tile, row, cx, cy, cz); break;
-                default: build_a_part<LIN, 3>(a_tile, row, cx, cy, cz); break;
+    const long long my_tiles = tiles > blockIdx.x ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    bool failed = false;
+    if (warp < kTcProducerWarps) {
+        // ---- producers: thread t builds rows t and t + 64 of every tile's A operand
+        constexpr int kRows = kTcTile / (32 * kTcProducerWarps);
+        float nx[kRows], ny[kRows], nz[kRows];
+#pragma unroll
+        for (int h = 0; h < kRows; ++h) {
+            const long long p = static_cast<long long>(blockIdx.x) * kTcTile + tid + 32 * kTcProducerWarps * h;
+            nx[h] = ny[h] = nz[h] = 0.0f;
+            if (p < n) {
+                nx[h] = __ldg(xyz + p);
+                ny[h] = __ldg(xyz + n + p);
+                nz[h] = __ldg(xyz + 2 * n + p);
             }
-            // the next tile's point, in flight during this iteration's epilogue
-            const long long p = (tile + gridDim.x) * kTcTile + row;
-            nx = ny = nz = 0.0f;
+        }
+        for (long long k = 0; k < my_tiles; ++k) {
+            const int st = static_cast<int>(k % kTcStages);
+            const unsigned ph = static_cast<unsigned>((k / kTcStages) & 1);
+            float cx[kRows], cy[kRows], cz[kRows];
+#pragma unroll
+            for (int h = 0; h < kRows; ++h) {
+                cx[h] = nx[h];
+                cy[h] = ny[h];
+                cz[h] = nz[h];
+                const long long p = (blockIdx.x + (k + 1) * gridDim.x) * kTcTile + tid + 32 * kTcProducerWarps * h;
+                nx[h] = ny[h] = nz[h] = 0.0f;                // the next tile's points, in flight meanwhile
+                if (p < n) {
+                    nx[h] = __ldg(xyz + p);
+                    ny[h] = __ldg(xyz + n + p);
+                    nz[h] = __ldg(xyz + 2 * n + p);
+                }
+            }
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_abortable(a_empty(st), ph ^ 1u, wait_limit, &abort_flag));
+            if (!ok) {
+                failed = true;
+                break;
+            }
+#pragma unroll
+            for (int h = 0; h < kRows; ++h)
+                build_a_row<LIN>(sa + st * kStageBytes, tid + 32 * kTcProducerWarps * h, cx[h], cy[h], cz[h]);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the tensor cores
+            mbar_arrive(a_full(st));
+        }
+    } else if (warp == kTcMmaWarp) {
+        // ---- MMA issuer (lane 0)
+        if (lane == 0) {
+            const unsigned idesc = umma_idesc_bf16(n_pad);
+            const unsigned sbo = static_cast<unsigned>(S::kK / 8 * 128);
+            const unsigned b_base = smem_addr(sb), a_base0 = smem_addr(sa);
+            failed = !mbar_wait_abortable(bar_b, 0, wait_limit, &abort_flag);
+            for (long long k = 0; !failed && k < my_tiles; ++k) {
+                const int st = static_cast<int>(k % kTcStages), acc = static_cast<int>(k & 1);
+                const unsigned ph = static_cast<unsigned>((k / kTcStages) & 1), aph = static_cast<unsigned>((k >> 1) & 1);
+                if (!mbar_wait_abortable(a_full(st), ph, wait_limit, &abort_flag) ||
+                    !mbar_wait_abortable(acc_empty(acc), aph ^ 1u, wait_limit, &abort_flag)) {
+                    failed = true;
+                    break;
+                }
+                tc_fence_after();
+                const unsigned d = tmem + static_cast<unsigned>(acc * 256);
+                const unsigned a_base = a_base0 + static_cast<unsigned>(st) * kStageBytes;
+#pragma unroll
+                for (int ks = 0; ks < S::kK / 16; ++ks)
+                    umma_bf16(d, umma_desc(a_base + ks * 256, 128, sbo), umma_desc(b_base + ks * 256, 128, sbo), idesc,
+                              ks > 0 ? 1u : 0u);
+                umma_commit(a_empty(st));          // the stage is free once these MMAs have read it
+                umma_commit(acc_full(acc));        // and the accumulator holds the tile
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp e handles TMEM lane quarter (warp % 4) for camera group e / 4
+        const int e = warp - kTcProducerWarps - 1, quad = warp & 3, grp = e >> 2;
+        const int c_begin = min(((grp * n_cams / kTcGroups) + 1) & ~1, n_cams);
+        const int c_end = min((((grp + 1) * n_cams / kTcGroups) + 1) & ~1, n_cams);
+        const int row = quad * 32 + lane;
+        float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+        if (LIN) {
+            const long long p = static_cast<long long>(blockIdx.x) * kTcTile + row;
             if (p < n) {
                 nx = __ldg(xyz + p);
                 ny = __ldg(xyz + n + p);
                 nz = __ldg(xyz + 2 * n + p);
             }
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        tc_fence_before();
-        const bool any_failed = __syncthreads_or(failed) != 0;
-        tc_fence_after();
-        if (any_failed) {
-            failed = true;
-            break;
-        }
-        if (have && tid == 0) {
-            const unsigned d = tmem + static_cast<unsigned>(buf * 256);
-            const unsigned a_base = smem_addr(sa0) + static_cast<unsigned>(buf * kTcTile * S::kRowBytes);
-#pragma unroll
-            for (int ks = 0; ks < S::kK / 16; ++ks)
-                umma_bf16(d, umma_desc(a_base + ks * 256, 128, sbo), umma_desc(b_base + ks * 256, 128, sbo), idesc,
-                          ks > 0 ? 1u : 0u);
-            umma_commit(smem_addr(&bar_mma[buf]));
-        }
-        // ---- epilogue of the previous tile (the other accumulator) ----
-        if (prev_tile >= 0) {
-            const int pb = buf ^ 1;
-            const unsigned parity = static_cast<unsigned>(((k - 1) >> 1) & 1);
-            if (!mbar_wait_bounded(smem_addr(&bar_mma[pb]), parity, wait_limit)) {
-                failed = true;
-            } else {
-                tc_fence_after();
-                const long long p = prev_tile * kTcTile + row;
-                const unsigned lane_base = tmem + (static_cast<unsigned>(quad * 32) << 16) + static_cast<unsigned>(pb * 256);
-                for (int cb = c_begin; cb < c_end; cb += 8) {
-                    unsigned r[4][8];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (cb + 2 * j < c_end) tmem_ld8(lane_base + 4 * (cb + 2 * j), r[j]);   // warp-uniform
-                    tmem_wait();
-                    // quotients of the chunk's cameras, branch-free; one warp-uniform check
-                    // sends rare operands to IEEE division.  Columns of cameras past c_end
-                    // (an odd last pair) are computed and dropped.
-                    const int nc = min(8, c_end - cb);
-                    float num[16], den[16], q[16];
-                    bool ok = true;
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) {
-                        const int j = e >> 2, h = (e >> 1) & 1, pl = e & 1;
-                        float nu = __uint_as_float(r[j][4 * h + 2 * pl]);
-                        float de = __uint_as_float(r[j][4 * h + 2 * pl + 1]);
-                        if (LIN) {
-                            const float4 *lc = slin + 4 * (cb + (e >> 1)) + 2 * pl;   // within slin's 64 cameras
-                            nu = add_linear(nu, lc[0], px, py, pz);
-                            de = add_linear(de, lc[1], px, py, pz);
-                        }
-                        num[e] = nu;
-                        den[e] = de;
-                        q[e] = quotient_fast(nu, de);
-                        if ((e >> 1) < nc) ok = ok && quotient_fast_ok(nu, de);
-                    }
-                    if (__builtin_expect(!__all_sync(0xffffffffu, ok), 0)) {
-#pragma unroll
-                        for (int e = 0; e < 16; ++e)
-                            if (!quotient_fast_ok(num[e], den[e])) q[e] = tc_quotient_ieee(num[e], den[e]);
-                    }
-                    if (p < n) {
-                        float *o = out + (2LL * cb) * n + p;     // plane 2 cb, then one plane per entry
-#pragma unroll
-                        for (int e = 0; e < 16; ++e, o += n) {
-                            if ((e >> 1) < nc) {
-                                const float2 dn = sden[2 * cb + e];
-                                __stcs(o, __fmaf_rn(q[e], dn.x, dn.y));
-                            }
-                        }
-                    }
+        for (long long k = 0; k < my_tiles; ++k) {
+            const int acc = static_cast<int>(k & 1);
+            const unsigned aph = static_cast<unsigned>((k >> 1) & 1);
+            const long long tile = blockIdx.x + k * gridDim.x;
+            const float cx = nx, cy = ny, cz = nz;
+            if (LIN) {
+                const long long p = (tile + gridDim.x) * kTcTile + row;   // next tile's point
+                nx = ny = nz = 0.0f;
+                if (p < n) {
+                    nx = __ldg(xyz + p);
+                    ny = __ldg(xyz + n + p);
+                    nz = __ldg(xyz + 2 * n + p);
                 }
             }
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_abortable(acc_full(acc), aph, wait_limit, &abort_flag));
+            if (!ok) {
+                failed = true;
+                break;
+            }
+            tc_fence_after();
+            const unsigned lane_base = tmem + (static_cast<unsigned>(quad * 32) << 16) + static_cast<unsigned>(acc * 256);
+            tc_epilogue<LIN, 4>(lane_base, c_begin, c_end, tile * kTcTile + row, n, cx, cy, cz, sden, slin, out);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty(acc));
         }
-        if (!have) break;
-        prev_tile = tile;
-        px = cx;
-        py = cy;
-        pz = cz;
     }
-    if (failed && tid == 0) atomicExch(w.err, 1);
+    if (failed) {
+        abort_flag = 1;
+        atomicExch(w.err, 1);
+    }
     // the coefficient copy and every committed MMA have completed before the CTA's shared
     // and tensor memory are released (bounded waits, full limit)
     tc_fence_before();
     __syncthreads();
-    if (tid == 0) {
-        mbar_wait_bounded(smem_addr(&bar_b), 0);
-        umma_commit(smem_addr(&bar_drain));
-        mbar_wait_bounded(smem_addr(&bar_drain), 0);
+    if (tid == kTcMmaWarp * 32) {
+        mbar_wait_bounded(bar_b, 0);
+        umma_commit(bar_drain);
+        mbar_wait_bounded(bar_drain, 0);
     }
     __syncthreads();
     tc_fence_after();
-    if (warp == 0)
+    if (warp == kTcMmaWarp)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
 }
 
@@ -424,7 +508,7 @@ template <bool LIN>
 size_t cube_tc_smem() {
     using S = TcScheme<LIN>;
     // at least half of the SM's shared memory: one CTA per SM, which owns all 512 TMEM columns
-    const size_t need = static_cast<size_t>(kTcMaxN + 2 * kTcTile) * S::kRowBytes + sizeof(float2) * 2 * kTcMaxCams +
+    const size_t need = static_cast<size_t>(kTcMaxN + kTcStages * kTcTile) * S::kRowBytes + sizeof(float2) * 2 * kTcMaxCams +
                         sizeof(float4) * 4 * kTcMaxCams + 1024;
     return std::max<size_t>(need, 120 * 1024);
 }

@@ -52,6 +52,10 @@ struct Axis {
     int shift;                   // d >> shift < 2^32
     float scale;                 // 2^shift * ulp(off) / res, so that q ~ (d >> shift) * scale
     float err_abs, err_rel;      // bound of |q - d * ulp / res|: err_abs + err_rel * q
+    // integer estimate: umulhi(d >> shift, mul) ~ q * 2^fbits; its fraction f (low fbits
+    // bits) proves the row when 4 <= f <= 2^fbits - 5
+    unsigned mul, fmask, fsure;
+    int fbits;
     int neg;                     // off < 0
     int dir;
     int fast;                    // fast path usable
@@ -217,7 +221,38 @@ struct FastAxis {
     unsigned top12;
     int shift, nm1;
     float scale, err_abs, err_rel;
+    unsigned mul, fmask, fsure;
+    int fbits;
 };
+
+FastAxis fast_axis_of(const Axis &ax) {
+    FastAxis fa;
+    memcpy(&fa.off_bits, &ax.off, sizeof(long long));
+    fa.tmax = ax.tmax;
+    fa.thr = ax.thr;
+    fa.top12 = ax.top12;
+    fa.shift = ax.shift;
+    fa.nm1 = static_cast<int>(ax.n - 1);
+    fa.scale = ax.scale;
+    fa.err_abs = ax.err_abs;
+    fa.err_rel = ax.err_rel;
+    fa.mul = ax.mul;
+    fa.fmask = ax.fmask;
+    fa.fsure = ax.fsure;
+    fa.fbits = ax.fbits;
+    return fa;
+}
+
+// Row from u = d >> shift by one 32-bit multiply-high: hi = floor(u * mul / 2^32) is the
+// quotient q = d * ulp / res in units of 2^-fbits cells, within [-0.5, 1.5) units plus
+// the reference's own FP64 rounding (2^-21 units); so when its fraction f = hi mod 2^fbits
+// keeps 4 units from both cell boundaries, hi >> fbits is the reference's
+// floor(fl(d * ulp / res)).  Integer multiply and logic only (no conversion, no FP32).
+__device__ __forceinline__ void axis_estimate(const FastAxis &a, unsigned u, int &r, bool &sure) {
+    const unsigned hi = __umulhi(u, a.mul);
+    r = static_cast<int>(hi >> a.fbits);
+    sure = ((hi & a.fmask) - 4u) < a.fsure;
+}
 
 template <bool FLIP>   // FLIP: d = off - v (rows of a positive origin, columns of a negative one)
 __device__ __forceinline__ bool axis_fast(const FastAxis &a, long long bv, int &r, long long &d, bool &sure) {
@@ -251,13 +286,7 @@ __device__ __forceinline__ bool axis_contained(const FastAxis &a, long long bv, 
                                        : static_cast<unsigned long long>(bv) - static_cast<unsigned long long>(a.off_bits);
     d = static_cast<long long>(ud);
     const bool ok = ud < static_cast<unsigned long long>(a.tmax);
-    const unsigned u = static_cast<unsigned>(ud >> a.shift);
-    const float q = __fmul_rn(__uint2float_rn(u), a.scale);
-    const float big = __fadd_rn(q, 12582912.0f);
-    const float fr = __fsub_rn(q, __fsub_rn(big, 12582912.0f));
-    const int rn = static_cast<int>(static_cast<unsigned>(__float_as_int(big)) - 0x4b400000u);
-    r = min(max(rn - (fr < 0.0f ? 1 : 0), 0), a.nm1);
-    sure = fabsf(fr) > __fmaf_rn(a.err_rel, q, a.err_abs);
+    axis_estimate(a, static_cast<unsigned>(ud >> a.shift), r, sure);   // r <= nm1 when ok && sure
     return ok;
 }
 
@@ -296,9 +325,50 @@ __device__ __forceinline__ void load_block(const long long *__restrict__ bits, l
     }
 }
 
-// Grid-stride over blocks of kFastPts consecutive points: each point's cell from its
-// coordinates' bit patterns (32-bit cell indices: the grid holds < 2^31 cells), runs of
+// The kFastPts consecutive points of one thread starting at index i: each point's cell from
+// its coordinates' bit patterns (32-bit cell indices: the grid holds < 2^31 cells), runs of
 // consecutive points in one cell merged before the 64-bit atomicMax of their keys.
+template <bool FLIP_ROW, bool FLIP_COL>
+__device__ __forceinline__ void bin_fast_block(const long long *__restrict__ bits, long long i, long long end,
+                                               const FastAxis &R, const FastAxis &C, unsigned ncols,
+                                               unsigned long long tag, unsigned long long *__restrict__ vk,
+                                               unsigned long long *__restrict__ first) {
+    PointBlock b;
+    load_block(bits, i, end, b);
+    unsigned cell[kFastPts];
+    unsigned long long key[kFastPts];
+    bool okk[kFastPts];
+#pragma unroll
+    for (int k = 0; k < kFastPts; ++k) {
+        const unsigned long long zb = static_cast<unsigned long long>(b.w[3 * k + 2]);
+        int r, c;
+        long long dr, dc;
+        bool sr, sc;
+        bool ok = axis_contained<FLIP_ROW>(R, b.w[3 * k + 1], r, dr, sr);
+        ok &= axis_contained<FLIP_COL>(C, b.w[3 * k], c, dc, sc);
+        ok &= !is_nan_bits(zb);
+        if (ok && !sr) r = axis_correct(R.thr, min(r, R.nm1), dr);
+        if (ok && !sc) c = axis_correct(C.thr, min(c, C.nm1), dc);
+        const unsigned cl = static_cast<unsigned>(r) * ncols + static_cast<unsigned>(c);
+        const bool zero = (zb << 1) == 0;
+        if (ok && zero) atomicMax(first + cl, tag | (kIdxMask - static_cast<unsigned long long>(i + k)));
+        const unsigned long long kz = (zb >> 63) ? ~zb : (zb | 0x8000000000000000ull);
+        key[k] = ok ? (zero ? kZeroKey : kz) : kEmptyKey;
+        cell[k] = cl;
+        okk[k] = ok;
+    }
+#pragma unroll
+    for (int k = 1; k < kFastPts; ++k) {     // merge runs of consecutive points in one cell
+        const bool same = okk[k] & okk[k - 1] & (cell[k] == cell[k - 1]);
+        key[k] = same ? max(key[k], key[k - 1]) : key[k];
+        key[k - 1] = same ? kEmptyKey : key[k - 1];
+    }
+#pragma unroll
+    for (int k = 0; k < kFastPts; ++k)
+        if (key[k] != kEmptyKey) atomicMax(vk + cell[k], key[k]);
+}
+
+// Grid-stride over blocks of kFastPts consecutive points.
 template <bool FLIP_ROW, bool FLIP_COL>
 __global__ void __launch_bounds__(256) bin_fast_kernel(const double *__restrict__ pts,
                                                        const long long *__restrict__ offsets, int v,
@@ -313,41 +383,8 @@ __global__ void __launch_bounds__(256) bin_fast_kernel(const double *__restrict_
     const unsigned ncols = static_cast<unsigned>(C.nm1 + 1);
     const long long *bits = reinterpret_cast<const long long *>(pts);
     for (long long i = begin + (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) * kFastPts; i < end;
-         i += stride) {
-        PointBlock b;
-        load_block(bits, i, end, b);
-        unsigned cell[kFastPts];
-        unsigned long long key[kFastPts];
-        bool okk[kFastPts];
-#pragma unroll
-        for (int k = 0; k < kFastPts; ++k) {
-            const unsigned long long zb = static_cast<unsigned long long>(b.w[3 * k + 2]);
-            int r, c;
-            long long dr, dc;
-            bool sr, sc;
-            bool ok = axis_contained<FLIP_ROW>(R, b.w[3 * k + 1], r, dr, sr);
-            ok &= axis_contained<FLIP_COL>(C, b.w[3 * k], c, dc, sc);
-            ok &= !is_nan_bits(zb);
-            if (ok && !sr) r = axis_correct(R.thr, r, dr);
-            if (ok && !sc) c = axis_correct(C.thr, c, dc);
-            const unsigned cl = static_cast<unsigned>(r) * ncols + static_cast<unsigned>(c);
-            const bool zero = (zb << 1) == 0;
-            if (ok && zero) atomicMax(first + cl, tag | (kIdxMask - static_cast<unsigned long long>(i + k)));
-            const unsigned long long kz = (zb >> 63) ? ~zb : (zb | 0x8000000000000000ull);
-            key[k] = ok ? (zero ? kZeroKey : kz) : kEmptyKey;
-            cell[k] = cl;
-            okk[k] = ok;
-        }
-#pragma unroll
-        for (int k = 1; k < kFastPts; ++k) {     // merge runs of consecutive points in one cell
-            const bool same = okk[k] & okk[k - 1] & (cell[k] == cell[k - 1]);
-            key[k] = same ? max(key[k], key[k - 1]) : key[k];
-            key[k - 1] = same ? kEmptyKey : key[k - 1];
-        }
-#pragma unroll
-        for (int k = 0; k < kFastPts; ++k)
-            if (key[k] != kEmptyKey) atomicMax(vk + cell[k], key[k]);
-    }
+         i += stride)
+        bin_fast_block<FLIP_ROW, FLIP_COL>(bits, i, end, R, C, ncols, tag, vk, first);
 }
 
 // Key of a cell's nanmax with the zero sign resolved (0 = empty cell).
@@ -704,6 +741,81 @@ __global__ void __launch_bounds__(TX *TY) dsm_epilogue_kernel(
     epilogue_tile(vk, PointsZeroDecoder{first, pts}, out, next_keys, H, W, blockIdx.y * TILE_Y, blockIdx.x * TX, sm);
 }
 
+// ---- pipelined rasterisation: view v's binning and view v-1's epilogue in one launch -----
+// The binning streams the points from HBM and waits on loads; the epilogue works on an
+// L2-resident key grid and is issue-bound.  Launched one after the other they barely
+// overlap (the binning's resident wave fills every SM until its tail), so one launch
+// carries both: its work items -- chunks of view v's points and 32x32 tiles of view v-1's
+// epilogue, interleaved evenly -- are handed out by a device counter, so every SM runs a
+// mix of both kinds until the launch drains.  The epilogue's inputs (view v-1's key grid
+// and first-zero words) were completed by the previous launch on the same stream; nothing
+// waits on another CTA.
+constexpr int kChunkIters = 8;                                   // blocks of kFastPts points per thread
+constexpr long long kChunkPoints = 1LL * TX * TY * kFastPts * kChunkIters;
+
+struct PipeBin {          // view v's binning (active = 0: none)
+    const long long *offsets;
+    int v, active;
+    FastAxis row, col;
+    unsigned long long *keys, *first;
+};
+
+struct PipeEpi {          // view v-1's epilogue (n_tiles = 0: none)
+    const unsigned long long *keys, *first;
+    float *out;
+    unsigned long long *clear;   // the key grid of view v+1, cleared tile by tile
+    int H, W, tiles_x;
+    long long n_tiles;
+};
+
+// MINB: resident CTAs per SM the registers are budgeted for (6: 40 registers, 5: 48).
+template <bool FLIP_ROW, bool FLIP_COL, int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB) raster_pipe_kernel(const double *__restrict__ pts, PipeBin bin,
+                                                                    PipeEpi epi, unsigned *__restrict__ counter) {
+    __shared__ EpilogueSmem sm;
+    __shared__ long long item_sh[2];
+    const int tid = threadIdx.y * TX + threadIdx.x;
+    const long long *bits = reinterpret_cast<const long long *>(pts);
+    long long begin = 0, end = 0;
+    if (bin.active) {
+        begin = bin.offsets[bin.v];
+        end = bin.offsets[bin.v + 1];
+    }
+    const long long n_chunks = end > begin ? (end - begin + kChunkPoints - 1) / kChunkPoints : 0;
+    const long long total = n_chunks + epi.n_tiles;
+    const unsigned long long tag = epoch_tag(bin.v);
+    const unsigned ncols = static_cast<unsigned>(bin.col.nm1 + 1);
+    for (int it = 0;; ++it) {
+        // thread 0 fetches the next item and classifies it: tiles sit at the items where
+        // floor(item * n_tiles / total) steps, chunks in between (encoded as -1 - chunk)
+        if (tid == 0) {
+            const long long item = atomicAdd(counter, 1u);
+            long long code = total;                       // done
+            if (item < total) {
+                const long long t0 = item * epi.n_tiles / total, t1 = (item + 1) * epi.n_tiles / total;
+                code = t1 > t0 ? t0 : -1 - (item - t0);
+            }
+            item_sh[it & 1] = code;
+        }
+        __syncthreads();    // also ends the previous item's use of the shared tile
+        const long long code = item_sh[it & 1];
+        if (code >= total) break;
+        if (code >= 0) {
+            const int ty = static_cast<int>(code / epi.tiles_x), tx = static_cast<int>(code - static_cast<long long>(ty) * epi.tiles_x);
+            epilogue_tile(epi.keys, PointsZeroDecoder{epi.first, pts}, epi.out, epi.clear, epi.H, epi.W, ty * TILE_Y,
+                          tx * TX, sm);
+        } else {
+            const long long c0 = begin + (-1 - code) * kChunkPoints;
+#pragma unroll 1
+            for (int k = 0; k < kChunkIters; ++k) {
+                const long long i = c0 + (static_cast<long long>(k) * (TX * TY) + tid) * kFastPts;
+                if (i < end) bin_fast_block<FLIP_ROW, FLIP_COL>(bits, i, end, bin.row, bin.col, ncols, tag, bin.keys,
+                                                                bin.first);
+            }
+        }
+    }
+}
+
 // ---- host side --------------------------------------------------------------------------
 // Host copy of the threshold search of axis_thresholds_kernel (same IEEE FP64 expression).
 long long host_threshold(long long r, double ulp, double res) {
@@ -732,6 +844,8 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
     ax.scale = 0.f;
     ax.err_abs = ax.err_rel = 0.f;
     ax.tmax = 0;
+    ax.mul = ax.fmask = ax.fsure = 0;
+    ax.fbits = 0;
     // the FP32 estimate needs cell indices below 2^22 and sane resolutions
     if (!(e >= 1 && e <= 2046 && isfinite(res) && res >= 1e-9 && res <= 1e9 && n < (1LL << 22))) return VS_OK;
     const double ulp = ldexp(1.0, static_cast<int>(e) - 1075);
@@ -747,6 +861,20 @@ int make_axis(Axis &ax, double off, double res, long long n, int dir, long long 
     ax.err_abs = static_cast<float>(1.01 * scale + 1e-9);
     ax.err_rel = static_cast<float>(4.0 * ldexp(1.0, -24));
     ax.tmax = host_threshold(n, ulp, res);
+    // integer estimate: mul = round(scale * 2^(32 + fbits)) in [2^31, 2^32]
+    int ke = 0;
+    frexp(scale, &ke);                               // scale = m * 2^ke, m in [0.5, 1)
+    int fb = -ke;
+    double m = nearbyint(ldexp(scale, 32 + fb));
+    if (m >= 4294967296.0) {
+        --fb;
+        m = nearbyint(ldexp(scale, 32 + fb));
+    }
+    if (fb < 4 || fb > 31 || m < 2147483648.0 || m >= 4294967296.0) return VS_OK;   // (cannot happen for n < 2^22)
+    ax.mul = static_cast<unsigned>(m);
+    ax.fbits = fb;
+    ax.fmask = (1u << fb) - 1u;
+    ax.fsure = (1u << fb) - 8u;
     ax.fast = 1;
     // the grid spans off .. off -/+ (n + 2) * res; contained when both ends keep off's sign
     // and exponent, so that any point with another sign/exponent lies >= 2 cells outside
@@ -793,6 +921,16 @@ int make_tables(double xoff, double yoff, double xres, double yres, long long xs
 // vs_set_binning_ctas_per_sm.
 int g_bin_ctas_per_sm = 0;
 
+// Both axes on the contained fast path and 32-bit cell indices: bin_fast_kernel applies.
+bool fast_binning(const Tables &tb) {
+    return tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained && tb.row.n * tb.col.n < (1LL << 31);
+}
+
+void fast_axes(const Tables &tb, FastAxis fa[2]) {
+    fa[0] = fast_axis_of(tb.row);
+    fa[1] = fast_axis_of(tb.col);
+}
+
 int bin_launch(const double *points, const long long *offsets, int v, long long single_n, long long max_points,
                const Tables &tb, unsigned long long *keys, unsigned long long *first, cudaStream_t st) {
     if (max_points <= 0) return VS_OK;
@@ -800,20 +938,9 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
     long long want = ceil_div(ceil_div(max_points, kPts), threads);
     long long cap = static_cast<long long>(sm_count()) * 8;
     unsigned gx = static_cast<unsigned>(std::max(1LL, std::min(want, cap)));
-    if (tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained && tb.row.n * tb.col.n < (1LL << 31)) {
+    if (fast_binning(tb)) {
         FastAxis fa[2];
-        const Axis *ax[2] = {&tb.row, &tb.col};
-        for (int a = 0; a < 2; ++a) {
-            memcpy(&fa[a].off_bits, &ax[a]->off, sizeof(long long));
-            fa[a].tmax = ax[a]->tmax;
-            fa[a].thr = ax[a]->thr;
-            fa[a].top12 = ax[a]->top12;
-            fa[a].shift = ax[a]->shift;
-            fa[a].nm1 = static_cast<int>(ax[a]->n - 1);
-            fa[a].scale = ax[a]->scale;
-            fa[a].err_abs = ax[a]->err_abs;
-            fa[a].err_rel = ax[a]->err_rel;
-        }
+        fast_axes(tb, fa);
         // rows: a = off - v unless the origin is negative; columns: a = v - off unless negative
         const bool flip_row = !tb.row.neg, flip_col = tb.col.neg != 0;
         // one wave of resident CTAs (grid-stride): a partial second wave would leave most
@@ -945,12 +1072,7 @@ struct MapTileSmem {
 // drops any row or column outside it, and the rare correction clamps first.
 __device__ __forceinline__ bool axis_tile(const FastAxis &a, long long d, int &r, bool &sure) {
     const bool ok = static_cast<unsigned long long>(d) < static_cast<unsigned long long>(a.tmax);
-    const unsigned u = static_cast<unsigned>(static_cast<unsigned long long>(d) >> a.shift);
-    const float q = __fmul_rn(__uint2float_rn(u), a.scale);
-    const float big = __fadd_rn(q, 12582912.0f);
-    const float fr = __fsub_rn(q, __fsub_rn(big, 12582912.0f));
-    r = static_cast<int>(static_cast<unsigned>(__float_as_int(big)) - 0x4b400000u) - (fr < 0.0f ? 1 : 0);
-    sure = fabsf(fr) > __fmaf_rn(a.err_rel, q, a.err_abs);
+    axis_estimate(a, static_cast<unsigned>(static_cast<unsigned long long>(d) >> a.shift), r, sure);
     return ok;
 }
 
@@ -1598,6 +1720,138 @@ extern "C" int vs_dsm_from_points_overlap(const double *points, const int64_t *o
     return VS_OK;
 }
 
+// Pipelined form: launch v (v = 0..V) bins view v and runs view v-1's epilogue
+// (raster_pipe_kernel), all on one stream.  Key grids rotate as in the overlapped form:
+// bin(v) fills K[v%3]; epilogue(v-1) reads K[(v-1)%3] and clears K[(v+1)%3], which
+// epilogue(v-2) finished reading in the previous launch; the first-zero words alternate.
+// One counter per launch (cleared once per call) hands out the work items.
+template <int MINB>
+static void launch_pipe(bool flip_row, bool flip_col, unsigned gx, cudaStream_t st, const double *points,
+                        const vs::PipeBin &b, const vs::PipeEpi &e, unsigned *counter) {
+    using namespace vs;
+    if (flip_row && !flip_col)
+        raster_pipe_kernel<true, false, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
+    else if (flip_row && flip_col)
+        raster_pipe_kernel<true, true, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
+    else if (!flip_row && !flip_col)
+        raster_pipe_kernel<false, false, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
+    else
+        raster_pipe_kernel<false, true, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
+}
+
+static size_t pipelined_counters_offset(int64_t xsize, int64_t ysize) {
+    return (vs::carve_overlap(nullptr, xsize, ysize).bytes + 255) & ~size_t(255);
+}
+
+extern "C" size_t vs_dsm_from_points_pipelined_workspace_size(int n_views, int64_t xsize, int64_t ysize) {
+    if (n_views <= 0 || xsize <= 0 || ysize <= 0) return 0;
+    return pipelined_counters_offset(xsize, ysize) + sizeof(unsigned) * (static_cast<size_t>(n_views) + 1) + 256;
+}
+
+extern "C" int vs_dsm_from_points_pipelined(const double *points, const int64_t *offsets, int n_views, double xoff,
+                                            double yoff, double xresolution, double yresolution, int64_t xsize,
+                                            int64_t ysize, float *dsm, void *workspace, size_t workspace_bytes,
+                                            void *stream, void *const *launch_events) {
+    using namespace vs;
+    VS_REQUIRE(n_views > 0 && n_views < (1 << 23) && grid_ok(xsize, ysize),
+               "vs_dsm_from_points_pipelined: bad sizes views=%d grid=%lldx%lld", n_views, (long long)xsize,
+               (long long)ysize);
+    VS_REQUIRE(points && offsets && dsm && workspace, "vs_dsm_from_points_pipelined: null pointer");
+    const size_t need = vs_dsm_from_points_pipelined_workspace_size(n_views, xsize, ysize);
+    if (workspace_bytes < need) {
+        set_error("vs_dsm_from_points_pipelined: workspace %zu < %zu bytes", workspace_bytes, need);
+        return VS_ERR_WORKSPACE;
+    }
+    cudaStream_t st = as_stream(stream);
+    OverlapWs w = carve_overlap(workspace, xsize, ysize);
+    unsigned *counters = reinterpret_cast<unsigned *>(static_cast<char *>(workspace) +
+                                                      pipelined_counters_offset(xsize, ysize));
+    RasterWs tw;                       // threshold tables only
+    tw.row_thr = w.row_thr;
+    tw.col_thr = w.col_thr;
+    Tables tb;
+    const long long cells = xsize * ysize;
+    int s = make_tables(xoff, yoff, xresolution, yresolution, xsize, ysize, tw, tb, st);
+    for (int i = 0; i < 2 && s == VS_OK; ++i) s = clear(w.keys[i], sizeof(unsigned long long) * cells, st);
+    for (int i = 0; i < 2 && s == VS_OK; ++i) s = clear(w.first[i], sizeof(unsigned long long) * cells, st);
+    if (s == VS_OK) s = clear(counters, sizeof(unsigned) * (static_cast<size_t>(n_views) + 1), st);
+    if (s != VS_OK) return s;
+    const int tiles_x = static_cast<int>(ceil_div(xsize, TX));
+    const long long n_tiles = static_cast<long long>(tiles_x) * ceil_div(ysize, TILE_Y);
+    if (!fast_binning(tb)) {
+        // points outside the fast path's precondition: the literal FP64 binning, then the
+        // epilogue, view by view (same results)
+        const long long launch_points = static_cast<long long>(sm_count()) * 8 * 256 * kPts;
+        const dim3 egrid(static_cast<unsigned>(tiles_x), static_cast<unsigned>(ceil_div(ysize, TILE_Y)));
+        for (int v = 0; v < n_views; ++v) {
+            s = bin_launch(points, reinterpret_cast<const long long *>(offsets), v, 0, launch_points, tb, w.keys[v % 3],
+                           w.first[v & 1], st);
+            if (s != VS_OK) return s;
+            unsigned long long *nxt = (v + 2 < n_views) ? w.keys[(v + 2) % 3] : nullptr;
+            dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, st>>>(w.keys[v % 3], w.first[v & 1], points,
+                                                                dsm + v * cells, nxt, static_cast<int>(ysize),
+                                                                static_cast<int>(xsize));
+            VS_LAUNCH_CHECK("dsm_epilogue_kernel");
+        }
+        return VS_OK;
+    }
+    FastAxis fa[2];
+    fast_axes(tb, fa);
+    const bool flip_row = !tb.row.neg, flip_col = tb.col.neg != 0;
+    // a cap of 5 or fewer CTAs per SM takes the 48-register build, which spills nothing
+    const bool narrow = g_bin_ctas_per_sm > 0 && g_bin_ctas_per_sm <= 5;
+    static int resident[2] = {0, 0};
+    if (!resident[narrow]) {
+        int per_sm = 0;
+        const cudaError_t e = narrow ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                           &per_sm, raster_pipe_kernel<true, false, 5>, TX * TY, 0)
+                                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                                           &per_sm, raster_pipe_kernel<true, false, 6>, TX * TY, 0);
+        resident[narrow] = (e == cudaSuccess && per_sm > 0) ? per_sm : 4;
+    }
+    const int per_sm = g_bin_ctas_per_sm > 0 ? std::min(g_bin_ctas_per_sm, resident[narrow]) : resident[narrow];
+    // the views' point counts stay on the device: every launch is one resident wave, and
+    // its CTAs derive the chunk count from the offsets
+    const unsigned gx = static_cast<unsigned>(sm_count() * per_sm);
+    for (int v = 0; v <= n_views; ++v) {
+        PipeBin b{};
+        b.offsets = reinterpret_cast<const long long *>(offsets);
+        b.v = v < n_views ? v : 0;
+        b.active = v < n_views;
+        b.row = fa[0];
+        b.col = fa[1];
+        if (v < n_views) {
+            b.keys = w.keys[v % 3];
+            b.first = w.first[v & 1];
+        }
+        PipeEpi e{};
+        e.H = static_cast<int>(ysize);
+        e.W = static_cast<int>(xsize);
+        e.tiles_x = tiles_x;
+        if (v > 0) {
+            e.keys = w.keys[(v - 1) % 3];
+            e.first = w.first[(v - 1) & 1];
+            e.out = dsm + (v - 1) * cells;
+            e.clear = (v + 1 < n_views) ? w.keys[(v + 1) % 3] : nullptr;
+            e.n_tiles = n_tiles;
+        }
+        if (launch_events && cudaEventRecord(static_cast<cudaEvent_t>(launch_events[2 * v]), st) != cudaSuccess) {
+            set_error("vs_dsm_from_points_pipelined: cudaEventRecord failed");
+            return VS_ERR_CUDA;
+        }
+        if (narrow)
+            launch_pipe<5>(flip_row, flip_col, gx, st, points, b, e, counters + v);
+        else
+            launch_pipe<6>(flip_row, flip_col, gx, st, points, b, e, counters + v);
+        VS_LAUNCH_CHECK("raster_pipe_kernel");
+        if (launch_events && cudaEventRecord(static_cast<cudaEvent_t>(launch_events[2 * v + 1]), st) != cudaSuccess) {
+            set_error("vs_dsm_from_points_pipelined: cudaEventRecord failed");
+            return VS_ERR_CUDA;
+        }
+    }
+    return VS_OK;
+}
+
 extern "C" int vs_median_blur3x3_f32(const float *in, float *out, int64_t h, int64_t w, int64_t n_img,
                                      void *stream) {
     VS_REQUIRE(h > 0 && w > 0 && n_img > 0 && in && out && in != out, "vs_median_blur3x3_f32: bad arguments");
@@ -1741,19 +1995,8 @@ extern "C" int vs_aoi_batch_plan(const VsAoi *aois, int n_aois, const VsMapView 
             return fail(VS_ERR_ARG);
         }
         AoiDev &ad = p->h_aois[a];
-        const Axis *ax[2] = {&tb.row, &tb.col};
-        FastAxis *fa[2] = {&ad.row, &ad.col};
-        for (int k = 0; k < 2; ++k) {
-            memcpy(&fa[k]->off_bits, &ax[k]->off, sizeof(long long));
-            fa[k]->tmax = ax[k]->tmax;
-            fa[k]->thr = ax[k]->thr;
-            fa[k]->top12 = ax[k]->top12;
-            fa[k]->shift = ax[k]->shift;
-            fa[k]->nm1 = static_cast<int>(ax[k]->n - 1);
-            fa[k]->scale = ax[k]->scale;
-            fa[k]->err_abs = ax[k]->err_abs;
-            fa[k]->err_rel = ax[k]->err_rel;
-        }
+        ad.row = fast_axis_of(tb.row);
+        ad.col = fast_axis_of(tb.col);
         int ex = 0, ey = 0;
         frexp(A.xoff, &ex);
         frexp(A.yoff, &ey);
@@ -2036,20 +2279,6 @@ __global__ void __launch_bounds__(TX *TY) depth_epilogue_kernel(const unsigned l
                                                                int W) {
     __shared__ EpilogueSmem sm;
     epilogue_tile(vk, SignZeroDecoder{first}, out, next_keys, H, W, blockIdx.y * TILE_Y, blockIdx.x * TX, sm);
-}
-
-FastAxis fast_axis_of(const Axis &ax) {
-    FastAxis fa;
-    memcpy(&fa.off_bits, &ax.off, sizeof(long long));
-    fa.tmax = ax.tmax;
-    fa.thr = ax.thr;
-    fa.top12 = ax.top12;
-    fa.shift = ax.shift;
-    fa.nm1 = static_cast<int>(ax.n - 1);
-    fa.scale = ax.scale;
-    fa.err_abs = ax.err_abs;
-    fa.err_rel = ax.err_rel;
-    return fa;
 }
 
 }  // namespace

@@ -18,9 +18,14 @@ def grid_size(aoi_width, aoi_height, e_resolution=E_RESOLUTION, n_resolution=N_R
 
 
 def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize, ysize, out=None,
-                    epilogue_stream=None, bin_events=None):
+                    epilogue_stream=None, bin_events=None, pipelined=False, launch_events=None):
     """points: (total, 3) float64 (device tensor or array); offsets: (V+1,) int64 view
     boundaries.  Returns (V, ysize, xsize) float32 device tensor.
+
+    ``pipelined``: V + 1 launches on the current stream, each binning one view while its
+    other CTAs run the previous view's decode / hole fill / blur (same results);
+    ``launch_events`` (with ``pipelined``): 2(V + 1) timing-enabled torch.cuda.Events
+    recorded around each launch.
 
     ``epilogue_stream`` (a torch.cuda.Stream): run each view's decode / hole fill / blur
     there, overlapped with the binning of the next view on the current stream (the
@@ -33,7 +38,12 @@ def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize
     buffers on a second stream while the earlier views are binned (the offsets are read on
     the host)."""
     require_cuda()
-    if not (isinstance(points, torch.Tensor) and points.is_cuda) and epilogue_stream is None and bin_events is None:
+    if pipelined and (epilogue_stream is not None or bin_events is not None):
+        raise ValueError('pipelined runs on the current stream only (no epilogue_stream, no bin_events)')
+    if launch_events is not None and not pipelined:
+        raise ValueError('launch_events needs pipelined=True')
+    if not (isinstance(points, torch.Tensor) and points.is_cuda) and epilogue_stream is None and bin_events is None \
+            and not pipelined:
         return _dsm_from_host_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize, ysize, out)
     pts = as_device(points, torch.float64)
     offs = as_device(offsets, torch.int64)
@@ -43,21 +53,30 @@ def dsm_from_points(points, offsets, xoff, yoff, xresolution, yresolution, xsize
         out = torch.empty((V, ysize, xsize), dtype=torch.float32, device='cuda')
     args = (ptr(pts), ptr(offs), V, float(xoff), float(yoff), float(xresolution), float(yresolution), xsize, ysize,
             ptr(out))
-    if epilogue_stream is None:
+    if pipelined:
+        wp, wb = workspace(_lib.lib().vs_dsm_from_points_pipelined_workspace_size(V, xsize, ysize))
+        _lib.call('vs_dsm_from_points_pipelined', *args, wp, wb, stream_handle(),
+                  _event_array(launch_events, 2 * (V + 1)))
+    elif epilogue_stream is None:
         wp, wb = workspace(_lib.lib().vs_dsm_from_points_workspace_size(V, xsize, ysize))
         _lib.call('vs_dsm_from_points', *args, wp, wb, stream_handle())
     else:
         wp, wb = workspace(_lib.lib().vs_dsm_from_points_overlap_workspace_size(V, xsize, ysize))
-        evs = None
-        if bin_events is not None:
-            if len(bin_events) != 2 * V:
-                raise ValueError('bin_events needs 2 events per view')
-            for e in bin_events:        # the event handle exists once the event was recorded
-                if not e.cuda_event:
-                    e.record()
-            evs = (ctypes.c_void_p * (2 * V))(*[e.cuda_event for e in bin_events])
-        _lib.call('vs_dsm_from_points_overlap', *args, wp, wb, stream_handle(), epilogue_stream.cuda_stream, evs)
+        _lib.call('vs_dsm_from_points_overlap', *args, wp, wb, stream_handle(), epilogue_stream.cuda_stream,
+                  _event_array(bin_events, 2 * V))
     return out
+
+
+def _event_array(events, count):
+    """ctypes array of the cudaEvent_t handles of torch.cuda.Events (None stays None)."""
+    if events is None:
+        return None
+    if len(events) != count:
+        raise ValueError(f'expected {count} events, got {len(events)}')
+    for e in events:            # the event handle exists once the event was recorded
+        if not e.cuda_event:
+            e.record()
+    return (ctypes.c_void_p * count)(*[e.cuda_event for e in events])
 
 
 _copy_streams = {}
