@@ -138,6 +138,52 @@ __device__ __forceinline__ df df_add_ops(df a, df b) {
     return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
+// ---- packed double-float pairs --------------------------------------------------------
+// Two independent double-float values per operation with Blackwell's FP32x2 instructions
+// (FADD2 / FMUL2 / FFMA2: IEEE round-to-nearest in each lane), so each lane computes
+// exactly what the scalar helpers above compute.  A difference y - x is fma(x, -1, y)
+// (one rounding, like the subtraction); a negated product -fl(a b) is fl((-a) b).
+struct df2 {
+    float2 hi, lo;
+};
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 sub2(float2 y, float2 x) { return __ffma2_rn(x, f2s(-1.0f), y); }
+__device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    const float2 bb = sub2(s, a);
+    return {s, __fadd2_rn(sub2(a, sub2(s, bb)), sub2(b, bb))};
+}
+__device__ __forceinline__ df2 fast_two_sum2(float2 a, float2 b) {  // |a| >= |b| per lane
+    const float2 s = __fadd2_rn(a, b);
+    return {s, sub2(b, sub2(s, a))};
+}
+// two_prod per lane given nb = -b: the error term fma(a, b, -fl(a b)), -fl(a b) = fl(a (-b))
+__device__ __forceinline__ df2 two_prod2(float2 a, float2 b, float2 nb) {
+    return {__fmul2_rn(a, b), __ffma2_rn(a, b, __fmul2_rn(a, nb))};
+}
+// df_mul per lane given nb_hi = -b.hi
+__device__ __forceinline__ df2 df_mul2(df2 a, df2 b, float2 nb_hi) {
+    df2 p = two_prod2(a.hi, b.hi, nb_hi);
+    p.lo = __ffma2_rn(a.hi, b.lo, __ffma2_rn(a.lo, b.hi, p.lo));
+    return fast_two_sum2(p.hi, p.lo);
+}
+// df_add_ops per lane
+__device__ __forceinline__ df2 df_add_ops2(df2 a, df2 b) {
+    const df2 s = two_sum2(a.hi, b.hi);
+    return fast_two_sum2(s.hi, __fadd2_rn(s.lo, __fadd2_rn(a.lo, b.lo)));
+}
+// df_recip per lane: 1 - p.hi is exact (p.hi = w.hi q is within 2^-21 of 1), so -p.hi is
+// recovered exactly as (1 - p.hi) - 1 for the error term of the product.
+__device__ __forceinline__ df2 df_recip2(df2 w) {
+    const float2 q = f2(__fdividef(1.0f, w.hi.x), __fdividef(1.0f, w.hi.y));
+    const float2 phi = __fmul2_rn(w.hi, q);
+    const float2 t = sub2(f2s(1.0f), phi);                               // 1 - p.hi
+    const float2 plo = __ffma2_rn(w.hi, q, __fadd2_rn(t, f2s(-1.0f)));   // fma(w.hi, q, -p.hi)
+    const float2 e = sub2(sub2(t, plo), __fmul2_rn(w.lo, q));
+    return fast_two_sum2(q, __fmul2_rn(q, e));
+}
+
 // 1 / w in double-float: an approximate reciprocal refined by one Newton step whose residual
 // 1 - w q is formed exactly (two_prod; 1 - p.hi is exact for p.hi near 1): relative error
 // about the square of the first estimate's, below 2^-43.

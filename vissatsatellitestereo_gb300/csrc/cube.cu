@@ -148,6 +148,19 @@ __device__ __forceinline__ float quotient_fast(float num, float den) {
     return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
 }
 
+// -(num / den) for two values at once with packed FP32x2 operations: quotient_fast's steps
+// with the reciprocal's sign flipped (nr = -r, q0n = -q0), so the residual
+// num - den q0 = fma(den, q0n, num) and -(q0 + e r) = fma(e, nr, q0n) need no negated
+// operand; each lane's products and sums are the scalar form's, negated exactly.
+__device__ __forceinline__ float2 quotient2_neg(float2 num, float2 den) {
+    float2 nr;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(nr.x) : "f"(-den.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(nr.y) : "f"(-den.y));
+    const float2 q0n = __fmul2_rn(num, nr);
+    const float2 e = __ffma2_rn(den, q0n, num);
+    return __ffma2_rn(e, nr, q0n);
+}
+
 __device__ __forceinline__ float quotient(float num, float den) {
     if (__builtin_expect(!quotient_fast_ok(num, den), 0)) return quotient_ieee(num, den);
     return quotient_fast(num, den);
@@ -218,12 +231,6 @@ __global__ void cube_prepare_mma_kernel(const VsRpcCamera *__restrict__ cams, in
             w.lincoef[i] = c;
         }
     }
-}
-
-// constant + linear terms (RPC order: 1, y, x, z) added to the tensor cores' higher-order
-// sum in the FP32 variant's order: z, x, y, then the constant
-__device__ __forceinline__ float add_linear(float hot, float4 c, float x, float y, float z) {
-    return __fadd_rn(__fmaf_rn(c.y, y, __fmaf_rn(c.z, x, __fmaf_rn(c.w, z, hot))), c.x);
 }
 
 __global__ void cube_prepare_fp32_kernel(const VsRpcCamera *__restrict__ cams, int n_cams, CubeWs w) {
@@ -411,46 +418,66 @@ __global__ void __launch_bounds__(kCubeWarps * 32, CubeCfg<V>::kMinBlocks) cube_
                         mma_tf32(d[mt], a[mt][0][2 * s], a[mt][1][2 * s], a[mt][0][2 * s + 1], a[mt][1][2 * s + 1],
                                  b[2 * s], b[2 * s + 1]);
                 }
-            if constexpr (C::kLin) {
+            // the two points of an accumulator row pair (g, g + 8) travel as one FP32x2 pair
+            // through the linear terms (LIN), the quotient and the denormalisation; one
+            // warp-uniform range test (min/max reductions, which NaN cannot trip and an
+            // infinity always does) sends rare operands to the per-value test and IEEE division
+            float2 num[MT], den[MT];
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                num[mt] = make_float2(d[mt][0], d[mt][2]);
+                den[mt] = make_float2(d[mt][1], d[mt][3]);
+            }
+            if constexpr (C::kLin) {     // constant + linear terms (RPC order 1, y, x, z): z, x, y, then 1
                 const float4 cn = lc[(4 * j + t) * 2], cd = lc[(4 * j + t) * 2 + 1];
 #pragma unroll
                 for (int mt = 0; mt < MT; ++mt) {
-                    d[mt][0] = add_linear(d[mt][0], cn, px[mt][0], py[mt][0], pz[mt][0]);
-                    d[mt][1] = add_linear(d[mt][1], cd, px[mt][0], py[mt][0], pz[mt][0]);
-                    d[mt][2] = add_linear(d[mt][2], cn, px[mt][1], py[mt][1], pz[mt][1]);
-                    d[mt][3] = add_linear(d[mt][3], cd, px[mt][1], py[mt][1], pz[mt][1]);
+                    const float2 X = make_float2(px[mt][0], px[mt][1]), Y = make_float2(py[mt][0], py[mt][1]),
+                                 Z = make_float2(pz[mt][0], pz[mt][1]);
+                    num[mt] = __ffma2_rn(make_float2(cn.w, cn.w), Z, num[mt]);
+                    den[mt] = __ffma2_rn(make_float2(cd.w, cd.w), Z, den[mt]);
+                    num[mt] = __ffma2_rn(make_float2(cn.z, cn.z), X, num[mt]);
+                    den[mt] = __ffma2_rn(make_float2(cd.z, cd.z), X, den[mt]);
+                    num[mt] = __ffma2_rn(make_float2(cn.y, cn.y), Y, num[mt]);
+                    den[mt] = __ffma2_rn(make_float2(cd.y, cd.y), Y, den[mt]);
+                    num[mt] = __fadd2_rn(num[mt], make_float2(cn.x, cn.x));
+                    den[mt] = __fadd2_rn(den[mt], make_float2(cd.x, cd.x));
                 }
             }
-            // quotients: the fast form for every value, one warp-uniform check for the rare
-            // operands outside its range
-            float q[MT][2];
-            bool ok = true;
+            float dlo = 1.0f, dhi = 1.0f, nhi = 0.0f;
 #pragma unroll
             for (int mt = 0; mt < MT; ++mt) {
-                q[mt][0] = quotient_fast(d[mt][0], d[mt][1]);
-                q[mt][1] = quotient_fast(d[mt][2], d[mt][3]);
-                ok = ok && quotient_fast_ok(d[mt][0], d[mt][1]) && quotient_fast_ok(d[mt][2], d[mt][3]);
+                dlo = fminf(dlo, fminf(fabsf(den[mt].x), fabsf(den[mt].y)));
+                dhi = fmaxf(dhi, fmaxf(fabsf(den[mt].x), fabsf(den[mt].y)));
+                nhi = fmaxf(nhi, fmaxf(fabsf(num[mt].x), fabsf(num[mt].y)));
             }
-            if (__builtin_expect(!__all_sync(0xffffffffu, ok), 0)) {
+            float2 qn[MT];                                   // -(num / den)
+            if (__builtin_expect(__all_sync(0xffffffffu, dlo > 1e-30f && dhi < 1e30f && nhi < 1e30f), 1)) {
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt) qn[mt] = quotient2_neg(num[mt], den[mt]);
+            } else {
 #pragma unroll
                 for (int mt = 0; mt < MT; ++mt) {
-                    if (!quotient_fast_ok(d[mt][0], d[mt][1])) q[mt][0] = quotient_ieee(d[mt][0], d[mt][1]);
-                    if (!quotient_fast_ok(d[mt][2], d[mt][3])) q[mt][1] = quotient_ieee(d[mt][2], d[mt][3]);
+                    qn[mt].x = -quotient(num[mt].x, den[mt].x);
+                    qn[mt].y = -quotient(num[mt].y, den[mt].y);
                 }
             }
             if (plane_ok) {
+                const float2 nsc = make_float2(-sc.x, -sc.x), off = make_float2(sc.y, sc.y);
                 if (full) {
 #pragma unroll
                     for (int mt = 0; mt < MT; ++mt) {
-                        __stcs(o + 16 * mt, __fmaf_rn(q[mt][0], sc.x, sc.y));
-                        __stcs(o + 16 * mt + 8, __fmaf_rn(q[mt][1], sc.x, sc.y));
+                        const float2 v = __ffma2_rn(qn[mt], nsc, off);
+                        __stcs(o + 16 * mt, v.x);
+                        __stcs(o + 16 * mt + 8, v.y);
                     }
                 } else {
 #pragma unroll
                     for (int mt = 0; mt < MT; ++mt) {
                         const long long p = p0 + 16 * mt + g;
-                        if (p < n) __stcs(o + 16 * mt, __fmaf_rn(q[mt][0], sc.x, sc.y));
-                        if (p + 8 < n) __stcs(o + 16 * mt + 8, __fmaf_rn(q[mt][1], sc.x, sc.y));
+                        const float2 v = __ffma2_rn(qn[mt], nsc, off);
+                        if (p < n) __stcs(o + 16 * mt, v.x);
+                        if (p + 8 < n) __stcs(o + 16 * mt + 8, v.y);
                     }
                 }
             }

@@ -156,23 +156,18 @@ __host__ __device__ __forceinline__ unsigned canon_offset(int row, int k, int K)
 // outside the range where that is accurate
 __device__ __noinline__ float tc_quotient_ieee(float num, float den) { return __fdiv_rn(num, den); }
 
-// constant + linear terms (RPC order: 1, y, x, z) added to the tensor cores' sum:
-// z, x, y, then the constant
-__device__ __forceinline__ float add_linear(float hot, float4 c, float x, float y, float z) {
-    return __fadd_rn(__fmaf_rn(c.y, y, __fmaf_rn(c.z, x, __fmaf_rn(c.w, z, hot))), c.x);
-}
-
 __device__ __forceinline__ const double *column_poly(const VsRpcCamera &cam, int p) {
     return p == 0 ? cam.col_num : p == 1 ? cam.col_den : p == 2 ? cam.row_num : cam.row_den;
 }
 
-// The per-call constants in the workspace: B pieces (canonical layout), the (scale,
-// offset) of each output plane, (LIN) the FP32 constant + linear coefficients, and the
-// error word.
+// The per-call constants in the workspace: B pieces (canonical layout), per camera the
+// negated scales and the offsets of its two planes, (LIN) per camera and term k the FP32
+// constant + linear coefficients of the four polynomials, paired (col, row) for the packed
+// FP32x2 epilogue, and the error word.
 struct CubeTcWs {
     __nv_bfloat16 *b;          // [n_pad x K]
-    float2 *den;               // [2C]
-    float4 *lin;               // [C][4 polys]
+    float4 *den;               // [C]: (-col_scale, -row_scale, col_off, row_off)
+    float4 *lin;               // [C][4 terms]: (colNum_k, rowNum_k, colDen_k, rowDen_k)
     int *err;
 };
 
@@ -182,7 +177,7 @@ CubeTcWs carve_cube_tc(void *ws, int n_cams) {
     Carver cv(ws);
     CubeTcWs w;
     w.b = cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * 64);
-    w.den = cv.take<float2>(2 * static_cast<size_t>(n_cams));
+    w.den = cv.take<float4>(static_cast<size_t>(n_cams));
     w.lin = cv.take<float4>(4 * static_cast<size_t>(n_cams));
     w.err = cv.take<int>(1);
     return w;
@@ -204,15 +199,16 @@ __global__ void cube_tc_prepare_kernel(const VsRpcCamera *__restrict__ cams, int
         }
         w.b[canon_offset(col, k, S::kK) / 2] = __float2bfloat16_rn(v);
     }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * n_cams; i += gridDim.x * blockDim.x) {
-        const VsRpcCamera &c = cams[i >> 1];
-        w.den[i] = (i & 1) == 0 ? make_float2(static_cast<float>(c.col_scale), static_cast<float>(c.col_off))
-                                : make_float2(static_cast<float>(c.row_scale), static_cast<float>(c.row_off));
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_cams; i += gridDim.x * blockDim.x) {
+        const VsRpcCamera &c = cams[i];
+        w.den[i] = make_float4(-static_cast<float>(c.col_scale), -static_cast<float>(c.row_scale),
+                               static_cast<float>(c.col_off), static_cast<float>(c.row_off));
     }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * n_cams; i += gridDim.x * blockDim.x) {
-        const double *poly = column_poly(cams[i >> 2], i & 3);
-        w.lin[i] = make_float4(static_cast<float>(poly[0]), static_cast<float>(poly[1]), static_cast<float>(poly[2]),
-                               static_cast<float>(poly[3]));
+        const VsRpcCamera &c = cams[i >> 2];
+        const int k = i & 3;
+        w.lin[i] = make_float4(static_cast<float>(c.col_num[k]), static_cast<float>(c.row_num[k]),
+                               static_cast<float>(c.col_den[k]), static_cast<float>(c.row_den[k]));
     }
 }
 
@@ -261,53 +257,94 @@ __device__ __forceinline__ float quotient_fast(float num, float den) {
     return __fmaf_rn(__fmaf_rn(-den, q0, num), r, q0);
 }
 
+// -(num / den) for a (col, row) pair with packed FP32x2 operations: the same steps as
+// quotient_fast with the reciprocal's sign flipped (nr = -r, q0n = -q0), so the residual
+// num - den q0 = fma(den, q0n, num) and the result -(q0 + e r) = fma(e, nr, q0n) need no
+// negated operand -- every product and sum is the scalar form's, negated exactly.
+__device__ __forceinline__ float2 quotient2_neg(float2 num, float2 den) {
+    float2 nr;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(nr.x) : "f"(-den.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(nr.y) : "f"(-den.y));
+    const float2 q0n = __fmul2_rn(num, nr);
+    const float2 e = __ffma2_rn(den, q0n, num);
+    return __ffma2_rn(e, nr, q0n);
+}
+
 // The epilogue of one tile for one warp: its lanes are 32 points of the tile (the TMEM
 // lanes of the warp's quarter), its cameras [c_begin, c_end) those of its warpgroup, taken
-// CH at a time (CH even: a tcgen05.ld of 8 columns covers two cameras).
+// CH at a time (CH even: a tcgen05.ld of 8 columns covers two cameras).  A camera's col and
+// row travel as one FP32x2 pair through the linear terms (LIN), the quotient and the
+// denormalisation (packed FFMA2/FMUL2/FADD2, IEEE round-to-nearest per lane, so the
+// values equal the scalar form's); one warp-uniform range test per chunk (denominators in
+// (1/2, 3/2), numerators below 1e30: min/max reductions, which NaN cannot trip and an
+// infinity always does) sends a chunk holding a rare operand to the per-lane test and
+// IEEE division.
 template <bool LIN, int CH>
 __device__ __forceinline__ void tc_epilogue(unsigned lane_base, int c_begin, int c_end, long long p, long long n,
-                                            float px, float py, float pz, const float2 *sden, const float4 *slin,
+                                            float2 x2, float2 y2, float2 z2, const float4 *sdn, const float4 *slin,
                                             float *__restrict__ out) {
-    constexpr int kE = 2 * CH;                     // (camera, plane) entries of a chunk
     for (int cb = c_begin; cb < c_end; cb += CH) {
         unsigned r[CH / 2][8];
 #pragma unroll
-        for (int j = 0; j < CH / 2; ++j)
-            if (cb + 2 * j < c_end) tmem_ld8(lane_base + 4 * (cb + 2 * j), r[j]);   // warp-uniform
-        tmem_wait();
-        // quotients of the chunk's cameras, branch-free; one warp-uniform check sends rare
-        // operands to IEEE division.  Columns of cameras past c_end (an odd last pair) are
-        // computed and dropped.
-        const int nc = min(CH, c_end - cb);
-        float num[kE], den[kE], q[kE];
-        bool ok = true;
+        for (int j = 0; j < CH / 2; ++j) {
+            if (cb + 2 * j < c_end) {
+                tmem_ld8(lane_base + 4 * (cb + 2 * j), r[j]);   // warp-uniform
+            } else {
 #pragma unroll
-        for (int e = 0; e < kE; ++e) {
-            const int j = e >> 2, h = (e >> 1) & 1, pl = e & 1;
-            float nu = __uint_as_float(r[j][4 * h + 2 * pl]);
-            float de = __uint_as_float(r[j][4 * h + 2 * pl + 1]);
-            if (LIN) {
-                const float4 *lc = slin + 4 * (cb + (e >> 1)) + 2 * pl;   // within slin's 64 cameras
-                nu = add_linear(nu, lc[0], px, py, pz);
-                de = add_linear(de, lc[1], px, py, pz);
+                for (int k = 0; k < 8; ++k) r[j][k] = 0u;
             }
-            num[e] = nu;
-            den[e] = de;
-            q[e] = quotient_fast(nu, de);
-            if ((e >> 1) < nc) ok = ok && quotient_fast_ok(nu, de);
         }
-        if (__builtin_expect(!__all_sync(0xffffffffu, ok), 0)) {
+        tmem_wait();
+        const int nc = min(CH, c_end - cb);
+        float2 num[CH], den[CH];
+        float dmin = 1.0f, dmax = 1.0f, nmax = 0.0f;
 #pragma unroll
-            for (int e = 0; e < kE; ++e)
-                if (!quotient_fast_ok(num[e], den[e])) q[e] = tc_quotient_ieee(num[e], den[e]);
+        for (int c = 0; c < CH; ++c) {
+            const unsigned *w4 = &r[c >> 1][4 * (c & 1)];     // colNum, colDen, rowNum, rowDen
+            float2 nu = make_float2(__uint_as_float(w4[0]), __uint_as_float(w4[2]));
+            float2 de = make_float2(__uint_as_float(w4[1]), __uint_as_float(w4[3]));
+            if (LIN) {      // + z, + x, + y terms, then the constant (within slin's 64 cameras)
+                const float4 *lc = slin + 4 * (cb + c);
+                const float4 l3 = lc[3], l2 = lc[2], l1 = lc[1], l0 = lc[0];
+                nu = __ffma2_rn(make_float2(l3.x, l3.y), z2, nu);
+                de = __ffma2_rn(make_float2(l3.z, l3.w), z2, de);
+                nu = __ffma2_rn(make_float2(l2.x, l2.y), x2, nu);
+                de = __ffma2_rn(make_float2(l2.z, l2.w), x2, de);
+                nu = __ffma2_rn(make_float2(l1.x, l1.y), y2, nu);
+                de = __ffma2_rn(make_float2(l1.z, l1.w), y2, de);
+                nu = __fadd2_rn(nu, make_float2(l0.x, l0.y));
+                de = __fadd2_rn(de, make_float2(l0.z, l0.w));
+            }
+            if (c < nc) {
+                dmin = fminf(dmin, fminf(de.x, de.y));
+                dmax = fmaxf(dmax, fmaxf(de.x, de.y));
+                nmax = fmaxf(nmax, fmaxf(fabsf(nu.x), fabsf(nu.y)));
+            }
+            num[c] = nu;
+            den[c] = de;
+        }
+        float2 qn[CH];                                   // -(num / den)
+        if (__builtin_expect(__all_sync(0xffffffffu, dmin > 0.5f && dmax < 1.5f && nmax < 1e30f), 1)) {
+#pragma unroll
+            for (int c = 0; c < CH; ++c) qn[c] = quotient2_neg(num[c], den[c]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                qn[c].x = -(quotient_fast_ok(num[c].x, den[c].x) ? quotient_fast(num[c].x, den[c].x)
+                                                                 : tc_quotient_ieee(num[c].x, den[c].x));
+                qn[c].y = -(quotient_fast_ok(num[c].y, den[c].y) ? quotient_fast(num[c].y, den[c].y)
+                                                                 : tc_quotient_ieee(num[c].y, den[c].y));
+            }
         }
         if (p < n) {
-            float *o = out + (2LL * cb) * n + p;     // plane 2 cb, then one plane per entry
+            float *o = out + (2LL * cb) * n + p;     // camera cb's col plane; its row plane follows
 #pragma unroll
-            for (int e = 0; e < kE; ++e, o += n) {
-                if ((e >> 1) < nc) {
-                    const float2 dn = sden[2 * cb + e];
-                    __stcs(o, __fmaf_rn(q[e], dn.x, dn.y));
+            for (int c = 0; c < CH; ++c, o += 2 * n) {
+                if (c < nc) {
+                    const float4 sd = sdn[cb + c];   // (-col_scale, -row_scale, col_off, row_off)
+                    const float2 v = __ffma2_rn(qn[c], make_float2(sd.x, sd.y), make_float2(sd.z, sd.w));
+                    __stcs(o, v.x);
+                    __stcs(o + n, v.y);
                 }
             }
         }
@@ -323,8 +360,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sb = smem;                                           // B: n_pad x K
     unsigned char *sa = sb + kTcMaxN * S::kRowBytes;                    // A ring: kTcStages x 128 x K
-    float2 *sden = reinterpret_cast<float2 *>(sa + kTcStages * kStageBytes);
-    float4 *slin = reinterpret_cast<float4 *>(sden + 2 * kTcMaxCams);
+    float4 *sden = reinterpret_cast<float4 *>(sa + kTcStages * kStageBytes);
+    float4 *slin = sden + kTcMaxCams;
     // mbarriers: A full / empty per stage, accumulator full / empty, B landed, final drain
     __shared__ __align__(8) unsigned long long bars[2 * kTcStages + 6];
     __shared__ unsigned tmem_base;
@@ -358,7 +395,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
             "l"(w.b), "r"(b_bytes), "r"(bar_b)
             : "memory");
     }
-    for (int i = tid; i < 2 * n_cams; i += kTcThreads) sden[i] = w.den[i];
+    for (int i = tid; i < n_cams; i += kTcThreads) sden[i] = w.den[i];
     if (LIN)
         for (int i = tid; i < 4 * n_cams; i += kTcThreads) slin[i] = w.lin[i];
     if (warp == kTcMmaWarp) {
@@ -479,7 +516,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) cube_tc_kernel(const float *__r
             }
             tc_fence_after();
             const unsigned lane_base = tmem + (static_cast<unsigned>(quad * 32) << 16) + static_cast<unsigned>(acc * 256);
-            tc_epilogue<LIN, 4>(lane_base, c_begin, c_end, tile * kTcTile + row, n, cx, cy, cz, sden, slin, out);
+            tc_epilogue<LIN, 4>(lane_base, c_begin, c_end, tile * kTcTile + row, n, make_float2(cx, cx),
+                                make_float2(cy, cy), make_float2(cz, cz), sden, slin, out);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(acc_empty(acc));
@@ -508,7 +546,7 @@ template <bool LIN>
 size_t cube_tc_smem() {
     using S = TcScheme<LIN>;
     // at least half of the SM's shared memory: one CTA per SM, which owns all 512 TMEM columns
-    const size_t need = static_cast<size_t>(kTcMaxN + kTcStages * kTcTile) * S::kRowBytes + sizeof(float2) * 2 * kTcMaxCams +
+    const size_t need = static_cast<size_t>(kTcMaxN + kTcStages * kTcTile) * S::kRowBytes + sizeof(float4) * kTcMaxCams +
                         sizeof(float4) * 4 * kTcMaxCams + 1024;
     return std::max<size_t>(need, 120 * 1024);
 }
@@ -522,7 +560,7 @@ unsigned g_tc_wait_limit = kWaitLimit;
 size_t cube_tc_workspace_bytes(int n_cams) {
     Carver cv(nullptr);
     cv.take<__nv_bfloat16>(static_cast<size_t>(kTcMaxN) * 64);
-    cv.take<float2>(2 * static_cast<size_t>(n_cams));
+    cv.take<float4>(static_cast<size_t>(n_cams));
     cv.take<float4>(4 * static_cast<size_t>(n_cams));
     cv.take<int>(1);
     return cv.used + 256;

@@ -16,16 +16,18 @@
 
 namespace vs {
 
-// Per-camera constants of the fast form, prepared once per call.
+// Per-camera constants of the fast form, prepared once per call.  The four polynomials
+// travel as two (col, row) pairs through packed FP32x2 arithmetic: pair 0 = (colNum,
+// rowNum), pair 1 = (colDen, rowDen).
 struct RpcFast {
     df lat_off, lon_off, alt_off;       // offsets (double-float)
     df inv_lat, inv_lon, inv_alt;       // 1 / scale (double-float)
-    df lin[4][4];                       // [poly][0..3] constant + linear coefficients
-    float hot[4][16];                   // [poly][k-4] higher-order coefficients (FP32)
-    df col_scale, col_off, row_scale, row_off;
+    float2 lin_hi[2][4], lin_lo[2][4];  // [pair][0..3] constant + linear coefficients
+    float2 lin_nhi[2][4];               // -lin_hi (error terms of the products)
+    float2 hot[2][16];                  // [pair][k-4] higher-order coefficients (FP32)
+    float2 scale_hi, scale_lo, scale_nhi, off_hi, off_lo;   // (col, row) denormalisation
     float width, height;
 };
-// poly order inside RpcFast: 0 = colNum, 1 = colDen, 2 = rowNum, 3 = rowDen
 
 // ---- exact FP64 (reference order) ------------------------------------------------------
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
@@ -88,29 +90,33 @@ __device__ __forceinline__ df split_double(double v) {
     return {hi, lo};
 }
 
-// constant + three linear terms in double-float, plus the FP32 higher-order sum
-__device__ __forceinline__ df poly_fast(const df (&lin)[4], const float (&hot)[16], df x, df y, df z,
-                                        const float (&m)[16]) {
-    // exact products of the high parts, cross terms into the low word
-    df p1 = two_prod(lin[1].hi, y.hi);
-    df p2 = two_prod(lin[2].hi, x.hi);
-    df p3 = two_prod(lin[3].hi, z.hi);
-    float low = lin[0].lo + p1.lo + p2.lo + p3.lo;
-    low = __fmaf_rn(lin[1].hi, y.lo, __fmaf_rn(lin[1].lo, y.hi, low));
-    low = __fmaf_rn(lin[2].hi, x.lo, __fmaf_rn(lin[2].lo, x.hi, low));
-    low = __fmaf_rn(lin[3].hi, z.lo, __fmaf_rn(lin[3].lo, z.hi, low));
-    float h = 0.0f;
+// constant + three linear terms in double-float, plus the FP32 higher-order sum, for the
+// two polynomials of a pair at once (same operations per lane as the scalar form: exact
+// products of the high parts with their cross terms in the low word, the TwoSum chain of
+// constant, linear terms and higher-order sum)
+__device__ __forceinline__ df2 poly_fast2(const float2 (&hi)[4], const float2 (&lo)[4], const float2 (&nhi)[4],
+                                          const float2 (&hot)[16], df x, df y, df z, const float (&m)[16]) {
+    const float2 Y = f2s(y.hi), X = f2s(x.hi), Z = f2s(z.hi);
+    // two_prod(c, v): -fl(c v) = fl((-c) v) from the negated coefficients
+    const df2 p1 = {__fmul2_rn(hi[1], Y), __ffma2_rn(hi[1], Y, __fmul2_rn(nhi[1], Y))};
+    const df2 p2 = {__fmul2_rn(hi[2], X), __ffma2_rn(hi[2], X, __fmul2_rn(nhi[2], X))};
+    const df2 p3 = {__fmul2_rn(hi[3], Z), __ffma2_rn(hi[3], Z, __fmul2_rn(nhi[3], Z))};
+    float2 low = __fadd2_rn(__fadd2_rn(__fadd2_rn(lo[0], p1.lo), p2.lo), p3.lo);
+    low = __ffma2_rn(hi[1], f2s(y.lo), __ffma2_rn(lo[1], Y, low));
+    low = __ffma2_rn(hi[2], f2s(x.lo), __ffma2_rn(lo[2], X, low));
+    low = __ffma2_rn(hi[3], f2s(z.lo), __ffma2_rn(lo[3], Z, low));
+    float2 h = f2s(0.0f);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) h = __fmaf_rn(hot[k], m[k], h);
-    df s = two_sum(lin[0].hi, p1.hi);
-    low += s.lo;
-    s = two_sum(s.hi, p2.hi);
-    low += s.lo;
-    s = two_sum(s.hi, p3.hi);
-    low += s.lo;
-    s = two_sum(s.hi, h);
-    low += s.lo;
-    return fast_two_sum(s.hi, low);
+    for (int k = 0; k < 16; ++k) h = __ffma2_rn(hot[k], f2s(m[k]), h);
+    df2 s = two_sum2(hi[0], p1.hi);
+    low = __fadd2_rn(low, s.lo);
+    s = two_sum2(s.hi, p2.hi);
+    low = __fadd2_rn(low, s.lo);
+    s = two_sum2(s.hi, p3.hi);
+    low = __fadd2_rn(low, s.lo);
+    s = two_sum2(s.hi, h);
+    low = __fadd2_rn(low, s.lo);
+    return fast_two_sum2(s.hi, low);
 }
 
 // monomials 4..19 of the RPC order from the high parts of the normalised coordinates
@@ -135,20 +141,22 @@ __device__ __forceinline__ df normalise(df v, df off, df inv) {
     return df_mul(df_add_ops(v, {-off.hi, -off.lo}), inv);
 }
 
-// (col, row) as double-floats for one point given as split lat/lon/alt.
+// (col, row) as double-floats for one point given as split lat/lon/alt: the numerator
+// pair and the denominator pair, then both quotients and denormalisations as one pair.
 __device__ __forceinline__ void project_fast(const RpcFast &c, df lat, df lon, df alt, df &col, df &row) {
     const df x = normalise(lat, c.lat_off, c.inv_lat);
     const df y = normalise(lon, c.lon_off, c.inv_lon);
     const df z = normalise(alt, c.alt_off, c.inv_alt);
     float m[16];
     monomials(x.hi, y.hi, z.hi, m);
-    const df cn = poly_fast(c.lin[0], c.hot[0], x, y, z, m);
-    const df cd = poly_fast(c.lin[1], c.hot[1], x, y, z, m);
-    const df rn = poly_fast(c.lin[2], c.hot[2], x, y, z, m);
-    const df rd = poly_fast(c.lin[3], c.hot[3], x, y, z, m);
+    const df2 num = poly_fast2(c.lin_hi[0], c.lin_lo[0], c.lin_nhi[0], c.hot[0], x, y, z, m);
+    const df2 den = poly_fast2(c.lin_hi[1], c.lin_lo[1], c.lin_nhi[1], c.hot[1], x, y, z, m);
     // quotients through a Newton-refined reciprocal (relative error < 2^-43)
-    col = df_add_ops(df_mul(df_mul(cn, df_recip(cd)), c.col_scale), c.col_off);
-    row = df_add_ops(df_mul(df_mul(rn, df_recip(rd)), c.row_scale), c.row_off);
+    const df2 r = df_recip2(den);
+    const df2 q = df_mul2(num, r, sub2(f2s(0.0f), r.hi));
+    const df2 v = df_add_ops2(df_mul2(q, {c.scale_hi, c.scale_lo}, c.scale_nhi), {c.off_hi, c.off_lo});
+    col = {v.hi.x, v.lo.x};
+    row = {v.hi.y, v.lo.y};
 }
 
 // df < float bound, for the in-image mask (col >= 0, col < width)
@@ -163,15 +171,24 @@ __device__ __forceinline__ void prepare_fast(const VsRpcCamera &cam, RpcFast &f)
     f.inv_lat = df_from_double(1.0 / cam.lat_scale);
     f.inv_lon = df_from_double(1.0 / cam.lon_scale);
     f.inv_alt = df_from_double(1.0 / cam.alt_scale);
-    const double *polys[4] = {cam.col_num, cam.col_den, cam.row_num, cam.row_den};
-    for (int p = 0; p < 4; ++p) {
-        for (int k = 0; k < 4; ++k) f.lin[p][k] = df_from_double(polys[p][k]);
-        for (int k = 4; k < 20; ++k) f.hot[p][k - 4] = static_cast<float>(polys[p][k]);
+    const double *polys[2][2] = {{cam.col_num, cam.row_num}, {cam.col_den, cam.row_den}};
+    for (int p = 0; p < 2; ++p) {
+        for (int k = 0; k < 4; ++k) {
+            const df a = df_from_double(polys[p][0][k]), b = df_from_double(polys[p][1][k]);
+            f.lin_hi[p][k] = make_float2(a.hi, b.hi);
+            f.lin_lo[p][k] = make_float2(a.lo, b.lo);
+            f.lin_nhi[p][k] = make_float2(-a.hi, -b.hi);
+        }
+        for (int k = 4; k < 20; ++k)
+            f.hot[p][k - 4] = make_float2(static_cast<float>(polys[p][0][k]), static_cast<float>(polys[p][1][k]));
     }
-    f.col_scale = df_from_double(cam.col_scale);
-    f.col_off = df_from_double(cam.col_off);
-    f.row_scale = df_from_double(cam.row_scale);
-    f.row_off = df_from_double(cam.row_off);
+    const df cs = df_from_double(cam.col_scale), co = df_from_double(cam.col_off);
+    const df rs = df_from_double(cam.row_scale), ro = df_from_double(cam.row_off);
+    f.scale_hi = make_float2(cs.hi, rs.hi);
+    f.scale_lo = make_float2(cs.lo, rs.lo);
+    f.scale_nhi = make_float2(-cs.hi, -rs.hi);
+    f.off_hi = make_float2(co.hi, ro.hi);
+    f.off_lo = make_float2(co.lo, ro.lo);
     f.width = static_cast<float>(cam.width);
     f.height = static_cast<float>(cam.height);
 }
