@@ -122,6 +122,9 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------
 # our arm
 # ------------------------------------------------------------------------------------
+# L2 reserved for persisting accesses to the binning's key grids (vs_set_l2_persisting)
+L2_PERSIST_MB = 64
+
 # DRAM bytes (read + write) of raster_pipe_kernel per point binned and per DSM cell of the
 # epilogue, from an ncu capture (None: not captured)
 PIPE_TRAFFIC = None
@@ -191,6 +194,10 @@ def run_ours(args):
                                                                            pipe=True, bin_ctas=c) for c in (4, 5)},
     }
     sched = [SCHEDULES['fit_concurrent']]
+    # an L2 set-aside for the key grids: the binning launches mark their grid persisting,
+    # so the 400 MB of streamed points per view cannot evict it (released after the e2e run)
+    l2_persist = L2_PERSIST_MB << 20
+    _lib.call('vs_set_l2_persisting', l2_persist)
     cams_t = torch.from_numpy(_lib.camera_array(wl.metas)).to(dev)
 
     def fit():
@@ -418,7 +425,8 @@ def run_ours(args):
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f64+f32', 'data': 'synthetic (seeded RPCs, box-city height maps)',
-        'config': dict(wl.describe(), l2='inputs (21 GB) exceed L2; no flush needed', parallelism='replicas'),
+        'config': dict(wl.describe(), l2='inputs (21 GB) exceed L2; no flush needed', parallelism='replicas',
+                       l2_persisting_mb=L2_PERSIST_MB),
         'rpc_pts_per_s': wl.rpc_points_per_step * args.steps * world / elapsed,
         'raster_pts_per_s': wl.views * n_pts * args.steps * world / elapsed,
         'stages_ms': stages, 'fit_status_ok': bool(np.all(status_np == 0)),
@@ -479,6 +487,7 @@ def run_ours(args):
                          'api': 'approx_perspective_enu (inputs copied on its stream) + dsm_from_points on pinned host '
                                 'points (copied view by view under the binning) + fuse_dsms; results copied back'}
         del host_pts
+        _lib.call('vs_set_l2_persisting', 0)
         # ---- plain per-view GPU form (drop-in calls, one view at a time)
         result['plain_per_view'] = plain_per_view(wl, grid_t, gargs, args)
         # ---- precision form (config: 16 M normalised points x the 50 cameras)
@@ -493,6 +502,7 @@ def run_ours(args):
         result['depth_form'] = depth_form()
         # ---- CPU baseline (oracle, bounded sample)
         result['cpu_baseline'] = cpu_baseline(wl, gargs, pool=False)
+    _lib.call('vs_set_l2_persisting', 0)
     replicas.finish()
     if rank == 0:
         print(json.dumps(result))

@@ -117,6 +117,14 @@ void vs_set_tc_wait_limit(unsigned polls);
  * kernels of other streams (the camera fit running concurrently with the rasterisation);
  * process-wide, read at each launch. */
 void vs_set_binning_ctas_per_sm(int ctas);
+/* Reserves up to `bytes` of L2 in the current context for persisting accesses
+ * (cudaLimitPersistingL2CacheSize, clamped to the device's maximum; the reservation ends
+ * with the context) and makes the point-binning launches of vs_proj_to_grid and
+ * vs_dsm_from_points* mark their key grid persisting with a per-launch access-policy
+ * window, so the streamed points cannot evict the grid the atomics update.  0 turns it off
+ * and releases the reservation.  Results are unchanged.  Process-wide, read at each
+ * launch; not thread-safe.  No counterpart in the reference. */
+int vs_set_l2_persisting(size_t bytes);
 
 /* Replaces RPCModel.inverse_projection (lib/rpc_model.py:170-249) for n_cams cameras:
  * (lon, lat) of image points (col, row) at altitudes alt, by the reference's iteration

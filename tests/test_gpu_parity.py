@@ -309,6 +309,39 @@ def test_dsm_from_points_pipelined_matches_serial_and_oracle(ctas):
         assert same_bits(pipe[v], ref), v
 
 
+def test_dsm_from_points_with_l2_persisting_key_grids():
+    """An L2 set-aside with persisting access-policy windows over the key grids
+    (vs_set_l2_persisting) leaves every DSM bit-identical: the serial, overlapped and
+    pipelined forms and proj_to_grid; a request above the device's maximum is clamped, and
+    0 releases the reservation."""
+    from vissatsatellitestereo_gb300 import _lib, synth
+    from vissatsatellitestereo_gb300.produce_dsm import dsm_from_points
+    from vissatsatellitestereo_gb300.proj_to_grid import proj_to_grid
+    grid = synth.DsmGrid(synth.EXPLORER_UL_EASTING, synth.EXPLORER_UL_NORTHING, 0.3, 0.3, 210, 190)
+    scene = synth.make_scene(85, grid, 25, 3.0, 80.0)
+    views = synth.make_views(86, scene, 4, 240, 280, 0.1, 0.3, 0.5)
+    clouds = [synth.view_points(scene, v) for v in views]
+    offsets = np.cumsum([0] + [len(c) for c in clouds])
+    pts = torch.from_numpy(np.concatenate(clouds)).cuda()
+    offs = torch.from_numpy(offsets).cuda()
+    args = (grid.xoff, grid.yoff, grid.xres, grid.yres, grid.xsize, grid.ysize)
+    ref = dsm_from_points(pts, offs, *args).cpu().numpy()
+    ref_grid = proj_to_grid(clouds[0], *args)
+    L = _lib.lib()
+    try:
+        assert L.vs_set_l2_persisting(64 << 20) == _lib.VS_OK, L.vs_last_error()
+        outs = [dsm_from_points(pts, offs, *args), dsm_from_points(pts, offs, *args, epilogue_stream=torch.cuda.Stream()),
+                dsm_from_points(pts, offs, *args, pipelined=True)]
+        got_grid = proj_to_grid(clouds[0], *args)
+        torch.cuda.synchronize()
+        assert L.vs_set_l2_persisting(1 << 40) == _lib.VS_OK, L.vs_last_error()      # clamped
+    finally:
+        assert L.vs_set_l2_persisting(0) == _lib.VS_OK, L.vs_last_error()
+    for o in outs:
+        assert same_bits(o.cpu().numpy(), ref)
+    assert same_bits(got_grid, ref_grid)
+
+
 @pytest.mark.parametrize('case', ['straddle', 'local_origin', 'single_view'])
 def test_dsm_from_points_pipelined_other_grids(case):
     """Grids outside the fast binning's precondition (a northing axis across 2^22, an origin

@@ -60,6 +60,7 @@ SIGNATURES = {
     'vs_map_upload': (_int, [_vp, _i64, _int, _int, _vp, _i64, _vp]),
     'vs_set_tc_wait_limit': (None, [ctypes.c_uint]),
     'vs_set_binning_ctas_per_sm': (None, [ctypes.c_int]),
+    'vs_set_l2_persisting': (_int, [_sz]),
     'vs_rpc_inverse_project_workspace_size': (_sz, [_int, _i64]),
     'vs_rpc_inverse_project': (_int, [_vp, _int, _vp, _vp, _vp, _i64, _i64, _int, _vp, _vp, _vp, _int, _vp, _vp, _sz,
                                       _vp]),

@@ -168,6 +168,15 @@ __device__ __forceinline__ df2 df_mul2(df2 a, df2 b, float2 nb_hi) {
     p.lo = __ffma2_rn(a.hi, b.lo, __ffma2_rn(a.lo, b.hi, p.lo));
     return fast_two_sum2(p.hi, p.lo);
 }
+// df_add per lane
+__device__ __forceinline__ df2 df_add2(df2 a, df2 b) {
+    df2 s = two_sum2(a.hi, b.hi);
+    const df2 t = two_sum2(a.lo, b.lo);
+    s.lo = __fadd2_rn(s.lo, t.hi);
+    s = fast_two_sum2(s.hi, s.lo);
+    s.lo = __fadd2_rn(s.lo, t.lo);
+    return fast_two_sum2(s.hi, s.lo);
+}
 // df_add_ops per lane
 __device__ __forceinline__ df2 df_add_ops2(df2 a, df2 b) {
     const df2 s = two_sum2(a.hi, b.hi);

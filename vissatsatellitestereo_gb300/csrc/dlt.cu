@@ -488,6 +488,7 @@ __device__ int factorize(double *P, double *K, double *R, double *t) {
 // (q = M p, rescaled) as double-floats, the normalisation, and K^-1.
 struct ErrCam {
     df q[12];
+    float2 q01_hi[4], q01_lo[4];   // rows 0 and 1 of q paired, for the packed dot products
     NormF nf;
     float qscale;      // q = qscale * M p
     float kinv[9];
@@ -521,6 +522,10 @@ __device__ void make_errcam(const double *K, const double *R, const double *t, c
     for (int i = 0; i < 12; ++i) mx = fmax(mx, fabs(q[i]));
     const double sc = (mx > 0.0 && isfinite(mx)) ? 1.0 / mx : 1.0;
     for (int i = 0; i < 12; ++i) ec.q[i] = df_from_double(q[i] * sc);
+    for (int j = 0; j < 4; ++j) {
+        ec.q01_hi[j] = make_float2(ec.q[j].hi, ec.q[4 + j].hi);
+        ec.q01_lo[j] = make_float2(ec.q[j].lo, ec.q[4 + j].lo);
+    }
     ec.qscale = static_cast<float>(sc);
     ec.nf = make_normf(nm);
     const double a = K[0], b = K[1], c = K[2], d = K[3], e = K[4], f = K[5], g = K[6], hh = K[7], i9 = K[8];
@@ -705,6 +710,25 @@ __device__ __forceinline__ df dot2(const df *q, float x, float y, float z) {
     return fast_two_sum(s.hi, err);
 }
 
+// dot2 for rows 0 and 1 of q at once (FP32x2 lanes; each lane performs dot2's operations)
+__device__ __forceinline__ df2 dot2_rows01(const ErrCam &ec, float x, float y, float z) {
+    const float2 X = f2s(x), Y = f2s(y), Z = f2s(z), nX = f2s(-x), nY = f2s(-y), nZ = f2s(-z);
+    const float2 h0 = ec.q01_hi[0], h1 = ec.q01_hi[1], h2 = ec.q01_hi[2];
+    const df2 p0 = {__fmul2_rn(h0, X), __ffma2_rn(h0, X, __fmul2_rn(h0, nX))};
+    const df2 p1 = {__fmul2_rn(h1, Y), __ffma2_rn(h1, Y, __fmul2_rn(h1, nY))};
+    const df2 p2 = {__fmul2_rn(h2, Z), __ffma2_rn(h2, Z, __fmul2_rn(h2, nZ))};
+    float2 err = __fadd2_rn(__fadd2_rn(__fadd2_rn(__ffma2_rn(ec.q01_lo[0], X, p0.lo), __ffma2_rn(ec.q01_lo[1], Y, p1.lo)),
+                                       __ffma2_rn(ec.q01_lo[2], Z, p2.lo)),
+                            ec.q01_lo[3]);
+    df2 s = two_sum2(p0.hi, p1.hi);
+    err = __fadd2_rn(err, s.lo);
+    s = two_sum2(s.hi, p2.hi);
+    err = __fadd2_rn(err, s.lo);
+    s = two_sum2(s.hi, ec.q01_hi[3]);
+    err = __fadd2_rn(err, s.lo);
+    return fast_two_sum2(s.hi, err);
+}
+
 // Per kept point: pixel reprojection error and metric inverse-projection error, written
 // as float bits for the median selection, plus block sums/maxima and the histogram of
 // the leading digit.
@@ -751,14 +775,19 @@ __global__ void __launch_bounds__(kErrThreads, 4) error_points_kernel(
             normalised_point(ec.nf, __ldg(reinterpret_cast<const long long *>(xv) + i),
                              __ldg(reinterpret_cast<const long long *>(yv) + i),
                              __ldg(reinterpret_cast<const long long *>(zv) + i), c, r, X, Y, Z, cf_, rf_);
-            const df h0 = dot2(ec.q, X, Y, Z), h1 = dot2(ec.q + 4, X, Y, Z), h2 = dot2(ec.q + 8, X, Y, Z);
+            // rows 0 and 1 of the camera (h0, h1) and the observations (c, r) travel as FP32x2
+            // pairs; every lane performs the scalar double-float operations
+            const df2 h01 = dot2_rows01(ec, X, Y, Z);
+            const df h2 = dot2(ec.q + 8, X, Y, Z);
             // observation in the normalised frame as a double-float: (c - c0) / sp
-            const df cn = df_mul(df_add(c, {-ec.nf.c0.hi, -ec.nf.c0.lo}), ec.nf.inv_sp);
-            const df rn = df_mul(df_add(r, {-ec.nf.r0.hi, -ec.nf.r0.lo}), ec.nf.inv_sp);
-            const df nc = df_add(h0, df_mul({-cn.hi, -cn.lo}, h2));
-            const df nr = df_add(h1, df_mul({-rn.hi, -rn.lo}, h2));
+            const df2 crn = df_mul2(df_add2({f2(c.hi, r.hi), f2(c.lo, r.lo)},
+                                            {f2(-ec.nf.c0.hi, -ec.nf.r0.hi), f2(-ec.nf.c0.lo, -ec.nf.r0.lo)}),
+                                    {f2s(ec.nf.inv_sp.hi), f2s(ec.nf.inv_sp.lo)}, f2s(-ec.nf.inv_sp.hi));
+            const df2 ncr = df_add2(h01, df_mul2({sub2(f2s(0.0f), crn.hi), sub2(f2s(0.0f), crn.lo)},
+                                                 {f2s(h2.hi), f2s(h2.lo)}, f2s(-h2.hi)));
             const float h2f = h2.hi + h2.lo;
-            const float dc = ec.nf.sp * ((nc.hi + nc.lo) / h2f), dr = ec.nf.sp * ((nr.hi + nr.lo) / h2f);
+            const float2 nsum = __fadd2_rn(ncr.hi, ncr.lo);
+            const float dc = ec.nf.sp * (nsum.x / h2f), dr = ec.nf.sp * (nsum.y / h2f);
             const float pe = sqrtf(__fmaf_rn(dr, dr, dc * dc));
             const float *ki = ec.kinv;
             const float cf = c.hi, rf = r.hi;

@@ -922,6 +922,38 @@ int make_tables(double xoff, double yoff, double xres, double yres, long long xs
 int g_bin_ctas_per_sm = 0;
 
 // Both axes on the contained fast path and 32-bit cell indices: bin_fast_kernel applies.
+// L2 set-aside for the key grids (vs_set_l2_persisting): bytes reserved in this context for
+// persisting accesses (0: off) and the device's largest access-policy window.
+size_t g_l2_persist = 0, g_l2_window_max = 0;
+
+// Launches `kernel` with an access-policy window that marks the key grid [base, base + bytes)
+// persisting in L2 -- the streamed points (evict-first loads) then cannot push the grid the
+// binning's atomics land in out of L2 -- when a set-aside is configured; otherwise a plain
+// launch.  The window is a per-launch attribute: the caller's stream keeps its own.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_with_key_window(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st,
+                                   const void *base, size_t bytes, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    if (g_l2_persist > 0 && base && bytes > 0) {
+        const size_t nb = std::min(bytes, g_l2_window_max);
+        attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[0].val.accessPolicyWindow.base_ptr = const_cast<void *>(base);
+        attr[0].val.accessPolicyWindow.num_bytes = nb;
+        attr[0].val.accessPolicyWindow.hitRatio =
+            nb <= g_l2_persist ? 1.0f : static_cast<float>(g_l2_persist) / static_cast<float>(nb);
+        attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 bool fast_binning(const Tables &tb) {
     return tb.row.fast && tb.row.contained && tb.col.fast && tb.col.contained && tb.row.n * tb.col.n < (1LL << 31);
 }
@@ -957,14 +989,12 @@ int bin_launch(const double *points, const long long *offsets, int v, long long 
         gx = static_cast<unsigned>(std::max<long long>(
             1LL, std::min<long long>(ceil_div(ceil_div(max_points, kFastPts), threads),
                                      static_cast<long long>(sm_count()) * per_sm)));
-        if (flip_row && !flip_col)
-            bin_fast_kernel<true, false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
-        else if (flip_row && flip_col)
-            bin_fast_kernel<true, true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
-        else if (!flip_row && !flip_col)
-            bin_fast_kernel<false, false><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
-        else
-            bin_fast_kernel<false, true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, fa[0], fa[1], keys, first);
+        const size_t key_bytes = sizeof(unsigned long long) * static_cast<size_t>(tb.row.n * tb.col.n);
+        auto kern = flip_row ? (flip_col ? bin_fast_kernel<true, true> : bin_fast_kernel<true, false>)
+                             : (flip_col ? bin_fast_kernel<false, true> : bin_fast_kernel<false, false>);
+        if (launch_with_key_window(kern, dim3(gx), dim3(threads), st, keys, key_bytes, points, offsets, v, single_n,
+                                   fa[0], fa[1], keys, first) != cudaSuccess)
+            return check_launch("bin_fast_kernel");
     } else {
         bin_max_kernel<true><<<gx, threads, 0, st>>>(points, offsets, v, single_n, tb, keys, first);
     }
@@ -1727,16 +1757,11 @@ extern "C" int vs_dsm_from_points_overlap(const double *points, const int64_t *o
 // One counter per launch (cleared once per call) hands out the work items.
 template <int MINB>
 static void launch_pipe(bool flip_row, bool flip_col, unsigned gx, cudaStream_t st, const double *points,
-                        const vs::PipeBin &b, const vs::PipeEpi &e, unsigned *counter) {
+                        const vs::PipeBin &b, const vs::PipeEpi &e, unsigned *counter, size_t key_bytes) {
     using namespace vs;
-    if (flip_row && !flip_col)
-        raster_pipe_kernel<true, false, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
-    else if (flip_row && flip_col)
-        raster_pipe_kernel<true, true, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
-    else if (!flip_row && !flip_col)
-        raster_pipe_kernel<false, false, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
-    else
-        raster_pipe_kernel<false, true, MINB><<<gx, dim3(TX, TY), 0, st>>>(points, b, e, counter);
+    auto kern = flip_row ? (flip_col ? raster_pipe_kernel<true, true, MINB> : raster_pipe_kernel<true, false, MINB>)
+                         : (flip_col ? raster_pipe_kernel<false, true, MINB> : raster_pipe_kernel<false, false, MINB>);
+    launch_with_key_window(kern, dim3(gx), dim3(TX, TY), st, b.keys, b.active ? key_bytes : 0, points, b, e, counter);
 }
 
 static size_t pipelined_counters_offset(int64_t xsize, int64_t ysize) {
@@ -1839,10 +1864,11 @@ extern "C" int vs_dsm_from_points_pipelined(const double *points, const int64_t 
             set_error("vs_dsm_from_points_pipelined: cudaEventRecord failed");
             return VS_ERR_CUDA;
         }
+        const size_t key_bytes = sizeof(unsigned long long) * static_cast<size_t>(cells);
         if (narrow)
-            launch_pipe<5>(flip_row, flip_col, gx, st, points, b, e, counters + v);
+            launch_pipe<5>(flip_row, flip_col, gx, st, points, b, e, counters + v, key_bytes);
         else
-            launch_pipe<6>(flip_row, flip_col, gx, st, points, b, e, counters + v);
+            launch_pipe<6>(flip_row, flip_col, gx, st, points, b, e, counters + v, key_bytes);
         VS_LAUNCH_CHECK("raster_pipe_kernel");
         if (launch_events && cudaEventRecord(static_cast<cudaEvent_t>(launch_events[2 * v + 1]), st) != cudaSuccess) {
             set_error("vs_dsm_from_points_pipelined: cudaEventRecord failed");
@@ -2344,6 +2370,29 @@ extern "C" int vs_dsm_from_depth_maps(const float *const *depths, const int64_t 
 }
 
 extern "C" void vs_set_binning_ctas_per_sm(int ctas) { vs::g_bin_ctas_per_sm = ctas > 0 ? ctas : 0; }
+
+extern "C" int vs_set_l2_persisting(size_t bytes) {
+    using namespace vs;
+    int dev = 0, maxp = 0, maxw = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess) {
+        set_error("vs_set_l2_persisting: device query failed");
+        return VS_ERR_CUDA;
+    }
+    const size_t want = std::min(bytes, static_cast<size_t>(std::max(maxp, 0)));
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+        set_error("vs_set_l2_persisting: cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, %zu) failed", want);
+        return VS_ERR_CUDA;
+    }
+    if (want == 0 && cudaCtxResetPersistingL2Cache() != cudaSuccess) {
+        set_error("vs_set_l2_persisting: cudaCtxResetPersistingL2Cache failed");
+        return VS_ERR_CUDA;
+    }
+    g_l2_persist = want;
+    g_l2_window_max = static_cast<size_t>(std::max(maxw, 0));
+    return VS_OK;
+}
 
 extern "C" int vs_map_upload(const float *host_heights, int64_t host_row_stride, int width, int height, float *heights,
                              int64_t row_stride, void *stream) {
