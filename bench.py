@@ -355,10 +355,10 @@ def run_ours(args):
     pipe_call_s = sum(pipe_ms) / 1e3 / alone_reps               # kernel time of one call
     pipe_bytes = wl.views * view_bytes                          # algorithmic bytes of one call
     pipe_gbs = pipe_bytes / pipe_call_s / 1e9
-    # DRAM traffic per launch from ncu: bin_fast_kernel on 4.19 M points moved 112.1 MB
-    # (read + write), i.e. 26.7 B per point, scaled by points; raster_pipe_kernel from its
-    # own capture (PIPE_TRAFFIC: bytes per point and per cell), scaled the same way
-    bin_traffic = int(26.73 * n_pts)
+    # DRAM traffic per launch from ncu: bin_fast_kernel on one full-size 4096^2 view moved
+    # 447.9 MB (read + write), i.e. 26.70 B per point; raster_pipe_kernel from its own
+    # capture (PIPE_TRAFFIC: bytes per point and per cell), scaled by points and cells
+    bin_traffic = int(26.70 * n_pts)
     timing = (f'CUDA events on the launching stream around each launch ({alone_reps} rasterisations of all '
               f'{wl.views} views on one stream, no concurrent work)')
     bin_alone = {'kernel': 'bin_fast_kernel (max-height binning of one view)', 'launch_ms': round(bin_s * 1e3, 4),
@@ -398,7 +398,8 @@ def run_ours(args):
                     'frac': round(bin_gbs / hbm_peak, 4), 'peak_source': peak_source,
                     'algorithmic_bytes_per_launch': bin_bytes, 'launch_ms': round(bin_s * 1e3, 4),
                     'timing': timing, 'traffic': bin_traffic,
-                    'traffic_source': 'ncu dram__bytes_read+write, 2048^2-point capture scaled',
+                    'traffic_source': 'ncu dram__bytes_read+write of one full-size 4096^2-point launch '
+                                      '(profiles/bin_fast_kernel_4096_view.md), per point',
                     'in_step': {'launch_ms': round(step_bin_s * 1e3, 4),
                                 'achieved': round(bin_bytes / step_bin_s / 1e9, 1),
                                 'frac': round(bin_bytes / step_bin_s / 1e9 / hbm_peak, 4),
