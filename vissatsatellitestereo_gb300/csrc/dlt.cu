@@ -79,7 +79,9 @@ struct Norm {
     double cx, cy, cz, s, c0, r0, sp;
 };
 
-constexpr int kBoxSamples = 65536;   // points sampled per view for the normalisation box
+// Points sampled per view for the normalisation box: each sample costs a DRAM sector per
+// coordinate array, and 8192 of them bound the data's extent well enough for scaling.
+constexpr int kBoxSamples = 8192;
 
 // Min/max of x, y, z (and col, row when given) over a strided sample of the kept points,
 // as order-preserving keys (the min through the complemented key).  Any centre and scale
@@ -189,17 +191,20 @@ constexpr int kSlots = 41;          // + kept-point count
 constexpr int kMomThreads = 128;
 constexpr int kChunk = 16;          // points per thread (FP32 partial sums)
 
-// Accumulates one point's 40 moment terms into FP32 partial sums.
-__device__ __forceinline__ void add_moments(float (&m)[kMom], float x, float y, float z, float c, float r) {
+// Accumulates one point's 40 moment terms into FP32 partial sums held as FP32x2 pairs:
+// ma[k] = (m[k], m[10 + k]) with weights (1, c), mb[k] = (m[20 + k], m[30 + k]) with
+// weights (r, c^2 + r^2) -- one FFMA2 per pair; 1 * e + m is exactly the plain sum, so
+// every lane rounds as the scalar accumulation does.
+__device__ __forceinline__ void add_moments(float2 (&ma)[10], float2 (&mb)[10], float x, float y, float z, float c,
+                                            float r) {
     const float xx = x * x, xy = x * y, xz = x * z, yy = y * y, yz = y * z, zz = z * z;
     const float e[10] = {xx, xy, xz, x, yy, yz, y, zz, z, 1.0f};
-    const float q = __fmaf_rn(c, c, r * r);
+    const float2 wa = make_float2(1.0f, c), wb = make_float2(r, __fmaf_rn(c, c, r * r));
 #pragma unroll
     for (int k = 0; k < 10; ++k) {
-        m[k] += e[k];
-        m[10 + k] = __fmaf_rn(c, e[k], m[10 + k]);
-        m[20 + k] = __fmaf_rn(r, e[k], m[20 + k]);
-        m[30 + k] = __fmaf_rn(q, e[k], m[30 + k]);
+        const float2 ek = make_float2(e[k], e[k]);
+        ma[k] = __ffma2_rn(wa, ek, ma[k]);
+        mb[k] = __ffma2_rn(wb, ek, mb[k]);
     }
 }
 
@@ -252,9 +257,9 @@ __global__ void __launch_bounds__(kMomThreads, 6) moments_kernel(
     const NormF nf = make_normf(norm[v]);
     const double *xv = x + v * xyz_stride, *yv = y + v * xyz_stride, *zv = z + v * xyz_stride;
     const float w = wh ? wh[2 * v] : 0.f, h = wh ? wh[2 * v + 1] : 0.f;
-    float m[kMom];
+    float2 ma[10], mb[10];
 #pragma unroll
-    for (int k = 0; k < kMom; ++k) m[k] = 0.0f;
+    for (int k = 0; k < 10; ++k) ma[k] = mb[k] = make_float2(0.0f, 0.0f);
     float count = 0.0f;
     const long long base = static_cast<long long>(blockIdx.x) * kMomThreads * kChunk + threadIdx.x;
     // groups of kAhead points: all loads of a group are issued before its arithmetic
@@ -293,9 +298,17 @@ __global__ void __launch_bounds__(kMomThreads, 6) moments_kernel(
             if (!ok[u]) continue;
             float px, py, pz, pc, pr;
             normalised_point(nf, X[u], Y[u], Z[u], c[u], r[u], px, py, pz, pc, pr);
-            add_moments(m, px, py, pz, pc, pr);
+            add_moments(ma, mb, px, py, pz, pc, pr);
             count += 1.0f;
         }
+    }
+    float m[kMom];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) {
+        m[k] = ma[k].x;
+        m[10 + k] = ma[k].y;
+        m[20 + k] = mb[k].x;
+        m[30 + k] = mb[k].y;
     }
     store_block_moments(m, count, partial + (static_cast<long long>(v) * gridDim.x + blockIdx.x) * kSlots, red);
 }
