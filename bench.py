@@ -482,9 +482,25 @@ def run_ours(args):
         h2d = (sum(v.numel() * v.element_size() for v in host.values()) + host_pts.numel() * 8 + host_off.numel() * 8
                + len(wl.metas) * _lib.CAMERA_DOUBLES * 8)
         d2h = out_fused.numel() * 4 + out_params.numel() * 8 + out_err.numel() * 8
+        # the host link on this machine: the same pinned point views copied to one device buffer
+        # (no compute), so the e2e step can be read against its copy-bound floor
+        link_views = min(10, wl.views)
+        link_buf = torch.empty((n_pts, 3), dtype=torch.float64, device=dev)
+        link_buf.copy_(host_pts[:n_pts], non_blocking=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for v in range(link_views):
+            link_buf.copy_(host_pts[v * n_pts:(v + 1) * n_pts], non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        link_gbs = link_views * n_pts * 24 / (e0.elapsed_time(e1) / 1e3) / 1e9
+        del link_buf
+        floor_ms = h2d / (link_gbs * 1e9) * 1e3
         result['e2e'] = {'value': wl.cells_per_step * e_steps / e_elapsed, 'unit': UNIT,
                          'ms_per_step': e_elapsed / e_steps * 1e3, 'steps': e_steps,
                          'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
+                         'host_link_gbs': round(link_gbs, 1), 'copy_floor_ms': round(floor_ms, 1),
+                         'frac_of_copy_floor': round(floor_ms / (e_elapsed / e_steps * 1e3), 3),
                          'api': 'approx_perspective_enu (inputs copied on its stream) + dsm_from_points on pinned host '
                                 'points (copied view by view under the binning) + fuse_dsms; results copied back'}
         del host_pts
