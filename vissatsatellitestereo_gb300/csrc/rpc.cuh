@@ -61,20 +61,12 @@ __device__ __forceinline__ void project_exact(const VsRpcCamera &cam, double lat
 }
 
 // ---- fast (double-float) ------------------------------------------------------------------
-// Integer -> float without the conversion instruction (it shares GB300's narrow FP64
-// pipe): 2^23 + u has u in its low mantissa bits for u < 2^23, so subtracting 2^23 is
-// exact; a 29-bit value is split into two such halves and rounded once by the final add.
-__device__ __forceinline__ float u23_to_float(unsigned u) {
-    return __fsub_rn(__uint_as_float(0x4b000000u | u), 8388608.0f);
-}
-__device__ __forceinline__ float u29_to_float(unsigned u) {
-    return __fadd_rn(__fmul_rn(u23_to_float(u >> 16), 65536.0f), u23_to_float(u & 0xffffu));
-}
-
-// Splits an FP64 value into hi + lo floats with integer operations only (no FP64 pipe):
-// hi keeps the top 24 significant bits (truncated, so the remainder is exact), lo is the
-// remaining 29 bits rounded to a float.  Magnitudes outside 2^+-100 (zero, tiny, huge,
-// inf, NaN) become the nearest float with lo = 0.
+// Splits an FP64 value into hi + lo floats without FP64 arithmetic: hi keeps the top 24
+// significant bits (truncated from the bit pattern, so the remainder is exact), lo is the
+// remaining 29 bits converted to a float (one rounding) and scaled by their power of two.
+// Magnitudes outside 2^+-100 (zero, tiny, huge, inf, NaN) become the nearest float with
+// lo = 0.  The integer conversion is one instruction (measured faster here than the
+// two-halves float trick it replaced, the fit 2.69 -> 2.64 ms).
 __device__ __forceinline__ df split_double(double v) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
     const int e = static_cast<int>((b >> 52) & 0x7ff);
@@ -85,7 +77,7 @@ __device__ __forceinline__ df split_double(double v) {
     const unsigned rest = static_cast<unsigned>(b & 0x1fffffffu);            // low 29 fraction bits
     // value of the low bits: rest * 2^(e - 1075); 2^(e-1075) = 2^(e-1023) * 2^-52
     const float scale = __uint_as_float(static_cast<unsigned>(e - 1023 - 52 + 127) << 23);
-    float lo = u29_to_float(rest) * scale;
+    float lo = __uint2float_rn(rest) * scale;
     lo = sign ? -lo : lo;
     return {hi, lo};
 }
