@@ -133,10 +133,29 @@ __device__ __forceinline__ double finite_or(double v, double fallback) {
     return (isfinite(v)) ? v : fallback;
 }
 
+// Per-view normalisation in the forms the per-point kernels use.
+struct NormF {
+    df cx, cy, cz, inv_s, c0, r0, inv_sp;
+    float sp;
+};
+
+__device__ __forceinline__ NormF make_normf(const Norm &nm) {
+    NormF f;
+    f.cx = df_from_double(nm.cx);
+    f.cy = df_from_double(nm.cy);
+    f.cz = df_from_double(nm.cz);
+    f.inv_s = df_from_double(1.0 / nm.s);
+    f.c0 = df_from_double(nm.c0);
+    f.r0 = df_from_double(nm.r0);
+    f.inv_sp = df_from_double(1.0 / nm.sp);
+    f.sp = static_cast<float>(nm.sp);
+    return f;
+}
+
 // Normalisation from the sampled boxes.  For the fused camera path the pixel frame is the
 // RPC's own (colOff/rowOff, larger scale).
 __global__ void norm_kernel(const unsigned long long *__restrict__ bb, const VsRpcCamera *__restrict__ cams,
-                            int n_views, Norm *__restrict__ norm) {
+                            int n_views, Norm *__restrict__ norm, NormF *__restrict__ normf) {
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n_views) return;
     const unsigned long long *b = bb + v * 10;
@@ -163,25 +182,7 @@ __global__ void norm_kernel(const unsigned long long *__restrict__ bb, const VsR
         nm.sp = (sp > 0.0 && isfinite(sp)) ? sp : 1.0;
     }
     norm[v] = nm;
-}
-
-// Per-view normalisation in the forms the per-point kernels use.
-struct NormF {
-    df cx, cy, cz, inv_s, c0, r0, inv_sp;
-    float sp;
-};
-
-__device__ __forceinline__ NormF make_normf(const Norm &nm) {
-    NormF f;
-    f.cx = df_from_double(nm.cx);
-    f.cy = df_from_double(nm.cy);
-    f.cz = df_from_double(nm.cz);
-    f.inv_s = df_from_double(1.0 / nm.s);
-    f.c0 = df_from_double(nm.c0);
-    f.r0 = df_from_double(nm.r0);
-    f.inv_sp = df_from_double(1.0 / nm.sp);
-    f.sp = static_cast<float>(nm.sp);
-    return f;
+    normf[v] = make_normf(nm);     // once per view: the per-point kernels read it (no FP64 there)
 }
 
 __device__ __forceinline__ df centre(df v, df off, df inv) { return df_mul(df_add(v, {-off.hi, -off.lo}), inv); }
@@ -250,11 +251,11 @@ __device__ __forceinline__ void normalised_point(const NormF &nf, long long X, l
 __global__ void __launch_bounds__(kMomThreads, 6) moments_kernel(
     const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z, long long xyz_stride,
     const double *__restrict__ col, const double *__restrict__ row, const float4 *__restrict__ colrow,
-    const uint8_t *__restrict__ keep, const float *__restrict__ wh, long long n, const Norm *__restrict__ norm,
+    const uint8_t *__restrict__ keep, const float *__restrict__ wh, long long n, const NormF *__restrict__ normf,
     double *__restrict__ partial) {
     __shared__ double red[(kMomThreads / 32) * kSlots];
     const int v = blockIdx.y;
-    const NormF nf = make_normf(norm[v]);
+    const NormF nf = normf[v];
     const double *xv = x + v * xyz_stride, *yv = y + v * xyz_stride, *zv = z + v * xyz_stride;
     const float w = wh ? wh[2 * v] : 0.f, h = wh ? wh[2 * v + 1] : 0.f;
     float2 ma[10], mb[10];
@@ -1039,6 +1040,7 @@ int box_blocks(long long n) {
 struct FitWs {
     unsigned long long *bb;
     Norm *norm;
+    NormF *normf;
     double *partial;
     ErrCam *errcam;
     float4 *colrow;
@@ -1050,6 +1052,7 @@ FitWs carve_fit(Carver &cv, int V, long long n, bool fused) {
     FitWs f;
     f.bb = cv.take<unsigned long long>(static_cast<size_t>(V) * 10);
     f.norm = cv.take<Norm>(V);
+    f.normf = cv.take<NormF>(V);
     f.partial = cv.take<double>(static_cast<size_t>(V) * mom_blocks(n) * kSlots);
     f.errcam = cv.take<ErrCam>(V);
     f.colrow = fused ? cv.take<float4>(static_cast<size_t>(V) * n) : nullptr;
@@ -1067,7 +1070,7 @@ int launch_norm(const double *x, const double *y, const double *z, long long xyz
         bbox_kernel<<<dim3(box_blocks(n), V), 256, 0, st>>>(x, y, z, xyz_stride, col, row, keep, n, box_step(n), f.bb);
         VS_LAUNCH_CHECK("bbox_kernel");
     }
-    norm_kernel<<<static_cast<unsigned>(ceil_div(V, 64)), 64, 0, st>>>(f.bb, cams, V, f.norm);
+    norm_kernel<<<static_cast<unsigned>(ceil_div(V, 64)), 64, 0, st>>>(f.bb, cams, V, f.norm, f.normf);
     VS_LAUNCH_CHECK("norm_kernel");
     return VS_OK;
 }
@@ -1121,7 +1124,7 @@ extern "C" int vs_dlt_fit(const double *x, const double *y, const double *z, int
     if (s != VS_OK) return s;
     const int blocks = mom_blocks(n);
     moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, xyz_stride, col, row, nullptr, keep,
-                                                                   nullptr, n, f.norm, f.partial);
+                                                                   nullptr, n, f.normf, f.partial);
     VS_LAUNCH_CHECK("moments_kernel");
     solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, nullptr, K, R, t, nullptr, nullptr, status);
     VS_LAUNCH_CHECK("solve_kernel");
@@ -1208,7 +1211,7 @@ extern "C" int vs_camera_approx_perspective(const VsRpcCamera *cams, int n_views
         VS_LAUNCH_CHECK("project_view_kernel");
     }
     moments_kernel<<<dim3(blocks, n_views), kMomThreads, 0, st>>>(x, y, z, point_stride, nullptr, nullptr, f.colrow,
-                                                                   nullptr, f.wh, n, f.norm, f.partial);
+                                                                   nullptr, f.wh, n, f.normf, f.partial);
     VS_LAUNCH_CHECK("moments_kernel");
     solve_kernel<<<n_views, 64, 0, st>>>(f.partial, blocks, f.norm, cams, K, R, t, params, f.errcam, status);
     VS_LAUNCH_CHECK("solve_kernel");
