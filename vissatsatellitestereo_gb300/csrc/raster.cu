@@ -1742,9 +1742,15 @@ extern "C" int vs_dsm_from_points_overlap(const double *points, const int64_t *o
             return VS_ERR_CUDA;
         if (!cuda_ok(cudaEventRecord(ev->bin[v % 3], st)) || !cuda_ok(cudaStreamWaitEvent(es, ev->bin[v % 3], 0)))
             return VS_ERR_CUDA;
+        // with an L2 set-aside the epilogue's clear of bin(v+2)'s grid is marked persisting:
+        // the zeros then stay in L2 while view v+1's points stream through, instead of being
+        // written back and fetched again by bin(v+2)'s first atomics
         unsigned long long *nxt = (v + 2 < n_views) ? w.keys[(v + 2) % 3] : nullptr;
-        dsm_epilogue_kernel<<<egrid, dim3(TX, TY), 0, es>>>(w.keys[v % 3], w.first[v & 1], points, dsm + v * cells, nxt,
-                                                            static_cast<int>(ysize), static_cast<int>(xsize));
+        const unsigned long long *cur = w.keys[v % 3], *fz = w.first[v & 1];
+        if (launch_with_key_window(dsm_epilogue_kernel, egrid, dim3(TX, TY), es, nxt,
+                                   nxt ? sizeof(unsigned long long) * static_cast<size_t>(cells) : 0, cur, fz, points,
+                                   dsm + v * cells, nxt, static_cast<int>(ysize), static_cast<int>(xsize)) != cudaSuccess)
+            return check_launch("dsm_epilogue_kernel");
         VS_LAUNCH_CHECK("dsm_epilogue_kernel");
         if (!cuda_ok(cudaEventRecord(ev->epi[v % 3], es))) return VS_ERR_CUDA;
     }
