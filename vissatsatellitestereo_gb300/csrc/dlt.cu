@@ -349,19 +349,40 @@ __global__ void __launch_bounds__(256) project_view_kernel(const VsRpcCamera *__
     }
     __syncthreads();
     const long long off = v * stride;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long step = static_cast<long long>(gridDim.x) * blockDim.x;
+    // the next point's coordinates (raw 64-bit patterns) are loaded before the current
+    // point's few hundred instructions, so their latency is hidden behind them
+    const long long *la = reinterpret_cast<const long long *>(lat + off);
+    const long long *lo = reinterpret_cast<const long long *>(lon + off);
+    const long long *al = reinterpret_cast<const long long *>(alt + off);
+    long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    long long a0 = 0, a1 = 0, a2 = 0;
+    if (i < n) {
+        a0 = __ldcs(la + i);
+        a1 = __ldcs(lo + i);
+        a2 = __ldcs(al + i);
+    }
+    for (; i < n; i += step) {
+        long long b0 = 0, b1 = 0, b2 = 0;
+        if (i + step < n) {
+            b0 = __ldcs(la + i + step);
+            b1 = __ldcs(lo + i + step);
+            b2 = __ldcs(al + i + step);
+        }
         df dc, dr;
         if (MODE == VS_PROJ_EXACT) {
             double cc, rr;
-            project_exact(cam, __ldcs(lat + off + i), __ldcs(lon + off + i), __ldcs(alt + off + i), cc, rr);
+            project_exact(cam, __longlong_as_double(a0), __longlong_as_double(a1), __longlong_as_double(a2), cc, rr);
             dc = split_double(cc);
             dr = split_double(rr);
         } else {
-            project_fast(fast, split_double(__ldcs(lat + off + i)), split_double(__ldcs(lon + off + i)),
-                         split_double(__ldcs(alt + off + i)), dc, dr);
+            project_fast(fast, split_double(__longlong_as_double(a0)), split_double(__longlong_as_double(a1)),
+                         split_double(__longlong_as_double(a2)), dc, dr);
         }
         colrow[static_cast<long long>(v) * n + i] = make_float4(dc.hi, dc.lo, dr.hi, dr.lo);
+        a0 = b0;
+        a1 = b1;
+        a2 = b2;
     }
 }
 
@@ -771,6 +792,11 @@ __global__ void __launch_bounds__(kErrThreads, 4) error_points_kernel(
     const double *xv = x + v * xyz_stride, *yv = y + v * xyz_stride, *zv = z + v * xyz_stride;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        // the point's coordinates are requested with its pixels, not after the in-image
+        // test on them: one memory round trip per point instead of two
+        const long long RX = __ldg(reinterpret_cast<const long long *>(xv) + i);
+        const long long RY = __ldg(reinterpret_cast<const long long *>(yv) + i);
+        const long long RZ = __ldg(reinterpret_cast<const long long *>(zv) + i);
         df c, r;
         bool k;
         if (colrow) {
@@ -786,9 +812,7 @@ __global__ void __launch_bounds__(kErrThreads, 4) error_points_kernel(
         unsigned pk = 0xffffffffu, ik = 0xffffffffu;
         if (k && ec.ok) {
             float X, Y, Z, cf_, rf_;
-            normalised_point(ec.nf, __ldg(reinterpret_cast<const long long *>(xv) + i),
-                             __ldg(reinterpret_cast<const long long *>(yv) + i),
-                             __ldg(reinterpret_cast<const long long *>(zv) + i), c, r, X, Y, Z, cf_, rf_);
+            normalised_point(ec.nf, RX, RY, RZ, c, r, X, Y, Z, cf_, rf_);
             // rows 0 and 1 of the camera (h0, h1) and the observations (c, r) travel as FP32x2
             // pairs; every lane performs the scalar double-float operations
             const df2 h01 = dot2_rows01(ec, X, Y, Z);
