@@ -121,7 +121,9 @@ void vs_set_binning_ctas_per_sm(int ctas);
  * (cudaLimitPersistingL2CacheSize, clamped to the device's maximum; the reservation ends
  * with the context) and makes the point-binning launches of vs_proj_to_grid and
  * vs_dsm_from_points* mark their key grid persisting with a per-launch access-policy
- * window, so the streamed points cannot evict the grid the atomics update.  0 turns it off
+ * window, so the streamed points cannot evict the grid the atomics update (in
+ * vs_dsm_from_points_overlap also the epilogue's clear of the grid two views ahead, so
+ * its zeros stay in L2 until that view's binning).  0 turns it off
  * and releases the reservation.  Results are unchanged.  Process-wide, read at each
  * launch; not thread-safe.  No counterpart in the reference. */
 int vs_set_l2_persisting(size_t bytes);
