@@ -212,16 +212,33 @@ __device__ __forceinline__ void add_moments(float2 (&ma)[10], float2 (&mb)[10], 
 // Warp sums in FP32, warps combined in FP64 in a fixed order (deterministic):
 // partial[kSlots] of this block.
 __device__ __forceinline__ void store_block_moments(float (&m)[kMom], float count, double *partial, double *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // moments 0..31: a reduce-scatter -- at the step of offset h a lane keeps the half of
+    // its remaining sums selected by lane bit h and adds its partner's copy of that half --
+    // so lane l ends with the warp sum of moment l after 31 shuffles instead of 160.  Each
+    // sum is formed as own + partner's at every step, as the butterfly below forms it, so
+    // the values are the butterfly's bit for bit.
 #pragma unroll
-    for (int k = 0; k < kMom; ++k)
+    for (int h = 16; h > 0; h >>= 1) {
+        const bool up = (lane & h) != 0;
+#pragma unroll
+        for (int j = 0; j < h; ++j) {
+            const float send = up ? m[j] : m[j + h];
+            const float keep = up ? m[j + h] : m[j];
+            m[j] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+        }
+    }
+    // moments 32..39 and the count: butterflies (every lane ends with the sum)
+#pragma unroll
+    for (int k = 32; k < kMom; ++k)
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) m[k] += __shfl_xor_sync(0xffffffffu, m[k], off);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) count += __shfl_xor_sync(0xffffffffu, count, off);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    red[warp * kSlots + lane] = f32_to_f64(m[0]);
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < kMom; ++k) red[warp * kSlots + k] = f32_to_f64(m[k]);
+        for (int k = 32; k < kMom; ++k) red[warp * kSlots + k] = f32_to_f64(m[k]);
         red[warp * kSlots + kMom] = f32_to_f64(count);
     }
     __syncthreads();
