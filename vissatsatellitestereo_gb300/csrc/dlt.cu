@@ -185,8 +185,6 @@ __global__ void norm_kernel(const unsigned long long *__restrict__ bb, const VsR
     normf[v] = make_normf(nm);     // once per view: the per-point kernels read it (no FP64 there)
 }
 
-__device__ __forceinline__ df centre(df v, df off, df inv) { return df_mul(df_add(v, {-off.hi, -off.lo}), inv); }
-
 constexpr int kMom = 40;            // 4 weights x 10 unique entries of X X^T
 constexpr int kSlots = 41;          // + kept-point count
 constexpr int kMomThreads = 128;
