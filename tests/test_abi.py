@@ -32,6 +32,39 @@ def test_library_exports_every_declared_symbol():
     assert lib.vs_version().decode().startswith('vissat-gb300')
 
 
+def header_declarations():
+    txt = open(os.path.join(ROOT, 'include', 'vissat_gb300.h')).read()
+    txt = re.sub(r'/\*.*?\*/', '', txt, flags=re.S)
+    txt = re.sub(r'//[^\n]*', '', txt)
+    out = {}
+    for name, params in re.findall(r'\b(vs_\w+)\s*\(([^;{}]*?)\)\s*;', txt):
+        out[name] = [p.strip() for p in params.split(',')] if params.strip() not in ('', 'void') else []
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every declared entry point's ctypes binding has the header's parameter count, a
+    pointer exactly where the header has one, and scalars of the header's width and kind."""
+    import ctypes
+    from vissatsatellitestereo_gb300 import _lib
+    scalars = {'int': ctypes.c_int, 'int32_t': ctypes.c_int32, 'int64_t': ctypes.c_int64, 'unsigned': ctypes.c_uint,
+               'size_t': ctypes.c_size_t, 'double': ctypes.c_double, 'float': ctypes.c_float}
+    decls = header_declarations()
+    assert len(decls) == len(header_symbols())
+    for name, params in decls.items():
+        _, args = _lib.SIGNATURES[name]
+        assert len(params) == len(args), name
+        for p, a in zip(params, args):
+            is_ptr = a in (ctypes.c_void_p, ctypes.c_char_p) or (isinstance(a, type) and issubclass(a, ctypes._Pointer))
+            assert ('*' in p) == is_ptr, (name, p, a)
+            if '*' in p:
+                continue
+            t = re.sub(r'\s+\w+$', '', p.replace('const ', '')).strip()
+            assert t in scalars, (name, p)
+            assert ctypes.sizeof(scalars[t]) == ctypes.sizeof(a), (name, p, a)
+            assert (t in ('double', 'float')) == (a in (ctypes.c_double, ctypes.c_float)), (name, p, a)
+
+
 def test_workspace_queries_need_no_gpu():
     from vissatsatellitestereo_gb300 import _lib
     lib = _lib.lib()
